@@ -1,0 +1,346 @@
+/*
+ * vsim.h -- C ABI of the GB300-native XPBD soft-body solver.
+ *
+ * This is the drop-in boundary for the solver/step interface of the
+ * visionary-sim kernel package. Every entry point below replaces one method
+ * of the reference's ES class `Simulator`
+ * (packages/visionary-sim/src/sim/simulator.js:35-518) or of the seams under
+ * it; the citation beside each names the exact method. A Node N-API shim (or
+ * any other FFI) binds these 1:1; see INTEGRATION.md for the bindings.
+ *
+ * Conventions
+ *   - Opaque handles, `int` status codes (VSIM_OK == 0), caller-owned output
+ *     buffers, no exceptions across the ABI.
+ *   - A handle is thread-compatible: calls on one handle must not overlap;
+ *     different handles may be used from different threads.
+ *   - Status codes map onto the reference's throws: VSIM_ERR_RANGE is its
+ *     `RangeError` (timing and material values, timestep.js:38-45,183-187,
+ *     material.js:80-85), VSIM_ERR_INVALID its `Error` (limits, a static
+ *     hold, kinematicDrive.js:158-160). `vsim_last_error()` returns the
+ *     message of the most recent failure on the calling thread.
+ *   - Node indices are the reference's: bodies are concatenated in scene
+ *     order, each body's nodes are its dense lattice grid
+ *     `i + nx * (j + ny * k)` (lattice.js:55-57, particles.js:55-65).
+ *   - Positions cross the ABI as xyzw float quadruples per node, w written as
+ *     0 on reads (state.wgsl:16-19, particles.js:227-231).
+ *   - All device work is issued on the handle's stream; calls that return
+ *     host data synchronise that stream.
+ */
+#ifndef VSIM_H
+#define VSIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VSIM_ABI_VERSION 1
+
+/* Status codes. */
+#define VSIM_OK 0
+#define VSIM_ERR_RANGE 1      /* a value outside its documented range (RangeError) */
+#define VSIM_ERR_INVALID 2    /* a request the simulator cannot honour (Error) */
+#define VSIM_ERR_CUDA 3       /* the CUDA runtime reported a failure */
+#define VSIM_ERR_NOMEM 4      /* device or host allocation failed, or a budget is full */
+#define VSIM_ERR_DESTROYED 5  /* the handle was already destroyed */
+#define VSIM_ERR_CAPACITY 6   /* a fixed-capacity buffer is too small */
+#define VSIM_ERR_TIMEOUT 7    /* a bounded device wait gave up */
+
+/* Drive laws (kinematicDrive.js:35, `DriveLaw`). */
+#define VSIM_DRIVE_HARD 0
+#define VSIM_DRIVE_COMPLIANT 1
+
+/* Nodes one hold can carry (kinematicDrive.js:49, MAX_DRIVEN). */
+#define VSIM_MAX_DRIVEN 4096
+
+/*
+ * A material, in the reference's units (material.js:11-28). Defaults are
+ * DEFAULT_MATERIAL (material.js:69-77): E 1.2e5 Pa, nu 0.40, rho 1000,
+ * friction 0.4, damping 0.6 /s, relaxation 0.012 s, maxStretch 0 (off).
+ */
+typedef struct vsim_material {
+    double youngs_modulus;  /* E, Pa; values below 1 are read as 1 (material.js:103) */
+    double poisson_ratio;   /* nu, clamped to [0.25, 0.49] (material.js:66,102) */
+    double density;         /* rho, kg/m^3 */
+    double friction;        /* Coulomb coefficient for the tank and contact */
+    double damping;         /* velocity drag, 1/s */
+    double relaxation;      /* Kelvin-Voigt relaxation time, s */
+    double max_stretch;     /* 0 (off) or a finite ratio > 1 (material.js:80-85) */
+} vsim_material;
+
+/*
+ * One soft body, given as the occupancy grid its voxeliser produced: the
+ * input `buildLattice(grid, {density})` takes (lattice.js:161-166). Cell
+ * (i, j, k) is occupancy[i + cx * (j + cy * k)] != 0. Nodes are the dense
+ * (cx+1)(cy+1)(cz+1) corner grid; node (i, j, k) rests at origin + (i, j, k) h.
+ */
+typedef struct vsim_body_desc {
+    uint32_t cell_dims[3];
+    double origin[3];
+    double h;                       /* cell edge, metres */
+    const uint8_t* occupancy;
+    vsim_material material;
+    const uint32_t* static_nodes;   /* body-local nodes held in place, or NULL
+                                       (staticPrescription.js:9-20) */
+    uint32_t static_count;
+} vsim_body_desc;
+
+/* Tank interior; the tank is open at the top (finalize.wgsl:61-67). */
+typedef struct vsim_tank {
+    double min[3];
+    double max[3];
+} vsim_tank;
+
+typedef struct vsim_sim vsim_sim;
+
+/* Simulator.stats() (simulator.js:194-230), the numeric part. */
+typedef struct vsim_stats {
+    uint32_t body_count;
+    uint32_t nodes;            /* dense node slots, inactive included */
+    uint32_t active_nodes;     /* nodes with material */
+    uint32_t cells;            /* occupied cells over all bodies */
+    uint32_t contact_nodes;    /* surface records */
+    int32_t contact;           /* body contact enabled */
+    int32_t self_contact;      /* same-body contact enabled (no reference counterpart) */
+    uint32_t iterations;       /* Gauss-Seidel sweeps per substep */
+    uint64_t steps;            /* total fixed steps taken */
+    uint32_t last_steps;       /* steps in the last frame */
+    uint32_t max_steps_per_frame;
+    double step_duration;      /* seconds per substep */
+    double simulated_time;
+    double backlog_time;
+    double frame_dropped_time;
+    double dropped_time;
+    int32_t overloaded;
+    double cfl;                /* wave rate x step duration (simulator.js:149-151) */
+    int32_t limited_by;        /* body index setting the CFL, -1 with no bodies */
+    uint32_t driven;           /* nodes currently held */
+    uint32_t drive_capacity;   /* VSIM_MAX_DRIVEN */
+} vsim_stats;
+
+/* ---- errors ---------------------------------------------------------- */
+
+/* Message of the last failure on this thread ("" if none). */
+const char* vsim_last_error(void);
+int vsim_abi_version(void);
+
+/* ---- lifecycle (simulator.js:44-115, :505-517) ----------------------- */
+
+/*
+ * `new Simulator(device, bodies, tank)`. Builds every lattice, uploads the
+ * node state and allocates everything the solver needs on the current CUDA
+ * device. On failure nothing is leaked (simulator.js:111-114).
+ * `stream` is a cudaStream_t to issue work on, or NULL for a stream the
+ * handle creates and owns.
+ */
+int vsim_create(const vsim_body_desc* bodies, uint32_t body_count,
+                const vsim_tank* tank, void* stream, vsim_sim** out);
+/* `destroy()`; idempotent on a NULL handle. */
+int vsim_destroy(vsim_sim* sim);
+
+/* ---- stepping (simulator.js:239-318, :495-500) ----------------------- */
+
+/* `step(dt)`: bank wall time on the fixed clock and dispatch its steps.
+   Non-finite or negative dt counts as 0 (simulator.js:256). */
+int vsim_step(vsim_sim* sim, double dt);
+/* `requestStep()`: the next vsim_step takes one step even when paused. */
+int vsim_request_step(vsim_sim* sim);
+/* `dispatch(steps)`: run `steps` fixed substeps now. */
+int vsim_dispatch(vsim_sim* sim, uint32_t steps);
+/* `reset()`: release the grab, return every node to rest, clear the clock. */
+int vsim_reset(vsim_sim* sim);
+/* Block until all work issued on the handle's stream has finished. */
+int vsim_synchronize(vsim_sim* sim);
+
+/* ---- state transfer (simulator.js:503, particles.js:227-231) --------- */
+
+/* `readPositions()`: xyzw per node, w = 0. `node_count` must equal the
+   simulator's node count. */
+int vsim_read_positions(vsim_sim* sim, float* xyzw, size_t node_count);
+/* Full state read/write (xyzw each; any pointer may be NULL). Used by
+   parity harnesses to start the solver and a reference from one state. */
+int vsim_read_state(vsim_sim* sim, float* pos, float* prev, float* vel, size_t node_count);
+int vsim_write_state(vsim_sim* sim, const float* pos, const float* prev, const float* vel,
+                     size_t node_count);
+uint32_t vsim_node_count(const vsim_sim* sim);
+/* Where body `b`'s nodes start (Particles.offsetOf, particles.js:119-121). */
+uint32_t vsim_body_node_offset(const vsim_sim* sim, uint32_t body);
+/* Material inverse mass per node (Particles.invMass), static nodes included. */
+int vsim_read_inv_mass(vsim_sim* sim, float* inv_mass, size_t node_count);
+
+/* ---- grab / drive (simulator.js:383-492, kinematicDrive.js:155-264) -- */
+
+/* KinematicDrive.hold(nodes, offsets): hold global nodes, offsets xyz per
+   node from the anchor. Holding a static node fails with VSIM_ERR_INVALID and
+   leaves the current hold unchanged; more than VSIM_MAX_DRIVEN keeps the
+   first VSIM_MAX_DRIVEN; an empty set releases. */
+int vsim_hold(vsim_sim* sim, const uint32_t* nodes, const float* offsets, uint32_t count);
+/* Simulator.moveGrab(position): the grab target; its velocity for a frame is
+   derived at dispatch from how far it moved (simulator.js:309-315). */
+int vsim_move_grab(vsim_sim* sim, const double position[3]);
+/* Place the grab target without implying motion (Simulator.grab's
+   `position = previousPosition = anchor`, simulator.js:419-422). */
+int vsim_place_grab(vsim_sim* sim, const double position[3]);
+/* Simulator.releaseGrab() / KinematicDrive.release(). */
+int vsim_release(vsim_sim* sim);
+/* Simulator.setDriveLaw(law). */
+int vsim_set_drive_law(vsim_sim* sim, int law);
+/* Simulator.setDriveResponseTime(seconds): finite and > 0, else RANGE. */
+int vsim_set_drive_response_time(vsim_sim* sim, double seconds);
+
+/* ---- settings (simulator.js:332-366) --------------------------------- */
+
+/* Bits of `fields` for vsim_set_material. */
+#define VSIM_MAT_YOUNGS     (1u << 0)
+#define VSIM_MAT_POISSON    (1u << 1)
+#define VSIM_MAT_DENSITY    (1u << 2)
+#define VSIM_MAT_FRICTION   (1u << 3)
+#define VSIM_MAT_DAMPING    (1u << 4)
+#define VSIM_MAT_RELAXATION (1u << 5)
+#define VSIM_MAT_MAX_STRETCH (1u << 6)
+/* Simulator.setMaterial(bodyIndex, changes): `fields` selects which members
+   of `changes` apply. Density rescales node masses; the step duration is
+   recomputed from the new wave rate. */
+int vsim_set_material(vsim_sim* sim, uint32_t body, const vsim_material* changes, uint32_t fields);
+/* Simulator.setContact(enabled). */
+int vsim_set_contact(vsim_sim* sim, int enabled);
+/* Same-body contact between nodes that share no cell. No counterpart in the
+   reference (its contact skips same-body pairs, collide.wgsl:66); off by
+   default. */
+int vsim_set_self_contact(vsim_sim* sim, int enabled);
+/* `params.gravity` (simulator.js:30-33). */
+int vsim_set_gravity(vsim_sim* sim, const double gravity[3]);
+/* `params.paused`. */
+int vsim_set_paused(vsim_sim* sim, int paused);
+/* Override the fixed step duration the clock chose from the CFL rule
+   (FixedTimestep.setStepDuration, timestep.js:56-59). RANGE unless finite
+   and > 0. */
+int vsim_set_step_duration(vsim_sim* sim, double seconds);
+/* Gauss-Seidel sweeps of the elastic colour passes per substep (1 in the
+   reference; each sweep restarts lambda at zero, xpbdCouple.wgsl:9-13). */
+int vsim_set_iterations(vsim_sim* sim, uint32_t iterations);
+/* Record each frame's substep sequence once as a CUDA graph and replay it
+   (default on). Off issues every kernel individually. */
+int vsim_set_graph(vsim_sim* sim, int enabled);
+/* Threads per block of the elastic colour pass (128, 256 or 512) and the
+   cell order inside each colour (0: lattice order, 4 or 8: bricks of that
+   many cells per axis). Chosen by vsim_tune; settable for sweeps. */
+int vsim_set_launch_shape(vsim_sim* sim, uint32_t block, uint32_t brick);
+/* Time every {brick 0,4,8} x {block 128,256,512} shape on `frames` frames of
+   the live state (which is saved and restored) and keep the fastest.
+   Writes the chosen shape to *block and *brick when non-NULL. */
+int vsim_tune(vsim_sim* sim, uint32_t frames, uint32_t* block, uint32_t* brick);
+
+/* Launch every substep kernel with programmatic dependent launch (default
+   on): the next kernel's launch overlaps the tail of the one before it. */
+int vsim_set_pdl(vsim_sim* sim, int enabled);
+
+/* ---- readout ---------------------------------------------------------- */
+
+/* The six Kuhn rest shape inverses of the unit cube the kernels use,
+   column-major 3x3 each (kuhn.js:78-80 as elasticCells.js:85-107 emits
+   them). */
+int vsim_kuhn_rest_inverse(float out[54]);
+
+/* Simulator.stats(). */
+int vsim_get_stats(vsim_sim* sim, vsim_stats* out);
+/* Simulator.cflNumber(). */
+int vsim_cfl_number(vsim_sim* sim, double* out);
+
+/*
+ * The contact pairs of the current positions: every pair of surface records
+ * (a < b) that the broadphase puts in neighbouring buckets (with the
+ * reference's 32-per-bucket visibility, contacts.wgsl:75), that the body rule
+ * admits and that overlap (distance < r_a + r_b). Written as (a, b) surface
+ * indices, in no particular order; *count receives the total even when it
+ * exceeds `capacity` (then VSIM_ERR_CAPACITY).
+ */
+int vsim_contact_pairs(vsim_sim* sim, uint32_t* pairs, size_t capacity, size_t* count);
+/* Surface record table (node, body) of the contact constraint
+   (bodyContact.js:325-340), `capacity` records at most. */
+int vsim_contact_surface(vsim_sim* sim, uint32_t* nodes, uint32_t* bodies, size_t capacity,
+                         size_t* count);
+
+/* ---- splats (sample.wgsl:40-80, covariance.wgsl:30-42) ---------------- */
+
+/*
+ * Bind Gaussian splats to body `body`'s lattice: rest means xyz, rotations
+ * xyzw, scales xyz (standard deviations), `count` splats. Replaces whatever
+ * was bound to that body. The embedding (cell and local coordinates,
+ * sample.wgsl:45-51) is computed here once.
+ */
+int vsim_splats_bind(vsim_sim* sim, uint32_t body, const float* means, const float* quats,
+                     const float* scales, uint32_t count);
+/* Total splats bound over all bodies. */
+uint32_t vsim_splats_count(const vsim_sim* sim);
+/* Deform every bound splat from the live node positions (device side):
+   mean' = x(rest) and covariance' = (F R S)(F R S)^T, and compute its depth
+   key along `view_dir` (larger depth sorts first: back to front). */
+int vsim_splats_deform(vsim_sim* sim, const float view_dir[3]);
+/* Stable radix sort of the depth keys: the draw order, back to front. */
+int vsim_splats_sort(vsim_sim* sim);
+/* Copy results to the host (any pointer may be NULL): means xyz, covariance
+   (xx, xy, xz, yy, yz, zz) and the draw order, splats in bind order (body
+   by body). */
+int vsim_splats_read(vsim_sim* sim, float* means, float* cov6, uint32_t* order, size_t count);
+
+/* ---- device radix sort -------------------------------------------------- */
+
+/*
+ * Stable LSD radix sort of `n` 32-bit keys in device memory (the splat depth
+ * sort's engine; PlayCanvas 2.21.3's GPU sorter is the reference's,
+ * apps/simulator/src/scene/app.js:71-75). Writes to `d_order` the
+ * permutation that sorts `d_keys` ascending, ties in index order; `d_keys`
+ * is not modified. Only the low `key_bits` bits take part (1..32).
+ * Scratch: call once with d_temp == NULL to receive the size in *temp_bytes.
+ */
+int vsim_radix_sort_u32(const uint32_t* d_keys, uint32_t* d_order, uint32_t n, uint32_t key_bits,
+                        void* d_temp, size_t* temp_bytes, void* stream);
+
+/* ---- fixed timestep clock (timestep.js:17-180), host only ------------- */
+
+typedef struct vsim_clock vsim_clock;
+typedef struct vsim_clock_report {
+    double step_duration;
+    uint32_t max_steps_per_frame;
+    uint32_t steps;
+    double elapsed;
+    uint64_t total_steps;
+    double simulated_time;
+    double backlog_time;
+    double frame_dropped_time;
+    double dropped_time;
+    int32_t overloaded;
+} vsim_clock_report;
+
+/* stableStepDuration(waveRate). RANGE for negative or non-finite rates. */
+int vsim_stable_step_duration(double wave_rate, double* out);
+/* new FixedTimestep(stepDuration, {maxStepsPerFrame}) (0 = 24). */
+int vsim_clock_create(double step_duration, uint32_t max_steps_per_frame, vsim_clock** out);
+int vsim_clock_destroy(vsim_clock* clock);
+int vsim_clock_consume(vsim_clock* clock, double elapsed, int force_step, vsim_clock_report* out);
+int vsim_clock_idle(vsim_clock* clock, vsim_clock_report* out);
+int vsim_clock_single_step(vsim_clock* clock, vsim_clock_report* out);
+int vsim_clock_set_step_duration(vsim_clock* clock, double step_duration);
+int vsim_clock_reset(vsim_clock* clock);
+int vsim_clock_snapshot(const vsim_clock* clock, vsim_clock_report* out);
+
+/* ---- material arithmetic (material.js:101-140, compliance.js:30-109) -- */
+
+/* Lame parameters after the reference's clamps. */
+int vsim_lame_parameters(const vsim_material* m, double* mu, double* lambda);
+/* Element compliances for a rest volume, and gamma = 1 + mu/lambda. */
+int vsim_element_compliance(const vsim_material* m, double rest_volume, double* deviatoric,
+                            double* hydrostatic, double* gamma);
+/* The collapse barrier of the stable Neo-Hookean energy under uniform scale. */
+double vsim_collapse_scale(double gamma);
+/* Longitudinal wave speed. */
+double vsim_wave_speed(const vsim_material* m);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VSIM_H */

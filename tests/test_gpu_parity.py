@@ -1,0 +1,319 @@
+"""GPU parity: libvsim's kernels against the float CPU oracle, through the C
+ABI, frame by frame from one shared state.
+
+The kernels evaluate every operation in the oracle's order with separately
+rounded multiplies and adds, so the expected agreement is exact equality
+(`==`: -0 and +0 compare equal). The configured tolerance -- 1e-5 relative,
+max_i |x_gpu - x_oracle| / max(|x_oracle|, L_body) -- is asserted as well, so
+a failure reports both how far apart and whether the bar itself is met.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def lib(vsimlib, gpu):
+    return vsimlib
+
+
+def rel_error(gpu_pos, ref_pos, scene):
+    """max_i |x_gpu - x_oracle| / max(|x_oracle|_inf, L_body), per body."""
+    worst = 0.0
+    at = 0
+    for b in scene.bodies:
+        n = b.node_count
+        g = gpu_pos[at:at + n, :3].astype(np.float64)
+        r = ref_pos[at:at + n, :3].astype(np.float64)
+        diag = float(np.linalg.norm(np.asarray(b.cell_dims) * b.h))
+        scale = max(float(np.max(np.abs(r))), diag)
+        worst = max(worst, float(np.max(np.abs(g - r))) / scale)
+        at += n
+    return worst
+
+
+def assert_same(sim, orc, scene, what=""):
+    gp, gq, gv = sim.read_state()
+    op, oq, ov = orc.state()
+    err = rel_error(gp, op, scene)
+    assert err <= TOL, f"{what}: relative position error {err:.3e}"
+    for name, g, o in (("pos", gp, op), ("prev", gq, oq), ("vel", gv, ov)):
+        bad = np.flatnonzero(np.any(g != o, axis=1))
+        assert bad.size == 0, (f"{what}: {name} differs at {bad.size} nodes, first {bad[:5]}, "
+                               f"max |diff| {np.max(np.abs(g - o)):.3e}")
+
+
+def make(scene):
+    import pyoracle
+    from vsim import Simulator
+
+    return Simulator(scene), pyoracle.Oracle(scene, 32)
+
+
+def test_single_box_frames_bit_exact(lib):
+    import vsim.scenes as sc
+
+    scene = sc.single_box()
+    sim, orc = make(scene)
+    assert np.array_equal(sim.inv_mass, orc.inv_mass())
+    for frame in range(40):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"frame {frame}")
+    sim.destroy()
+
+
+@pytest.mark.parametrize("graph,pdl", [(False, False), (False, True), (True, False)])
+def test_launch_modes_agree(lib, graph, pdl):
+    import vsim.scenes as sc
+
+    scene = sc.single_box()
+    sim, orc = make(scene)
+    sim.set_graph(graph)
+    sim.set_pdl(pdl)
+    for frame in range(5):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+    assert_same(sim, orc, scene, f"graph={graph} pdl={pdl}")
+
+
+def test_blob_contact_self_contact(lib):
+    import vsim.scenes as sc
+
+    scene = sc.noise_blob(n=16, seed=3, splats=0)
+    sim, orc = make(scene)
+    nodes_g, bodies_g = sim.contact_surface()
+    nodes_o, bodies_o = orc.surface()
+    assert np.array_equal(nodes_g, nodes_o) and np.array_equal(bodies_g, bodies_o)
+    for frame in range(20):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"frame {frame}")
+    assert sim.read_positions()[:, 1].min() > -0.01  # the ground held
+
+
+def squeeze(pos, scene, factor=0.6):
+    """A shared state with overlapping surfaces: every body squashed toward
+    its own bottom plane."""
+    out = pos.copy()
+    at = 0
+    for b in scene.bodies:
+        n = b.node_count
+        y0 = b.origin[1]
+        out[at:at + n, 1] = y0 + (out[at:at + n, 1] - y0) * factor
+        at += n
+    return out
+
+
+def test_contact_pairs_bit_exact(lib):
+    import vsim.scenes as sc
+
+    scene = sc.noise_blob(n=20, seed=5, splats=0)
+    sim, orc = make(scene)
+    pos, prev, vel = orc.state()
+    squashed = squeeze(pos, scene, 0.55)
+    for s in (sim, orc):
+        s.write_state(squashed, pos, vel) if s is sim else s.set_state(squashed, pos, vel)
+    gp = sim.contact_pairs()
+    op = orc.contact_pairs()
+    assert op.shape[0] > 100
+    assert np.array_equal(gp, op)
+    sim.dispatch(scene.substeps)
+    orc.dispatch(scene.substeps)
+    assert_same(sim, orc, scene, "after squeeze")
+
+
+def test_two_bodies_contact(lib):
+    """Inter-body contact as the reference has it: a box dropped on another."""
+    import vsim.scenes as sc
+
+    a = sc.Body((8, 4, 8), (0.0, 0.0, 0.0), sc.H, np.ones(256, np.uint8), dict(sc.DEFAULT_MATERIAL))
+    b = sc.Body((6, 4, 6), (0.01, 4 * sc.H + 0.004, 0.012), sc.H, np.ones(144, np.uint8),
+                dict(sc.DEFAULT_MATERIAL, density=600.0, friction=0.2))
+    scene = sc.Scene([a, b], ((-0.5, 0.0, -0.5), (0.5, 1.0, 0.5)), step_duration=1 / 1200, substeps=20)
+    sim, orc = make(scene)
+    pairs = sim.contact_pairs()
+    assert np.array_equal(pairs, orc.contact_pairs())
+    for frame in range(15):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"frame {frame}")
+    assert len(sim.contact_pairs()) > 0
+
+
+def test_box_batch_frames(lib):
+    import vsim.scenes as sc
+
+    scene = sc.box_batch(12, seed=7)
+    sim, orc = make(scene)
+    for frame in range(8):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"frame {frame}")
+
+
+def test_iterations_and_stretch(lib):
+    import vsim.scenes as sc
+
+    scene = sc.single_box()
+    scene.iterations = 2
+    scene.bodies[0].material["max_stretch"] = 1.05
+    sim, orc = make(scene)
+    for frame in range(10):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"frame {frame}")
+
+
+def grab_velocity(pos, prev_pos, steps, dt):
+    return [(pos[a] - prev_pos[a]) / (steps * dt) for a in range(3)]
+
+
+@pytest.mark.parametrize("law", ["hard", "compliant"])
+def test_drive_laws(lib, law):
+    import vsim.scenes as sc
+
+    scene = sc.single_box()
+    sim, orc = make(scene)
+    sim.set_drive_law(law)
+    orc.set_drive_law(law)
+    dims = scene.bodies[0].node_dims
+    tip = [sc.node_index(dims, 16, j, k) for j in range(5) for k in range(5)]
+    rest = sim.read_positions()
+    anchor = rest[tip[0], :3].astype(np.float64)
+    offsets = (rest[tip, :3] - rest[tip[0], :3]).astype(np.float32)
+    sim.hold(tip, offsets)
+    assert orc.hold(tip, offsets) == 0
+    sim.place_grab(anchor)
+    target = anchor.copy()
+    previous = anchor.copy()
+    dt = scene.step_duration
+    for frame in range(12):
+        target = target + np.array([0.0, 0.004, 0.002])
+        sim.move_grab(target)
+        orc.set_grab(target, grab_velocity(target, previous, scene.substeps, dt))
+        previous = target.copy()
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"{law} frame {frame}")
+    sim.release_grab()
+    orc.release()
+    for frame in range(4):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+    assert_same(sim, orc, scene, f"{law} after release")
+
+
+def test_errors_map_to_reference_throws(lib):
+    import vsim.scenes as sc
+    from vsim import VsimError, VsimRangeError
+
+    scene = sc.single_box()
+    sim, _ = make(scene)
+    with pytest.raises(VsimError) as info:
+        sim.hold([0], np.zeros((1, 3)))  # node 0 is on the pinned face
+    assert info.value.code == lib.VSIM_ERR_INVALID
+    with pytest.raises(VsimRangeError):
+        sim.set_drive_response_time(-1.0)
+    with pytest.raises(VsimRangeError):
+        sim.set_material(0, {"max_stretch": 0.5})
+    with pytest.raises(VsimError):
+        sim.set_drive_law("sticky")
+    sim.step(float("nan"))  # garbage dt is a frame of no time
+    assert sim.stats()["last_steps"] == 0
+
+
+def test_material_change_midrun(lib):
+    import vsim.scenes as sc
+
+    scene = sc.single_box()
+    sim, orc = make(scene)
+    for frame in range(3):
+        sim.dispatch(10)
+        orc.dispatch(10)
+    change = {"density": 1500.0, "youngs_modulus": 3e5, "damping": 1.0}
+    sim.set_material(0, change)
+    orc.set_material(0, change)
+    sim.set_step_duration(1 / 600)  # keep the fixed step of the workload
+    orc.set_step_duration(1 / 600)
+    assert np.array_equal(sim.inv_mass, orc.inv_mass())
+    for frame in range(5):
+        sim.dispatch(10)
+        orc.dispatch(10)
+        assert_same(sim, orc, scene, f"after change {frame}")
+
+
+def test_run_twice_identical(lib):
+    import vsim.scenes as sc
+
+    scene = sc.noise_blob(n=16, seed=11, splats=0)
+    out = []
+    for _ in range(2):
+        sim, _o = make(scene)
+        for _f in range(5):
+            sim.dispatch(scene.substeps)
+        out.append(sim.read_positions())
+        sim.destroy()
+    assert np.array_equal(out[0], out[1])
+
+
+def test_reset_and_step_clock(lib):
+    import vsim.scenes as sc
+
+    scene = sc.single_box()
+    sim, _ = make(scene)
+    rest = sim.read_positions()
+    sim.step(1 / 60)
+    st = sim.stats()
+    assert st["last_steps"] == 10 and abs(st["step_duration"] - 1 / 600) < 1e-15
+    assert not np.array_equal(sim.read_positions(), rest)
+    sim.reset()
+    assert np.array_equal(sim.read_positions(), rest)
+    assert sim.stats()["steps"] == 0
+
+
+def test_splats_and_sort(lib):
+    import pyoracle
+    import vsim.scenes as sc
+
+    scene = sc.noise_blob(n=16, seed=2, splats=20000)
+    sim, orc = make(scene)
+    for frame in range(3):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+    view = (0.3, -0.2, -0.93)
+    sim.deform_splats(view)
+    sim.sort_splats()
+    means, cov, order = sim.read_splats()
+    m, q, s, *_ = scene.splats[0]
+    om, oc, keys = orc.splat_deform(0, m, q, s, view)
+    assert np.array_equal(means, om)
+    assert np.array_equal(cov, oc)
+    assert np.array_equal(order, pyoracle.stable_sort(keys))
+
+
+@pytest.mark.parametrize("n,bits", [(1, 32), (4095, 32), (4097, 8), (1_000_003, 32), (300_000, 20)])
+def test_radix_sort_matches_stable_sort(lib, gpu, n, bits):
+    import torch
+    import pyoracle
+
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    keys[: n // 3] = keys[n // 2] if n > 2 else keys[: n // 3]  # many duplicates
+    dk = torch.from_numpy(keys.view(np.int32)).to(gpu)
+    do = torch.empty(n, dtype=torch.int32, device=gpu)
+    need = C.c_size_t()
+    L = lib.lib()
+    assert L.vsim_radix_sort_u32(dk.data_ptr(), do.data_ptr(), n, bits, None, C.byref(need), None) == 0
+    temp = torch.empty(need.value, dtype=torch.uint8, device=gpu)
+    stream = torch.cuda.current_stream().cuda_stream
+    assert L.vsim_radix_sort_u32(dk.data_ptr(), do.data_ptr(), n, bits, temp.data_ptr(), C.byref(need), stream) == 0
+    torch.cuda.synchronize()
+    got = do.cpu().numpy().view(np.uint32)
+    assert np.array_equal(got, pyoracle.stable_sort(keys, bits))
+    assert np.array_equal(dk.cpu().numpy().view(np.uint32), keys)  # input untouched

@@ -1,0 +1,93 @@
+// Declarations shared between the kernel files and the simulator object.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "vmath.cuh"
+#include "vsim_internal.h"
+
+namespace vsim {
+
+// Device buffers of one simulator, as the kernels see them.
+struct DeviceState {
+    float4* pos = nullptr;        // xyz position, w = inverse mass the solver uses
+    float4* prev = nullptr;       // position at the start of the substep
+    float4* vel = nullptr;
+    float* baseW = nullptr;       // material inverse mass with static nodes zeroed
+    uint32_t* active = nullptr;   // nodes with material that are not static
+    uint32_t* activeBody = nullptr;
+    uint2* cells = nullptr;       // colour-major (corner-0 node, body)
+    DevBody* bodies = nullptr;
+    FrameParams* fp = nullptr;
+    // contact
+    uint4* surf = nullptr;        // (node, body, packed rest coords, radius bits)
+    uint32_t* key = nullptr;
+    uint32_t* rank = nullptr;
+    uint32_t* entries = nullptr;
+    uint32_t* count = nullptr;    // per bucket
+    uint32_t* start = nullptr;    // per bucket
+    uint32_t* cursor = nullptr;
+    float4* delta = nullptr;
+    // drive
+    uint32_t* driven = nullptr;
+    float4* drivenOffset = nullptr;
+};
+
+struct LaunchCtx {
+    cudaStream_t stream;
+    bool pdl;
+};
+
+// Rest lengths of the cube's edges, face and body diagonals (stretch.js:5-7),
+// as f32; indexed by the number of axes the two corners differ in, minus one.
+struct StretchLengths {
+    float len[3];
+};
+
+enum class ContactMode { Solve, Pairs };
+
+void kuhnTable(float out[54]);
+
+cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount);
+cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drivenCount);
+cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint2* cells, uint32_t count,
+                          bool limitOnly, uint32_t block, const StretchLengths& lens);
+cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount);
+cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, uint32_t surfaceCount, ContactMode mode,
+                          uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount);
+cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos);
+cudaError_t launchZeroW(cudaStream_t st, const uint32_t* nodes, uint32_t n, float4* pos);
+cudaError_t launchRefreshW(cudaStream_t st, uint32_t first, uint32_t n, const float* base, float4* pos);
+cudaError_t launchMergeXyz(cudaStream_t st, const float4* in, uint32_t n, float4* pos);
+
+// ---- splats ---------------------------------------------------------------
+
+struct SplatBody {
+    uint32_t nx, nxy;
+    float inv;  // 1 / h
+    uint32_t pad;
+};
+
+struct SplatState {
+    float4* embed = nullptr;    // (u, v, w local coordinates, corner-0 node as bits)
+    float4* quat = nullptr;     // xyzw
+    float4* scaleBody = nullptr;  // (sx, sy, sz, body as bits)
+    SplatBody* bodies = nullptr;
+    float4* meanDepth = nullptr;  // deformed mean, depth along the view
+    float2* cov = nullptr;        // 3 x float2 per splat: (xx, xy), (xz, yy), (yz, zz)
+    uint32_t* keys = nullptr;
+    uint32_t* order = nullptr;
+    void* sortTemp = nullptr;
+    size_t sortTempBytes = 0;
+};
+
+cudaError_t launchSplatDeform(cudaStream_t st, const SplatState& s, const float4* pos, uint32_t n, float vx, float vy,
+                              float vz);
+
+// ---- radix sort -------------------------------------------------------------
+
+size_t radixSortTempBytes(uint32_t n);
+cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint32_t keyBits, void* temp,
+                         size_t tempBytes, cudaStream_t st);
+
+}  // namespace vsim

@@ -1,0 +1,1124 @@
+// The simulator object behind the C ABI: it owns every device buffer of a
+// scene, encodes a frame's substeps as kernel launches (captured once per
+// topology into a CUDA graph and replayed), and carries the host-side state
+// of the reference's Simulator (simulator.js:35-518): clock, grab, drive law,
+// materials.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <numeric>
+
+#include "kernels.cuh"
+
+using namespace vsim;
+
+namespace {
+
+
+// Restores the caller's current device when a call returns.
+struct DeviceGuard {
+    int previous = -1;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&previous) != cudaSuccess) previous = -1;
+        if (previous != device) cudaSetDevice(device);
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        if (previous >= 0 && cudaGetDevice(&now) == cudaSuccess && now != previous) cudaSetDevice(previous);
+    }
+};
+
+int cudaFail(cudaError_t e, const char* what) {
+    return fail(VSIM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                       \
+    do {                                                     \
+        cudaError_t _e = (expr);                             \
+        if (_e != cudaSuccess) return cudaFail(_e, what);    \
+    } while (0)
+
+template <class T>
+cudaError_t allocN(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    return cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+}
+
+__global__ void setParamsKernel(FrameParams* dst, FrameParams src) { *dst = src; }
+
+}  // namespace
+
+struct GraphEntry {
+    uint64_t key;
+    cudaGraphExec_t exec;
+};
+
+struct vsim_sim {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+    cudaStream_t capture = nullptr;
+
+    // topology
+    std::vector<Lattice> lat;
+    std::vector<vsim_material> mat;
+    std::vector<uint32_t> offsets;
+    std::vector<uint8_t> isStatic;
+    std::vector<float> invMass;  // material inverse mass (Particles.invMass)
+    std::vector<float> baseW;    // invMass with static nodes zeroed
+    std::vector<float> restPos;  // xyzw per node, w = baseW
+    uint32_t nodeCount = 0, activeCount = 0, cellCount = 0, surfaceCount = 0;
+    uint32_t colorStart[9] = {};
+    std::vector<uint4> surfHost;
+    vsim_tank tank{};
+    Grid grid{};
+
+    // settings
+    double gravity[3] = {0, -9.81, 0};
+    bool paused = false, pendingStep = false;
+    bool contact = true, selfContact = false;
+    uint32_t iterations = 1;
+    bool useGraph = true, pdl = true;
+    uint32_t block = 256, brick = 0;
+    Clock clock;
+    bool stepOverridden = false;
+
+    // drive
+    std::vector<uint32_t> held;
+    int law = VSIM_DRIVE_HARD;
+    double responseTime = kResponseTime;
+    double grabPos[3] = {0, 0, 0}, grabPrev[3] = {0, 0, 0};
+    double grabVel[3] = {0, 0, 0};
+
+    // device
+    DeviceState d;
+    float4* staging = nullptr;
+    uint32_t* pairs = nullptr;
+    size_t pairsCapacity = 0;
+    unsigned long long* pairCount = nullptr;
+    SplatState sp;
+    uint32_t splatCount = 0;
+    std::vector<std::vector<float>> splatMeans, splatQuats, splatScales;  // per body, host copies
+    FrameParams fpHost{};
+    bool paramsDirty = true, frameDirty = true;
+    std::vector<GraphEntry> graphs;
+};
+
+namespace {
+
+StretchLengths stretchLengths() {
+    StretchLengths s;
+    // stretch.js:5-7: Math.hypot of the corner offset, one to three unit axes.
+    s.len[0] = float(std::hypot(std::hypot(1.0, 0.0), 0.0));
+    s.len[1] = float(std::hypot(std::hypot(1.0, 1.0), 0.0));
+    s.len[2] = float(std::hypot(std::hypot(1.0, 1.0), 1.0));
+    return s;
+}
+
+bool anyStretch(const vsim_sim* s) {
+    for (const auto& m : s->mat)
+        if (m.max_stretch > 1) return true;
+    return false;
+}
+
+double waveRateOf(const vsim_sim* s, int* worst) {
+    // simulator.js:162-186: the body with the largest wave speed / cflLength
+    // (the cell edge, voxelLattice.js:63); the first of equals wins.
+    double best = 0;
+    int at = -1;
+    for (size_t b = 0; b < s->lat.size(); b++) {
+        const double rate = waveSpeed(s->mat[b]) / s->lat[b].h;
+        if (at < 0 || rate > best) {
+            best = rate;
+            at = int(b);
+        }
+    }
+    if (worst) *worst = at;
+    return at < 0 ? 0 : best;
+}
+
+// Per-body constants, in the order and precision project.wgsl:64-73 and
+// finalize.wgsl:71-72 derive them.
+void bodyParams(const vsim_sim* s, std::vector<DevBody>& out) {
+    const float dt = float(s->clock.stepDuration);
+    const float invDt2 = 1.0f / (dt * dt);
+    out.resize(s->lat.size());
+    for (size_t b = 0; b < s->lat.size(); b++) {
+        const Lattice& L = s->lat[b];
+        const vsim_material& m = s->mat[b];
+        double mu, lambda;
+        lame(m, mu, lambda);
+        const double volume = (1.0 / 6.0) * std::pow(L.h, 3.0);  // kuhn.js:48-50
+        const float alphaDev = float(1 / (mu * volume));         // compliance.js:30-37
+        const float alphaHyd = float(1 / (lambda * volume));
+        DevBody& d = out[b];
+        std::memset(&d, 0, sizeof d);
+        d.nodeOffset = s->offsets[b];
+        d.nx = L.nodeDims[0];
+        d.nxy = L.nodeDims[0] * L.nodeDims[1];
+        d.alphaDev = alphaDev * invDt2;
+        d.alphaHyd = alphaHyd * invDt2;
+        d.gamma = float(1 + mu / lambda);
+        d.relax = float(m.relaxation) / dt;
+        d.h = float(L.h);
+        d.restScale = 1.0f / d.h;
+        d.maxStretch = float(m.max_stretch);
+        d.friction = float(m.friction);
+        const float damping = float(m.damping);
+        const float arg = -damping * dt;
+        d.damp = float(std::exp(double(arg)));
+    }
+}
+
+void frameParams(vsim_sim* s) {
+    FrameParams& f = s->fpHost;
+    std::memset(&f, 0, sizeof f);
+    f.dt = float(s->clock.stepDuration);
+    f.gx = float(s->gravity[0]);
+    f.gy = float(s->gravity[1]);
+    f.gz = float(s->gravity[2]);
+    for (int a = 0; a < 3; a++) {
+        f.tankMin[a] = float(s->tank.min[a]);
+        f.tankMax[a] = float(s->tank.max[a]);
+        f.grabTarget[a] = float(s->grabPos[a]);
+        f.grabVelocity[a] = float(s->grabVel[a]);
+        f.gridOrigin[a] = float(s->grid.origin[a]);
+        f.gridDims[a] = s->grid.dims[a];
+    }
+    f.invDt2 = 1.0f / (f.dt * f.dt);
+    f.responseTime = float(s->responseTime);
+    f.drivenCount = uint32_t(s->held.size());
+    f.law = uint32_t(s->law);
+    f.bucket = float(s->grid.bucket);
+    f.surfaceCount = s->surfaceCount;
+    f.selfContact = s->selfContact ? 1u : 0u;
+    f.activeCount = s->activeCount;
+}
+
+// Uploads what changed since the last frame, in stream order.
+int syncParams(vsim_sim* s) {
+    if (s->paramsDirty) {
+        std::vector<DevBody> bodies;
+        bodyParams(s, bodies);
+        CK(cudaMemcpyAsync(s->d.bodies, bodies.data(), bodies.size() * sizeof(DevBody), cudaMemcpyHostToDevice,
+                           s->stream),
+           "upload body constants");
+        s->paramsDirty = false;
+        s->frameDirty = true;
+    }
+    if (s->frameDirty) {
+        frameParams(s);
+        setParamsKernel<<<1, 1, 0, s->stream>>>(s->d.fp, s->fpHost);
+        CK(cudaGetLastError(), "upload frame parameters");
+        s->frameDirty = false;
+    }
+    return VSIM_OK;
+}
+
+// The cell list, colour-major over bodies (elasticCells.js:143-163). Inside a
+// colour and body the cells run in lattice order, or brick by brick when
+// `brick` is 4 or 8 (bricks of that many cells per axis).
+void buildCells(vsim_sim* s, std::vector<uint2>& out) {
+    out.clear();
+    out.reserve(s->cellCount);
+    for (int c = 0; c < 8; c++) {
+        s->colorStart[c] = uint32_t(out.size());
+        for (size_t b = 0; b < s->lat.size(); b++) {
+            const Lattice& L = s->lat[b];
+            std::vector<uint32_t> order(L.cellsByColor[c]);
+            if (s->brick > 1) {
+                const uint32_t B = s->brick;
+                auto brickKey = [&](uint32_t cell) {
+                    const uint32_t i = cell % L.cellDims[0], j = (cell / L.cellDims[0]) % L.cellDims[1],
+                                   k = cell / (L.cellDims[0] * L.cellDims[1]);
+                    const uint32_t bx = (L.cellDims[0] + B - 1) / B, by = (L.cellDims[1] + B - 1) / B;
+                    return uint64_t((i / B) + bx * ((j / B) + by * (k / B))) << 32 | cell;
+                };
+                std::sort(order.begin(), order.end(),
+                          [&](uint32_t a, uint32_t bb) { return brickKey(a) < brickKey(bb); });
+            }
+            for (uint32_t cell : order) {
+                const uint32_t i = cell % L.cellDims[0], j = (cell / L.cellDims[0]) % L.cellDims[1],
+                               k = cell / (L.cellDims[0] * L.cellDims[1]);
+                out.push_back(make_uint2(s->offsets[b] + i + L.nodeDims[0] * (j + L.nodeDims[1] * k), uint32_t(b)));
+            }
+        }
+    }
+    s->colorStart[8] = uint32_t(out.size());
+}
+
+// stepper.js:101-108 with simulator.js:83's constraint order.
+cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMode mode = ContactMode::Solve) {
+    const LaunchCtx c{st, s->pdl};
+    const StretchLengths lens = stretchLengths();
+    const bool limited = anyStretch(s);
+    const bool driving = !s->held.empty();
+    const bool contact = s->contact && s->surfaceCount > 0;
+    cudaError_t e;
+    for (uint32_t step = 0; step < steps; step++) {
+        if ((e = launchPredict(c, s->d, s->activeCount))) return e;
+        if (driving && (e = launchDrive(c, s->d, VSIM_MAX_DRIVEN))) return e;
+        for (uint32_t it = 0; it < s->iterations; it++)
+            for (int col = 0; col < 8; col++) {
+                const uint32_t n = s->colorStart[col + 1] - s->colorStart[col];
+                if (n && (e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], n, false, s->block, lens))) return e;
+            }
+        if (limited)
+            for (int sweep = 0; sweep < 3; sweep++)
+                for (int col = 0; col < 8; col++) {
+                    const uint32_t n = s->colorStart[col + 1] - s->colorStart[col];
+                    if (n && (e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], n, true, s->block, lens)))
+                        return e;
+                }
+        if (contact && (e = launchContact(c, s->d, s->surfaceCount, mode, nullptr, 0, nullptr))) return e;
+        if ((e = launchFinalize(c, s->d, s->activeCount))) return e;
+    }
+    return cudaSuccess;
+}
+
+uint64_t graphKey(const vsim_sim* s, uint32_t steps) {
+    uint64_t k = steps;
+    k = k * 31 + (s->held.empty() ? 0 : 1);
+    k = k * 31 + ((s->contact && s->surfaceCount > 0) ? 1 : 0);
+    k = k * 31 + s->iterations;
+    k = k * 31 + (anyStretch(s) ? 1 : 0);
+    k = k * 1031 + s->block;
+    k = k * 31 + (s->pdl ? 1 : 0);
+    return k;
+}
+
+void dropGraphs(vsim_sim* s) {
+    for (auto& g : s->graphs) cudaGraphExecDestroy(g.exec);
+    s->graphs.clear();
+}
+
+int runFrame(vsim_sim* s, uint32_t steps) {
+    int rc = syncParams(s);
+    if (rc) return rc;
+    if (!s->useGraph) {
+        CK(encodeFrame(s, s->stream, steps), "launch substep");
+        return VSIM_OK;
+    }
+    const uint64_t key = graphKey(s, steps);
+    cudaGraphExec_t exec = nullptr;
+    for (auto& g : s->graphs)
+        if (g.key == key) exec = g.exec;
+    if (!exec) {
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal), "begin capture");
+        const cudaError_t enc = encodeFrame(s, s->capture, steps);
+        const cudaError_t end = cudaStreamEndCapture(s->capture, &graph);
+        if (enc != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return cudaFail(enc, "capture substep");
+        }
+        CK(end, "end capture");
+        const cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(inst, "instantiate frame graph");
+        if (s->graphs.size() >= 8) {
+            cudaGraphExecDestroy(s->graphs.front().exec);
+            s->graphs.erase(s->graphs.begin());
+        }
+        s->graphs.push_back({key, exec});
+    }
+    CK(cudaGraphLaunch(exec, s->stream), "launch frame graph");
+    return VSIM_OK;
+}
+
+void freeAll(vsim_sim* s) {
+    dropGraphs(s);
+    DeviceState& d = s->d;
+    void* ptrs[] = {d.pos, d.prev, d.vel, d.baseW, d.active, d.activeBody, d.cells, d.bodies, d.fp,
+                    d.surf, d.key, d.rank, d.entries, d.count, d.start, d.cursor, d.delta, d.driven,
+                    d.drivenOffset, s->staging, s->pairs, s->pairCount, s->sp.embed, s->sp.quat,
+                    s->sp.scaleBody, s->sp.bodies, s->sp.meanDepth, s->sp.cov, s->sp.keys, s->sp.order,
+                    s->sp.sortTemp};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (s->capture) cudaStreamDestroy(s->capture);
+    if (s->ownStream && s->stream) cudaStreamDestroy(s->stream);
+}
+
+int restoreHeld(vsim_sim* s) {
+    if (s->law == VSIM_DRIVE_HARD && !s->held.empty())
+        CK(launchRestoreW(s->stream, s->d.driven, uint32_t(s->held.size()), s->d.baseW, s->d.pos), "restore hold");
+    return VSIM_OK;
+}
+
+int zeroHeld(vsim_sim* s) {
+    if (s->law == VSIM_DRIVE_HARD && !s->held.empty())
+        CK(launchZeroW(s->stream, s->d.driven, uint32_t(s->held.size()), s->d.pos), "prescribe hold");
+    return VSIM_OK;
+}
+
+int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void* stream, vsim_sim* s) {
+    if (n > 0 && !bodies) return fail(VSIM_ERR_INVALID, "bodies is NULL");
+    CK(cudaGetDevice(&s->device), "query device");
+    int major = 0;
+    CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, s->device), "query device");
+    if (major < 10) return fail(VSIM_ERR_INVALID, "libvsim is built for sm_103a (GB300) only");
+    if (tank) {
+        s->tank = *tank;
+    } else {
+        for (int a = 0; a < 3; a++) {
+            s->tank.min[a] = -INFINITY;
+            s->tank.max[a] = INFINITY;
+        }
+    }
+    s->lat.resize(n);
+    s->mat.resize(n);
+    uint64_t total = 0;
+    for (uint32_t b = 0; b < n; b++) {
+        int rc = buildLattice(bodies[b], s->lat[b]);
+        if (rc) return rc;
+        s->mat[b] = bodies[b].material;
+        s->offsets.push_back(uint32_t(total));
+        total += s->lat[b].nodeCount;
+        if (total >= (1ull << 31)) return fail(VSIM_ERR_RANGE, "scene has too many nodes");
+    }
+    s->nodeCount = uint32_t(total);
+    s->isStatic.assign(total, 0);
+    s->invMass.assign(total, 0.0f);
+    for (uint32_t b = 0; b < n; b++) {
+        const Lattice& L = s->lat[b];
+        std::copy(L.invMass.begin(), L.invMass.end(), s->invMass.begin() + s->offsets[b]);
+        for (uint32_t i = 0; i < bodies[b].static_count; i++) {
+            const uint32_t node = bodies[b].static_nodes[i];
+            if (node >= L.nodeCount) return fail(VSIM_ERR_RANGE, "static node outside its body");
+            s->isStatic[s->offsets[b] + node] = 1;
+        }
+        s->cellCount += L.cellCount;
+    }
+    s->baseW.resize(total);
+    for (uint64_t i = 0; i < total; i++) s->baseW[i] = s->isStatic[i] ? 0.0f : s->invMass[i];
+
+    // Active nodes: material and not static (predict and finalize skip the rest).
+    std::vector<uint32_t> active, activeBody;
+    for (uint32_t b = 0; b < n; b++)
+        for (uint32_t m = 0; m < s->lat[b].nodeCount; m++) {
+            const uint32_t node = s->offsets[b] + m;
+            if (s->baseW[node] > 0) {
+                active.push_back(node);
+                activeBody.push_back(b);
+            }
+        }
+    s->activeCount = uint32_t(active.size());
+
+    // Surface records (bodyContact.js:325-340), radius h/2.
+    double widest = 0;
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t b = 0; b < n; b++) {
+        const Lattice& L = s->lat[b];
+        const float radius = float(L.h * kContactRadiusCells);
+        for (uint32_t node : L.surface) {
+            const uint32_t i = node % L.nodeDims[0], j = (node / L.nodeDims[0]) % L.nodeDims[1],
+                           k = node / (L.nodeDims[0] * L.nodeDims[1]);
+            uint32_t bits;
+            std::memcpy(&bits, &radius, 4);
+            const uint32_t coord = (i & 1023u) | ((j & 1023u) << 10) | ((k & 1023u) << 20);
+            s->surfHost.push_back(make_uint4(s->offsets[b] + node, b, coord, bits));
+            widest = std::max(widest, double(radius));
+        }
+        for (int a = 0; a < 3; a++) {
+            lo[a] = std::min(lo[a], L.origin[a]);
+            hi[a] = std::max(hi[a], L.origin[a] + L.cellDims[a] * L.h);
+        }
+    }
+    s->surfaceCount = uint32_t(s->surfHost.size());
+    s->grid = contactGrid(s->tank, widest, lo, hi);
+    if (double(s->grid.count()) > 4.0 * kGridLimit) return fail(VSIM_ERR_RANGE, "contact grid too large");
+
+    // Clock (simulator.js:88).
+    s->clock.stepDuration = stableStepDuration(waveRateOf(s, nullptr));
+    s->clock.reset();
+
+    // Streams.
+    if (stream) {
+        s->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "create stream");
+        s->ownStream = true;
+    }
+    CK(cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking), "create capture stream");
+
+    // Device buffers.
+    DeviceState& d = s->d;
+    const size_t N = s->nodeCount;
+    CK(allocN(&d.pos, N), "allocate positions");
+    CK(allocN(&d.prev, N), "allocate previous positions");
+    CK(allocN(&d.vel, N), "allocate velocities");
+    CK(allocN(&d.baseW, N), "allocate masses");
+    CK(allocN(&d.active, s->activeCount), "allocate active list");
+    CK(allocN(&d.activeBody, s->activeCount), "allocate active list");
+    CK(allocN(&d.cells, s->cellCount), "allocate cells");
+    CK(allocN(&d.bodies, n), "allocate body constants");
+    CK(allocN(&d.fp, 1), "allocate frame parameters");
+    CK(allocN(&d.surf, s->surfaceCount), "allocate surface");
+    CK(allocN(&d.key, s->surfaceCount), "allocate contact keys");
+    CK(allocN(&d.rank, s->surfaceCount), "allocate contact ranks");
+    CK(allocN(&d.entries, s->surfaceCount), "allocate contact entries");
+    CK(allocN(&d.delta, s->surfaceCount), "allocate contact deltas");
+    CK(allocN(&d.count, s->grid.count()), "allocate contact grid");
+    CK(allocN(&d.start, s->grid.count()), "allocate contact grid");
+    CK(allocN(&d.cursor, 1), "allocate contact cursor");
+    CK(allocN(&d.driven, VSIM_MAX_DRIVEN), "allocate drive");
+    CK(allocN(&d.drivenOffset, VSIM_MAX_DRIVEN), "allocate drive");
+    CK(allocN(&s->pairCount, 1), "allocate pair counter");
+
+    // Initial state (particles.js:67-102).
+    s->restPos.assign(4 * N, 0.0f);
+    for (uint32_t b = 0; b < n; b++) {
+        const Lattice& L = s->lat[b];
+        for (uint32_t m = 0; m < L.nodeCount; m++) {
+            const size_t node = s->offsets[b] + m;
+            s->restPos[4 * node] = L.rest[3 * m];
+            s->restPos[4 * node + 1] = L.rest[3 * m + 1];
+            s->restPos[4 * node + 2] = L.rest[3 * m + 2];
+            s->restPos[4 * node + 3] = s->baseW[node];
+        }
+    }
+    std::vector<uint2> cells;
+    buildCells(s, cells);
+    CK(cudaMemcpyAsync(d.pos, s->restPos.data(), N * 16, cudaMemcpyHostToDevice, s->stream), "upload state");
+    CK(cudaMemcpyAsync(d.prev, s->restPos.data(), N * 16, cudaMemcpyHostToDevice, s->stream), "upload state");
+    CK(cudaMemsetAsync(d.vel, 0, N * 16, s->stream), "upload state");
+    CK(cudaMemcpyAsync(d.baseW, s->baseW.data(), N * 4, cudaMemcpyHostToDevice, s->stream), "upload masses");
+    CK(cudaMemcpyAsync(d.active, active.data(), active.size() * 4, cudaMemcpyHostToDevice, s->stream), "upload");
+    CK(cudaMemcpyAsync(d.activeBody, activeBody.data(), activeBody.size() * 4, cudaMemcpyHostToDevice, s->stream),
+       "upload");
+    CK(cudaMemcpyAsync(d.cells, cells.data(), cells.size() * 8, cudaMemcpyHostToDevice, s->stream), "upload cells");
+    CK(cudaMemcpyAsync(d.surf, s->surfHost.data(), s->surfHost.size() * 16, cudaMemcpyHostToDevice, s->stream),
+       "upload surface");
+    CK(cudaMemsetAsync(d.count, 0, s->grid.count() * 4, s->stream), "clear grid");
+    CK(cudaMemsetAsync(d.cursor, 0, 4, s->stream), "clear grid");
+    s->paramsDirty = true;
+    int rc = syncParams(s);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream), "initialise");
+    s->splatMeans.resize(n);
+    s->splatQuats.resize(n);
+    s->splatScales.resize(n);
+    return VSIM_OK;
+}
+
+#define SIM_GUARD(s)                                                                  \
+    if (!(s)) return fail(VSIM_ERR_INVALID, "simulator handle is NULL");              \
+    DeviceGuard _guard((s)->device);                                                  \
+    clearError()
+
+}  // namespace
+
+extern "C" {
+
+int vsim_create(const vsim_body_desc* bodies, uint32_t body_count, const vsim_tank* tank, void* stream,
+                vsim_sim** out) {
+    clearError();
+    if (!out) return fail(VSIM_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    vsim_sim* s = new (std::nothrow) vsim_sim();
+    if (!s) return fail(VSIM_ERR_NOMEM, "out of host memory");
+    int rc;
+    try {
+        rc = create(bodies, body_count, tank, stream, s);
+    } catch (const std::bad_alloc&) {
+        rc = fail(VSIM_ERR_NOMEM, "out of host memory");
+    }
+    if (rc != VSIM_OK) {
+        freeAll(s);
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return VSIM_OK;
+}
+
+int vsim_destroy(vsim_sim* sim) {
+    if (!sim) return VSIM_OK;
+    {
+        DeviceGuard guard(sim->device);
+        cudaStreamSynchronize(sim->stream);
+        freeAll(sim);
+    }
+    delete sim;
+    return VSIM_OK;
+}
+
+int vsim_synchronize(vsim_sim* s) {
+    SIM_GUARD(s);
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    return VSIM_OK;
+}
+
+// simulator.js:292-318.
+int vsim_dispatch(vsim_sim* s, uint32_t steps) {
+    SIM_GUARD(s);
+    if (steps < 1 || s->nodeCount == 0) return VSIM_OK;
+    if (!s->held.empty()) {
+        const double frameDt = steps * s->clock.stepDuration;
+        for (int a = 0; a < 3; a++) s->grabVel[a] = (s->grabPos[a] - s->grabPrev[a]) / frameDt;
+        std::memcpy(s->grabPrev, s->grabPos, sizeof s->grabPos);
+        s->frameDirty = true;
+    }
+    return runFrame(s, steps);
+}
+
+// simulator.js:239-278.
+int vsim_step(vsim_sim* s, double dt) {
+    SIM_GUARD(s);
+    if (s->nodeCount == 0) {
+        s->pendingStep = false;
+        s->clock.idle();
+        return VSIM_OK;
+    }
+    const double elapsed = std::isfinite(dt) && dt >= 0 ? dt : 0;
+    const bool pending = s->pendingStep;
+    s->pendingStep = false;
+    if (s->paused) {
+        if (!pending) {
+            s->clock.idle();
+            return VSIM_OK;
+        }
+        s->clock.singleStep();
+    } else {
+        s->clock.consume(elapsed, pending);
+    }
+    return vsim_dispatch(s, s->clock.lastSteps);
+}
+
+int vsim_request_step(vsim_sim* s) {
+    SIM_GUARD(s);
+    s->pendingStep = true;
+    return VSIM_OK;
+}
+
+// simulator.js:495-500, particles.js:245-249.
+int vsim_reset(vsim_sim* s) {
+    SIM_GUARD(s);
+    int rc = vsim_release(s);
+    if (rc) return rc;
+    const size_t N = s->nodeCount;
+    CK(cudaMemcpyAsync(s->d.pos, s->restPos.data(), N * 16, cudaMemcpyHostToDevice, s->stream), "reset");
+    CK(cudaMemcpyAsync(s->d.prev, s->restPos.data(), N * 16, cudaMemcpyHostToDevice, s->stream), "reset");
+    CK(cudaMemsetAsync(s->d.vel, 0, N * 16, s->stream), "reset");
+    s->clock.reset();
+    s->pendingStep = false;
+    return VSIM_OK;
+}
+
+int vsim_read_positions(vsim_sim* s, float* xyzw, size_t node_count) {
+    return vsim_read_state(s, xyzw, nullptr, nullptr, node_count);
+}
+
+int vsim_read_state(vsim_sim* s, float* pos, float* prev, float* vel, size_t node_count) {
+    SIM_GUARD(s);
+    if (node_count != s->nodeCount) return fail(VSIM_ERR_CAPACITY, "node_count does not match the simulator");
+    float* out[3] = {pos, prev, vel};
+    const float4* from[3] = {s->d.pos, s->d.prev, s->d.vel};
+    for (int a = 0; a < 3; a++)
+        if (out[a])
+            CK(cudaMemcpyAsync(out[a], from[a], node_count * 16, cudaMemcpyDeviceToHost, s->stream), "read state");
+    CK(cudaStreamSynchronize(s->stream), "read state");
+    for (int a = 0; a < 3; a++)
+        if (out[a])
+            for (size_t n = 0; n < node_count; n++) out[a][4 * n + 3] = 0.0f;
+    return VSIM_OK;
+}
+
+int vsim_write_state(vsim_sim* s, const float* pos, const float* prev, const float* vel, size_t node_count) {
+    SIM_GUARD(s);
+    if (node_count != s->nodeCount) return fail(VSIM_ERR_CAPACITY, "node_count does not match the simulator");
+    if (pos) {
+        if (!s->staging) CK(allocN(&s->staging, s->nodeCount), "allocate staging");
+        CK(cudaMemcpyAsync(s->staging, pos, node_count * 16, cudaMemcpyHostToDevice, s->stream), "write state");
+        CK(launchMergeXyz(s->stream, s->staging, s->nodeCount, s->d.pos), "write state");
+    }
+    if (prev) CK(cudaMemcpyAsync(s->d.prev, prev, node_count * 16, cudaMemcpyHostToDevice, s->stream), "write state");
+    if (vel) CK(cudaMemcpyAsync(s->d.vel, vel, node_count * 16, cudaMemcpyHostToDevice, s->stream), "write state");
+    CK(cudaStreamSynchronize(s->stream), "write state");
+    return VSIM_OK;
+}
+
+uint32_t vsim_node_count(const vsim_sim* s) { return s ? s->nodeCount : 0; }
+
+uint32_t vsim_body_node_offset(const vsim_sim* s, uint32_t body) {
+    return s && body < s->offsets.size() ? s->offsets[body] : 0;
+}
+
+int vsim_read_inv_mass(vsim_sim* s, float* inv_mass, size_t node_count) {
+    SIM_GUARD(s);
+    if (node_count != s->nodeCount) return fail(VSIM_ERR_CAPACITY, "node_count does not match the simulator");
+    std::copy(s->invMass.begin(), s->invMass.end(), inv_mass);
+    return VSIM_OK;
+}
+
+// kinematicDrive.js:155-191.
+int vsim_hold(vsim_sim* s, const uint32_t* nodes, const float* offsets, uint32_t count) {
+    SIM_GUARD(s);
+    if (count > 0 && (!nodes || !offsets)) return fail(VSIM_ERR_INVALID, "nodes or offsets is NULL");
+    for (uint32_t i = 0; i < count; i++) {
+        if (nodes[i] >= s->nodeCount) return fail(VSIM_ERR_RANGE, "held node outside the scene");
+        if (s->isStatic[nodes[i]]) return fail(VSIM_ERR_INVALID, "[drive] cannot hold a static prescribed node");
+    }
+    if (count == 0) return vsim_release(s);
+    const uint32_t kept = std::min<uint32_t>(count, VSIM_MAX_DRIVEN);
+    int rc = restoreHeld(s);
+    if (rc) return rc;
+    std::vector<float4> off(kept);
+    for (uint32_t i = 0; i < kept; i++) off[i] = make_float4(offsets[3 * i], offsets[3 * i + 1], offsets[3 * i + 2], 0);
+    CK(cudaMemcpyAsync(s->d.driven, nodes, kept * 4, cudaMemcpyHostToDevice, s->stream), "upload hold");
+    CK(cudaMemcpyAsync(s->d.drivenOffset, off.data(), kept * 16, cudaMemcpyHostToDevice, s->stream), "upload hold");
+    s->held.assign(nodes, nodes + kept);
+    rc = zeroHeld(s);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream), "upload hold");
+    s->frameDirty = true;
+    return kept < count ? fail(VSIM_OK, "hold truncated to VSIM_MAX_DRIVEN nodes") : VSIM_OK;
+}
+
+int vsim_move_grab(vsim_sim* s, const double position[3]) {
+    SIM_GUARD(s);
+    std::memcpy(s->grabPos, position, sizeof s->grabPos);
+    s->frameDirty = true;
+    return VSIM_OK;
+}
+
+int vsim_place_grab(vsim_sim* s, const double position[3]) {
+    SIM_GUARD(s);
+    std::memcpy(s->grabPos, position, sizeof s->grabPos);
+    std::memcpy(s->grabPrev, position, sizeof s->grabPrev);
+    s->frameDirty = true;
+    return VSIM_OK;
+}
+
+int vsim_release(vsim_sim* s) {
+    SIM_GUARD(s);
+    int rc = restoreHeld(s);
+    if (rc) return rc;
+    s->held.clear();
+    s->frameDirty = true;
+    return VSIM_OK;
+}
+
+int vsim_set_drive_law(vsim_sim* s, int law) {
+    SIM_GUARD(s);
+    if (law != VSIM_DRIVE_HARD && law != VSIM_DRIVE_COMPLIANT) return fail(VSIM_ERR_INVALID, "[drive] unknown law");
+    if (law == s->law) return VSIM_OK;
+    int rc = restoreHeld(s);
+    if (rc) return rc;
+    s->law = law;
+    rc = zeroHeld(s);
+    if (rc) return rc;
+    s->frameDirty = true;
+    return VSIM_OK;
+}
+
+int vsim_set_drive_response_time(vsim_sim* s, double seconds) {
+    SIM_GUARD(s);
+    if (!std::isfinite(seconds) || seconds <= 0)
+        return fail(VSIM_ERR_RANGE, "drive responseTime must be a finite positive number of seconds");
+    s->responseTime = seconds;
+    s->frameDirty = true;
+    return VSIM_OK;
+}
+
+// simulator.js:332-353.
+int vsim_set_material(vsim_sim* s, uint32_t body, const vsim_material* m, uint32_t fields) {
+    SIM_GUARD(s);
+    if (!m) return fail(VSIM_ERR_INVALID, "changes is NULL");
+    if (body >= s->mat.size()) return fail(VSIM_ERR_RANGE, "body index out of range");
+    if ((fields & VSIM_MAT_MAX_STRETCH) && !validMaxStretch(m->max_stretch))
+        return fail(VSIM_ERR_RANGE, "maxStretch must be zero (disabled) or a finite ratio greater than one");
+    vsim_material& mat = s->mat[body];
+    if (fields & VSIM_MAT_YOUNGS) mat.youngs_modulus = m->youngs_modulus;
+    if (fields & VSIM_MAT_POISSON) mat.poisson_ratio = m->poisson_ratio;
+    if (fields & VSIM_MAT_FRICTION) mat.friction = m->friction;
+    if (fields & VSIM_MAT_DAMPING) mat.damping = m->damping;
+    if (fields & VSIM_MAT_RELAXATION) mat.relaxation = m->relaxation;
+    if (fields & VSIM_MAT_MAX_STRETCH) mat.max_stretch = m->max_stretch;
+    if ((fields & VSIM_MAT_DENSITY) && m->density > 0 && m->density != mat.density) {
+        // voxelLattice.js:188-195: node masses rescale in place.
+        const double ratio = mat.density / m->density;
+        const uint32_t first = s->offsets[body], count = s->lat[body].nodeCount;
+        for (uint32_t i = 0; i < count; i++) {
+            float& inv = s->invMass[first + i];
+            inv = float(double(inv) * ratio);
+            s->baseW[first + i] = s->isStatic[first + i] ? 0.0f : inv;
+            s->restPos[4 * size_t(first + i) + 3] = s->baseW[first + i];
+        }
+        mat.density = m->density;
+        CK(cudaMemcpyAsync(s->d.baseW + first, s->baseW.data() + first, count * 4, cudaMemcpyHostToDevice, s->stream),
+           "upload masses");
+        CK(launchRefreshW(s->stream, first, count, s->d.baseW, s->d.pos), "upload masses");
+        int rc = zeroHeld(s);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(s->stream), "upload masses");
+    }
+    if (!s->stepOverridden) s->clock.stepDuration = stableStepDuration(waveRateOf(s, nullptr));
+    s->paramsDirty = true;
+    return VSIM_OK;
+}
+
+int vsim_set_contact(vsim_sim* s, int enabled) {
+    SIM_GUARD(s);
+    s->contact = enabled != 0;
+    return VSIM_OK;
+}
+
+int vsim_set_self_contact(vsim_sim* s, int enabled) {
+    SIM_GUARD(s);
+    for (const Lattice& L : s->lat)
+        for (int a = 0; a < 3; a++)
+            if (enabled && L.nodeDims[a] > 1024) return fail(VSIM_ERR_RANGE, "self contact needs bodies of at most 1023 cells per axis");
+    s->selfContact = enabled != 0;
+    s->frameDirty = true;
+    return VSIM_OK;
+}
+
+int vsim_set_gravity(vsim_sim* s, const double g[3]) {
+    SIM_GUARD(s);
+    std::memcpy(s->gravity, g, sizeof s->gravity);
+    s->frameDirty = true;
+    return VSIM_OK;
+}
+
+int vsim_set_paused(vsim_sim* s, int paused) {
+    SIM_GUARD(s);
+    s->paused = paused != 0;
+    return VSIM_OK;
+}
+
+int vsim_set_step_duration(vsim_sim* s, double seconds) {
+    SIM_GUARD(s);
+    if (!std::isfinite(seconds) || seconds <= 0)
+        return fail(VSIM_ERR_RANGE, "stepDuration must be a finite positive number");
+    s->clock.stepDuration = seconds;
+    s->stepOverridden = true;
+    s->paramsDirty = true;
+    return VSIM_OK;
+}
+
+int vsim_set_iterations(vsim_sim* s, uint32_t iterations) {
+    SIM_GUARD(s);
+    if (iterations < 1 || iterations > 64) return fail(VSIM_ERR_RANGE, "iterations must be in [1, 64]");
+    s->iterations = iterations;
+    return VSIM_OK;
+}
+
+int vsim_set_graph(vsim_sim* s, int enabled) {
+    SIM_GUARD(s);
+    s->useGraph = enabled != 0;
+    return VSIM_OK;
+}
+
+int vsim_set_launch_shape(vsim_sim* s, uint32_t block, uint32_t brick) {
+    SIM_GUARD(s);
+    if (block != 128 && block != 256 && block != 512) return fail(VSIM_ERR_RANGE, "block must be 128, 256 or 512");
+    if (brick != 0 && brick != 4 && brick != 8) return fail(VSIM_ERR_RANGE, "brick must be 0, 4 or 8");
+    s->block = block;
+    if (brick != s->brick) {
+        s->brick = brick;
+        std::vector<uint2> cells;
+        buildCells(s, cells);
+        CK(cudaMemcpyAsync(s->d.cells, cells.data(), cells.size() * 8, cudaMemcpyHostToDevice, s->stream),
+           "upload cells");
+        CK(cudaStreamSynchronize(s->stream), "upload cells");
+    }
+    return VSIM_OK;
+}
+
+int vsim_tune(vsim_sim* s, uint32_t frames, uint32_t* block, uint32_t* brick) {
+    SIM_GUARD(s);
+    if (frames < 1) frames = 1;
+    const size_t N = s->nodeCount;
+    std::vector<float> saved(12 * N);
+    CK(cudaMemcpyAsync(saved.data(), s->d.pos, N * 16, cudaMemcpyDeviceToHost, s->stream), "tune");
+    CK(cudaMemcpyAsync(saved.data() + 4 * N, s->d.prev, N * 16, cudaMemcpyDeviceToHost, s->stream), "tune");
+    CK(cudaMemcpyAsync(saved.data() + 8 * N, s->d.vel, N * 16, cudaMemcpyDeviceToHost, s->stream), "tune");
+    CK(cudaStreamSynchronize(s->stream), "tune");
+    const uint32_t steps = std::max<uint32_t>(1, uint32_t(std::lround(1.0 / 60.0 / s->clock.stepDuration)));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "tune");
+    CK(cudaEventCreate(&e1), "tune");
+    float best = INFINITY;
+    uint32_t bestBlock = s->block, bestBrick = s->brick;
+    const uint32_t bricks[3] = {0, 4, 8}, blocksz[3] = {128, 256, 512};
+    for (uint32_t br : bricks)
+        for (uint32_t bl : blocksz) {
+            int rc = vsim_set_launch_shape(s, bl, br);
+            if (rc) return rc;
+            rc = runFrame(s, steps);  // warm-up and graph capture
+            if (rc) return rc;
+            CK(cudaEventRecord(e0, s->stream), "tune");
+            for (uint32_t f = 0; f < frames; f++) {
+                rc = runFrame(s, steps);
+                if (rc) return rc;
+            }
+            CK(cudaEventRecord(e1, s->stream), "tune");
+            CK(cudaEventSynchronize(e1), "tune");
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e0, e1), "tune");
+            if (ms < best) {
+                best = ms;
+                bestBlock = bl;
+                bestBrick = br;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int rc = vsim_set_launch_shape(s, bestBlock, bestBrick);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(s->d.pos, saved.data(), N * 16, cudaMemcpyHostToDevice, s->stream), "tune");
+    CK(cudaMemcpyAsync(s->d.prev, saved.data() + 4 * N, N * 16, cudaMemcpyHostToDevice, s->stream), "tune");
+    CK(cudaMemcpyAsync(s->d.vel, saved.data() + 8 * N, N * 16, cudaMemcpyHostToDevice, s->stream), "tune");
+    CK(cudaStreamSynchronize(s->stream), "tune");
+    if (block) *block = bestBlock;
+    if (brick) *brick = bestBrick;
+    return VSIM_OK;
+}
+
+int vsim_get_stats(vsim_sim* s, vsim_stats* o) {
+    SIM_GUARD(s);
+    if (!o) return fail(VSIM_ERR_INVALID, "out is NULL");
+    std::memset(o, 0, sizeof *o);
+    o->body_count = uint32_t(s->lat.size());
+    o->nodes = s->nodeCount;
+    uint32_t material = 0;
+    for (float m : s->invMass) material += m > 0 ? 1 : 0;
+    o->active_nodes = material;
+    o->cells = s->cellCount;
+    o->contact_nodes = s->surfaceCount;
+    o->contact = s->contact;
+    o->self_contact = s->selfContact;
+    o->iterations = s->iterations;
+    const vsim_clock_report r = s->clock.snapshot();
+    o->steps = r.total_steps;
+    o->last_steps = r.steps;
+    o->max_steps_per_frame = r.max_steps_per_frame;
+    o->step_duration = r.step_duration;
+    o->simulated_time = r.simulated_time;
+    o->backlog_time = r.backlog_time;
+    o->frame_dropped_time = r.frame_dropped_time;
+    o->dropped_time = r.dropped_time;
+    o->overloaded = r.overloaded;
+    int worst = -1;
+    o->cfl = waveRateOf(s, &worst) * s->clock.stepDuration;
+    o->limited_by = worst;
+    o->driven = uint32_t(s->held.size());
+    o->drive_capacity = VSIM_MAX_DRIVEN;
+    return VSIM_OK;
+}
+
+int vsim_cfl_number(vsim_sim* s, double* out) {
+    SIM_GUARD(s);
+    if (!out) return fail(VSIM_ERR_INVALID, "out is NULL");
+    *out = waveRateOf(s, nullptr) * s->clock.stepDuration;
+    return VSIM_OK;
+}
+
+int vsim_contact_pairs(vsim_sim* s, uint32_t* pairs, size_t capacity, size_t* count) {
+    SIM_GUARD(s);
+    if (!count) return fail(VSIM_ERR_INVALID, "count is NULL");
+    *count = 0;
+    if (s->surfaceCount == 0) return VSIM_OK;
+    if (capacity > s->pairsCapacity) {
+        if (s->pairs) cudaFree(s->pairs);
+        s->pairs = nullptr;
+        s->pairsCapacity = 0;
+        CK(allocN(&s->pairs, 2 * capacity), "allocate pairs");
+        s->pairsCapacity = capacity;
+    }
+    int rc = syncParams(s);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(s->pairCount, 0, sizeof(unsigned long long), s->stream), "count pairs");
+    const LaunchCtx c{s->stream, false};
+    CK(launchContact(c, s->d, s->surfaceCount, ContactMode::Pairs, s->pairs, uint32_t(capacity), s->pairCount),
+       "list pairs");
+    unsigned long long total = 0;
+    CK(cudaMemcpyAsync(&total, s->pairCount, sizeof total, cudaMemcpyDeviceToHost, s->stream), "count pairs");
+    CK(cudaStreamSynchronize(s->stream), "count pairs");
+    const size_t copied = std::min<size_t>(total, capacity);
+    if (copied && pairs)
+        CK(cudaMemcpy(pairs, s->pairs, copied * 8, cudaMemcpyDeviceToHost), "copy pairs");
+    *count = size_t(total);
+    return total > capacity ? fail(VSIM_ERR_CAPACITY, "pair buffer too small") : VSIM_OK;
+}
+
+int vsim_contact_surface(vsim_sim* s, uint32_t* nodes, uint32_t* bodies, size_t capacity, size_t* count) {
+    SIM_GUARD(s);
+    if (count) *count = s->surfaceCount;
+    const size_t n = std::min<size_t>(capacity, s->surfaceCount);
+    for (size_t i = 0; i < n; i++) {
+        if (nodes) nodes[i] = s->surfHost[i].x;
+        if (bodies) bodies[i] = s->surfHost[i].y;
+    }
+    return capacity < s->surfaceCount ? fail(VSIM_ERR_CAPACITY, "surface buffer too small") : VSIM_OK;
+}
+
+int vsim_kuhn_rest_inverse(float out[54]) {
+    if (!out) return fail(VSIM_ERR_INVALID, "out is NULL");
+    kuhnTable(out);
+    return VSIM_OK;
+}
+
+int vsim_set_pdl(vsim_sim* s, int enabled) {
+    SIM_GUARD(s);
+    s->pdl = enabled != 0;
+    return VSIM_OK;
+}
+
+// ---- splats -------------------------------------------------------------
+
+namespace {
+
+int rebuildSplats(vsim_sim* s) {
+    SplatState& sp = s->sp;
+    void* old[] = {sp.embed, sp.quat, sp.scaleBody, sp.bodies, sp.meanDepth, sp.cov, sp.keys, sp.order, sp.sortTemp};
+    CK(cudaStreamSynchronize(s->stream), "rebind splats");
+    for (void* p : old)
+        if (p) cudaFree(p);
+    sp = SplatState{};
+    size_t total = 0;
+    for (auto& m : s->splatMeans) total += m.size() / 3;
+    if (total >= (1ull << 31)) return fail(VSIM_ERR_RANGE, "too many splats");
+    s->splatCount = uint32_t(total);
+    const size_t n = total;
+    std::vector<float4> embed(n), quat(n), scaleBody(n);
+    std::vector<SplatBody> bodies(s->lat.size());
+    size_t at = 0;
+    for (size_t b = 0; b < s->lat.size(); b++) {
+        const Lattice& L = s->lat[b];
+        // sample.wgsl:40-51 in f32: the uniforms deformOrigin and deformH.
+        const float origin[3] = {float(L.origin[0]), float(L.origin[1]), float(L.origin[2])};
+        const float inv = 1.0f / float(L.h);
+        bodies[b] = SplatBody{L.nodeDims[0], L.nodeDims[0] * L.nodeDims[1], inv, 0};
+        const std::vector<float>& m = s->splatMeans[b];
+        const size_t count = m.size() / 3;
+        for (size_t i = 0; i < count; i++, at++) {
+            float local[3];
+            uint32_t base[3];
+            for (int a = 0; a < 3; a++) {
+                const float grid = (m[3 * i + a] - origin[a]) * inv;
+                const float cell = std::min(std::max(std::floor(grid), 0.0f), float(L.cellDims[a]) - 1.0f);
+                local[a] = grid - cell;
+                base[a] = uint32_t(cell);
+            }
+            const uint32_t node = s->offsets[b] + base[0] + L.nodeDims[0] * (base[1] + L.nodeDims[1] * base[2]);
+            float nodeBits, bodyBits;
+            std::memcpy(&nodeBits, &node, 4);
+            const uint32_t body = uint32_t(b);
+            std::memcpy(&bodyBits, &body, 4);
+            embed[at] = make_float4(local[0], local[1], local[2], nodeBits);
+            const std::vector<float>& q = s->splatQuats[b];
+            const std::vector<float>& sc = s->splatScales[b];
+            quat[at] = make_float4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
+            scaleBody[at] = make_float4(sc[3 * i], sc[3 * i + 1], sc[3 * i + 2], bodyBits);
+        }
+    }
+    if (n == 0) return VSIM_OK;
+    CK(allocN(&sp.embed, n), "allocate splats");
+    CK(allocN(&sp.quat, n), "allocate splats");
+    CK(allocN(&sp.scaleBody, n), "allocate splats");
+    CK(allocN(&sp.bodies, bodies.size()), "allocate splats");
+    CK(allocN(&sp.meanDepth, n), "allocate splats");
+    CK(allocN(&sp.cov, 3 * n), "allocate splats");
+    CK(allocN(&sp.keys, n), "allocate splats");
+    CK(allocN(&sp.order, n), "allocate splats");
+    sp.sortTempBytes = radixSortTempBytes(uint32_t(n));
+    CK(cudaMalloc(&sp.sortTemp, sp.sortTempBytes), "allocate sort scratch");
+    CK(cudaMemcpyAsync(sp.embed, embed.data(), n * 16, cudaMemcpyHostToDevice, s->stream), "upload splats");
+    CK(cudaMemcpyAsync(sp.quat, quat.data(), n * 16, cudaMemcpyHostToDevice, s->stream), "upload splats");
+    CK(cudaMemcpyAsync(sp.scaleBody, scaleBody.data(), n * 16, cudaMemcpyHostToDevice, s->stream), "upload splats");
+    CK(cudaMemcpyAsync(sp.bodies, bodies.data(), bodies.size() * sizeof(SplatBody), cudaMemcpyHostToDevice,
+                       s->stream),
+       "upload splats");
+    CK(cudaStreamSynchronize(s->stream), "upload splats");
+    return VSIM_OK;
+}
+
+}  // namespace
+
+int vsim_splats_bind(vsim_sim* s, uint32_t body, const float* means, const float* quats, const float* scales,
+                     uint32_t count) {
+    SIM_GUARD(s);
+    if (body >= s->lat.size()) return fail(VSIM_ERR_RANGE, "body index out of range");
+    if (count && (!means || !quats || !scales)) return fail(VSIM_ERR_INVALID, "splat arrays are NULL");
+    s->splatMeans[body].assign(means, means + 3 * size_t(count));
+    s->splatQuats[body].assign(quats, quats + 4 * size_t(count));
+    s->splatScales[body].assign(scales, scales + 3 * size_t(count));
+    return rebuildSplats(s);
+}
+
+uint32_t vsim_splats_count(const vsim_sim* s) { return s ? s->splatCount : 0; }
+
+int vsim_splats_deform(vsim_sim* s, const float view_dir[3]) {
+    SIM_GUARD(s);
+    if (!view_dir) return fail(VSIM_ERR_INVALID, "view_dir is NULL");
+    if (s->splatCount == 0) return VSIM_OK;
+    CK(launchSplatDeform(s->stream, s->sp, s->d.pos, s->splatCount, view_dir[0], view_dir[1], view_dir[2]),
+       "deform splats");
+    return VSIM_OK;
+}
+
+int vsim_splats_sort(vsim_sim* s) {
+    SIM_GUARD(s);
+    if (s->splatCount == 0) return VSIM_OK;
+    CK(radixSortU32(s->sp.keys, s->sp.order, s->splatCount, 32, s->sp.sortTemp, s->sp.sortTempBytes, s->stream),
+       "sort splats");
+    return VSIM_OK;
+}
+
+int vsim_splats_read(vsim_sim* s, float* means, float* cov6, uint32_t* order, size_t count) {
+    SIM_GUARD(s);
+    if (count != s->splatCount) return fail(VSIM_ERR_CAPACITY, "count does not match the bound splats");
+    if (count == 0) return VSIM_OK;
+    if (means || cov6) {
+        std::vector<float4> md(count);
+        std::vector<float2> cv(3 * count);
+        CK(cudaMemcpyAsync(md.data(), s->sp.meanDepth, count * 16, cudaMemcpyDeviceToHost, s->stream), "read splats");
+        CK(cudaMemcpyAsync(cv.data(), s->sp.cov, count * 24, cudaMemcpyDeviceToHost, s->stream), "read splats");
+        CK(cudaStreamSynchronize(s->stream), "read splats");
+        for (size_t i = 0; i < count; i++) {
+            if (means) {
+                means[3 * i] = md[i].x;
+                means[3 * i + 1] = md[i].y;
+                means[3 * i + 2] = md[i].z;
+            }
+            if (cov6) {
+                cov6[6 * i] = cv[3 * i].x;
+                cov6[6 * i + 1] = cv[3 * i].y;
+                cov6[6 * i + 2] = cv[3 * i + 1].x;
+                cov6[6 * i + 3] = cv[3 * i + 1].y;
+                cov6[6 * i + 4] = cv[3 * i + 2].x;
+                cov6[6 * i + 5] = cv[3 * i + 2].y;
+            }
+        }
+    }
+    if (order) {
+        CK(cudaMemcpyAsync(order, s->sp.order, count * 4, cudaMemcpyDeviceToHost, s->stream), "read order");
+        CK(cudaStreamSynchronize(s->stream), "read order");
+    }
+    return VSIM_OK;
+}
+
+int vsim_radix_sort_u32(const uint32_t* d_keys, uint32_t* d_order, uint32_t n, uint32_t key_bits, void* d_temp,
+                        size_t* temp_bytes, void* stream) {
+    clearError();
+    if (!temp_bytes) return fail(VSIM_ERR_INVALID, "temp_bytes is NULL");
+    if (key_bits < 1 || key_bits > 32) return fail(VSIM_ERR_RANGE, "key_bits must be in [1, 32]");
+    const size_t need = radixSortTempBytes(n);
+    if (!d_temp) {
+        *temp_bytes = need;
+        return VSIM_OK;
+    }
+    if (*temp_bytes < need) return fail(VSIM_ERR_CAPACITY, "scratch smaller than the size query returned");
+    if (n == 0) return VSIM_OK;
+    CK(radixSortU32(d_keys, d_order, n, key_bits, d_temp, *temp_bytes, static_cast<cudaStream_t>(stream)),
+       "radix sort");
+    return VSIM_OK;
+}
+
+}  // extern "C"

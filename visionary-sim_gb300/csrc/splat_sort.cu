@@ -1,0 +1,325 @@
+// Gaussian-splat deformation (sample.wgsl:40-80 with covariance.wgsl:18-42)
+// and the stable LSD radix sort behind the depth order.
+#include "kernels.cuh"
+
+namespace vsim {
+
+// ------------------------------------------------------------- splats --
+
+// Back-to-front draw key: ascending key order is descending depth.
+__device__ __forceinline__ uint32_t depthKey(float depth) {
+    const uint32_t bits = __float_as_uint(depth);
+    const uint32_t ordered = (bits & 0x80000000u) ? ~bits : (bits | 0x80000000u);
+    return ~ordered;
+}
+
+// One thread per splat: trilinear position and gradient F from the cell's
+// eight live nodes, then Sigma' = (F R S)(F R S)^T, then the depth key. The
+// embedding (cell corner node, local coordinates) was computed at bind time
+// with sample.wgsl:45-51's arithmetic.
+__global__ void __launch_bounds__(256) splatDeformKernel(const float4* __restrict__ embed,
+                                                         const float4* __restrict__ quat,
+                                                         const float4* __restrict__ scaleBody,
+                                                         const SplatBody* __restrict__ bodies,
+                                                         const float4* __restrict__ pos, uint32_t n, float vx,
+                                                         float vy, float vz, float4* __restrict__ meanDepth,
+                                                         float2* __restrict__ cov, uint32_t* __restrict__ keys,
+                                                         uint32_t* __restrict__ order) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 e = embed[i];
+    const float4 sb = scaleBody[i];
+    const SplatBody B = bodies[__float_as_uint(sb.w)];
+    const uint32_t node0 = __float_as_uint(e.w);
+    const float local[3] = {e.x, e.y, e.z};
+    const float inv = B.inv;
+    V position = mk(0.0f, 0.0f, 0.0f);
+    V col0 = mk(0.0f, 0.0f, 0.0f), col1 = col0, col2 = col0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const int cx = c & 1, cy = (c >> 1) & 1, cz = (c >> 2) & 1;
+        const float fx = cx ? local[0] : 1.0f - local[0];
+        const float fy = cy ? local[1] : 1.0f - local[1];
+        const float fz = cz ? local[2] : 1.0f - local[2];
+        const float dx = cx ? 1.0f : -1.0f, dy = cy ? 1.0f : -1.0f, dz = cz ? 1.0f : -1.0f;
+        const V p = xyz(pos[node0 + cx + B.nx * cy + B.nxy * cz]);
+        position = position + p * (fx * fy * fz);
+        const V g = mk(dx * fy * fz, dy * fx * fz, dz * fx * fy) * inv;
+        col0 = col0 + p * g.x;
+        col1 = col1 + p * g.y;
+        col2 = col2 + p * g.z;
+    }
+    const M F{{col0, col1, col2}};
+    const float4 q4 = quat[i];
+    const float x = q4.x, y = q4.y, z = q4.z, w = q4.w;
+    const V r0 = mk(1.0f - 2.0f * (y * y + z * z), 2.0f * (x * y + z * w), 2.0f * (x * z - y * w));
+    const V r1 = mk(2.0f * (x * y - z * w), 1.0f - 2.0f * (x * x + z * z), 2.0f * (y * z + x * w));
+    const V r2 = mk(2.0f * (x * z + y * w), 2.0f * (y * z - x * w), 1.0f - 2.0f * (x * x + y * y));
+    const V a0 = mul(F, r0) * sb.x;
+    const V a1 = mul(F, r1) * sb.y;
+    const V a2 = mul(F, r2) * sb.z;
+    // (A A^T)(row, col) = a0[row] a0[col] + a1[row] a1[col] + a2[row] a2[col].
+    const float xx = a0.x * a0.x + a1.x * a1.x + a2.x * a2.x;
+    const float xy = a0.y * a0.x + a1.y * a1.x + a2.y * a2.x;
+    const float xz = a0.z * a0.x + a1.z * a1.x + a2.z * a2.x;
+    const float yy = a0.y * a0.y + a1.y * a1.y + a2.y * a2.y;
+    const float yz = a0.z * a0.y + a1.z * a1.y + a2.z * a2.y;
+    const float zz = a0.z * a0.z + a1.z * a1.z + a2.z * a2.z;
+    const float depth = position.x * vx + position.y * vy + position.z * vz;
+    meanDepth[i] = make_float4(position.x, position.y, position.z, depth);
+    cov[3 * i] = make_float2(xx, xy);
+    cov[3 * i + 1] = make_float2(xz, yy);
+    cov[3 * i + 2] = make_float2(yz, zz);
+    keys[i] = depthKey(depth);
+    (void)order;
+}
+
+cudaError_t launchSplatDeform(cudaStream_t st, const SplatState& s, const float4* pos, uint32_t n, float vx, float vy,
+                              float vz) {
+    if (n == 0) return cudaSuccess;
+    splatDeformKernel<<<(n + 255) / 256, 256, 0, st>>>(s.embed, s.quat, s.scaleBody, s.bodies, pos, n, vx, vy, vz,
+                                                       s.meanDepth, s.cov, s.keys, s.order);
+    return cudaGetLastError();
+}
+
+// --------------------------------------------------------- radix sort --
+//
+// Least-significant-digit radix sort, 8-bit digits, reduce-then-scan per
+// pass (no waits between blocks): a per-tile digit histogram, one
+// device-wide exclusive scan of the (digit, tile) counts, then a scatter in
+// which every warp ranks its 512 consecutive keys with __match_any_sync,
+// the block stages the tile in shared memory in digit order, and the tile
+// is written out in runs that are contiguous per digit. Tiles and ranks
+// follow input order, so each pass -- and the sort -- is stable.
+
+constexpr uint32_t kSortThreads = 256;
+constexpr uint32_t kSortItems = 16;
+constexpr uint32_t kSortTile = kSortThreads * kSortItems;  // 4096 keys
+constexpr uint32_t kWarps = kSortThreads / 32;
+constexpr uint32_t kScanChunk = 4096;  // elements per block of the scan
+constexpr uint32_t kScanMaxChunks = 4096;
+
+namespace {
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+inline uint32_t tilesOf(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
+}  // namespace
+
+size_t radixSortTempBytes(uint32_t n) {
+    const size_t tiles = tilesOf(n);
+    return 4 * align256(size_t(n) * 4) + align256(256 * tiles * 4) + align256(kScanMaxChunks * 4);
+}
+
+__global__ void __launch_bounds__(kSortThreads) sortHistKernel(const uint32_t* __restrict__ keys, uint32_t n,
+                                                               uint32_t shift, uint32_t mask, uint32_t tiles,
+                                                               uint32_t* __restrict__ hist) {
+    __shared__ uint32_t bins[256];
+    bins[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kSortTile;
+#pragma unroll
+    for (uint32_t r = 0; r < kSortItems; r++) {
+        const uint32_t idx = base + r * kSortThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&bins[(keys[idx] >> shift) & mask], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * tiles + blockIdx.x] = bins[threadIdx.x];
+}
+
+// Block-wide exclusive scan of one value per thread (256 threads); returns
+// the block total through `total`.
+__device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* warpSums, uint32_t& total) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= uint32_t(d)) incl += u;
+    }
+    if (lane == 31) warpSums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t s = lane < kWarps ? warpSums[lane] : 0;
+        uint32_t sc = s;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, sc, d);
+            if (lane >= uint32_t(d)) sc += u;
+        }
+        if (lane < kWarps) warpSums[lane] = sc - s;
+        if (lane == kWarps - 1) warpSums[kWarps] = sc;
+    }
+    __syncthreads();
+    total = warpSums[kWarps];
+    const uint32_t out = warpSums[warp] + incl - v;
+    __syncthreads();
+    return out;
+}
+
+// Scan, level 1: each block sums its chunk.
+__global__ void __launch_bounds__(kSortThreads) scanReduceKernel(const uint32_t* __restrict__ in, uint32_t n,
+                                                                 uint32_t* __restrict__ partial) {
+    __shared__ uint32_t warpSums[kWarps + 1];
+    const uint32_t base = blockIdx.x * kScanChunk;
+    uint32_t sum = 0;
+    for (uint32_t r = 0; r < kScanChunk / kSortThreads; r++) {
+        const uint32_t idx = base + r * kSortThreads + threadIdx.x;
+        if (idx < n) sum += in[idx];
+    }
+    uint32_t total;
+    blockExclusiveScan(sum, warpSums, total);
+    if (threadIdx.x == 0) partial[blockIdx.x] = total;
+}
+
+// Scan, level 2: one block scans the chunk sums (at most kScanMaxChunks).
+__global__ void __launch_bounds__(kSortThreads) scanPartialKernel(uint32_t* __restrict__ partial, uint32_t chunks) {
+    __shared__ uint32_t warpSums[kWarps + 1];
+    constexpr uint32_t per = kScanMaxChunks / kSortThreads;
+    uint32_t v[per];
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < per; i++) {
+        const uint32_t idx = threadIdx.x * per + i;
+        v[i] = idx < chunks ? partial[idx] : 0;
+        sum += v[i];
+    }
+    uint32_t total;
+    uint32_t run = blockExclusiveScan(sum, warpSums, total);
+#pragma unroll
+    for (uint32_t i = 0; i < per; i++) {
+        const uint32_t idx = threadIdx.x * per + i;
+        if (idx < chunks) partial[idx] = run;
+        run += v[i];
+    }
+}
+
+// Scan, level 3: each block scans its chunk from its offset, in place.
+__global__ void __launch_bounds__(kSortThreads) scanDownKernel(uint32_t* __restrict__ data, uint32_t n,
+                                                               const uint32_t* __restrict__ partial) {
+    __shared__ uint32_t warpSums[kWarps + 1];
+    constexpr uint32_t per = kScanChunk / kSortThreads;
+    const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * per;
+    uint32_t v[per];
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < per; i++) {
+        v[i] = base + i < n ? data[base + i] : 0;
+        sum += v[i];
+    }
+    uint32_t total;
+    uint32_t run = blockExclusiveScan(sum, warpSums, total) + partial[blockIdx.x];
+#pragma unroll
+    for (uint32_t i = 0; i < per; i++) {
+        if (base + i < n) data[base + i] = run;
+        run += v[i];
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) sortScatterKernel(const uint32_t* __restrict__ keysIn,
+                                                                  const uint32_t* __restrict__ valsIn, uint32_t n,
+                                                                  uint32_t shift, uint32_t mask, uint32_t tiles,
+                                                                  const uint32_t* __restrict__ offsets,
+                                                                  uint32_t* __restrict__ keysOut,
+                                                                  uint32_t* __restrict__ valsOut) {
+    __shared__ uint32_t sKeys[kSortTile];
+    __shared__ uint32_t sVals[kSortTile];
+    __shared__ uint32_t warpHist[kWarps][256];
+    __shared__ uint32_t digitStart[256];
+    __shared__ uint32_t globalStart[256];
+    __shared__ uint32_t warpSums[kWarps + 1];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t i = threadIdx.x; i < kWarps * 256; i += kSortThreads) (&warpHist[0][0])[i] = 0;
+    __syncthreads();
+
+    const uint32_t tileBase = blockIdx.x * kSortTile;
+    const uint32_t warpBase = tileBase + warp * 32 * kSortItems;
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+#pragma unroll
+    for (uint32_t r = 0; r < kSortItems; r++) {
+        const uint32_t idx = warpBase + r * 32 + lane;
+        const bool valid = idx < n;
+        key[r] = valid ? keysIn[idx] : 0u;
+        val[r] = valid ? (valsIn ? valsIn[idx] : idx) : 0u;
+        const uint32_t digit = valid ? (key[r] >> shift) & mask : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        const uint32_t before = valid ? warpHist[warp][digit] : 0u;
+        __syncwarp();
+        if (valid && (peers & lt) == 0) warpHist[warp][digit] = before + __popc(peers);
+        __syncwarp();
+        rank[r] = before + __popc(peers & lt);
+    }
+    __syncthreads();
+    // Per digit: exclusive prefix over warps, then over digits.
+    {
+        const uint32_t d = threadIdx.x;
+        uint32_t running = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < kWarps; w++) {
+            const uint32_t c = warpHist[w][d];
+            warpHist[w][d] = running;
+            running += c;
+        }
+        uint32_t total;
+        digitStart[d] = blockExclusiveScan(running, warpSums, total);
+        globalStart[d] = offsets[d * tiles + blockIdx.x];
+    }
+    __syncthreads();
+#pragma unroll
+    for (uint32_t r = 0; r < kSortItems; r++) {
+        const uint32_t idx = warpBase + r * 32 + lane;
+        if (idx < n) {
+            const uint32_t digit = (key[r] >> shift) & mask;
+            const uint32_t slot = digitStart[digit] + warpHist[warp][digit] + rank[r];
+            sKeys[slot] = key[r];
+            sVals[slot] = val[r];
+        }
+    }
+    __syncthreads();
+    const uint32_t count = n - tileBase < kSortTile ? n - tileBase : kSortTile;
+    for (uint32_t j = threadIdx.x; j < count; j += kSortThreads) {
+        const uint32_t k = sKeys[j];
+        const uint32_t digit = (k >> shift) & mask;
+        const uint32_t out = globalStart[digit] + (j - digitStart[digit]);
+        if (keysOut) keysOut[out] = k;
+        valsOut[out] = sVals[j];
+    }
+}
+
+cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint32_t keyBits, void* temp,
+                         size_t tempBytes, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    if (tempBytes < radixSortTempBytes(n)) return cudaErrorInvalidValue;
+    const uint32_t tiles = tilesOf(n);
+    const uint32_t histCount = 256 * tiles;
+    const uint32_t chunks = (histCount + kScanChunk - 1) / kScanChunk;
+    if (chunks > kScanMaxChunks) return cudaErrorInvalidValue;
+    char* p = static_cast<char*>(temp);
+    const size_t vec = align256(size_t(n) * 4);
+    uint32_t* keysA = reinterpret_cast<uint32_t*>(p);
+    uint32_t* keysB = reinterpret_cast<uint32_t*>(p + vec);
+    uint32_t* valsA = reinterpret_cast<uint32_t*>(p + 2 * vec);
+    uint32_t* valsB = reinterpret_cast<uint32_t*>(p + 3 * vec);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(p + 4 * vec);
+    uint32_t* partial = reinterpret_cast<uint32_t*>(p + 4 * vec + align256(size_t(histCount) * 4));
+    const uint32_t passes = (keyBits + 7) / 8;
+    const uint32_t* kin = keys;
+    const uint32_t* vin = nullptr;
+    for (uint32_t pass = 0; pass < passes; pass++) {
+        const uint32_t shift = 8 * pass;
+        const uint32_t bits = keyBits - shift < 8 ? keyBits - shift : 8;
+        const uint32_t mask = (1u << bits) - 1u;
+        const bool last = pass + 1 == passes;
+        uint32_t* kout = last ? nullptr : (pass % 2 == 0 ? keysA : keysB);
+        uint32_t* vout = last ? order : (pass % 2 == 0 ? valsA : valsB);
+        sortHistKernel<<<tiles, kSortThreads, 0, st>>>(kin, n, shift, mask, tiles, hist);
+        scanReduceKernel<<<chunks, kSortThreads, 0, st>>>(hist, histCount, partial);
+        scanPartialKernel<<<1, kSortThreads, 0, st>>>(partial, chunks);
+        scanDownKernel<<<chunks, kSortThreads, 0, st>>>(hist, histCount, partial);
+        sortScatterKernel<<<tiles, kSortThreads, 0, st>>>(kin, vin, n, shift, mask, tiles, hist, kout, vout);
+        kin = kout;
+        vin = vout;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace vsim

@@ -1,0 +1,675 @@
+// The substep kernels of the solver: prediction, the kinematic drive, the
+// 8-colour stable Neo-Hookean projection, body contact and the closing pass.
+//
+// Node state lives in HBM as three float4 arrays in the reference's dense
+// node order (pos, prev, vel; state.wgsl:16-19). pos.w carries the node's
+// inverse mass as the solver sees it (the reference's separate nodeInvMass
+// buffer, particles.js:206-215), so one 16-byte load brings a node's
+// position and weight together; every kernel that writes pos keeps w.
+#include "kernels.cuh"
+
+namespace vsim {
+
+// ------------------------------------------------------- Kuhn constants --
+
+// kuhn.js:28-35: corner indices of the six tetrahedra.
+__host__ __device__ constexpr int kTet(int t, int i) {
+    constexpr int tets[6][4] = {{0, 1, 3, 7}, {0, 5, 1, 7}, {0, 3, 2, 7}, {0, 2, 6, 7}, {0, 4, 5, 7}, {0, 6, 4, 7}};
+    return tets[t][i];
+}
+
+// The inverse rest shape of tetrahedron t of the unit cube, entry (row r,
+// column c) of the column-major matrix (kuhn.js:59-80). The rest shapes are
+// unimodular, so the inverse is the integer adjugate divided by det = +-1.
+struct KuhnInv {
+    int v[6][3][3];  // [t][column][row]
+};
+
+__host__ __device__ constexpr KuhnInv makeKuhnInv() {
+    KuhnInv out{};
+    for (int t = 0; t < 6; t++) {
+        int m[9] = {};  // column-major Dm
+        for (int col = 0; col < 3; col++)
+            for (int row = 0; row < 3; row++)
+                m[col * 3 + row] = ((kTet(t, col + 1) >> row) & 1) - ((kTet(t, 0) >> row) & 1);
+        const int det = m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) +
+                        m[6] * (m[1] * m[5] - m[4] * m[2]);
+        const int adj[9] = {m[4] * m[8] - m[7] * m[5], m[7] * m[2] - m[1] * m[8], m[1] * m[5] - m[4] * m[2],
+                            m[6] * m[5] - m[3] * m[8], m[0] * m[8] - m[6] * m[2], m[3] * m[2] - m[0] * m[5],
+                            m[3] * m[7] - m[6] * m[4], m[6] * m[1] - m[0] * m[7], m[0] * m[4] - m[3] * m[1]};
+        for (int col = 0; col < 3; col++)
+            for (int row = 0; row < 3; row++) out.v[t][col][row] = adj[col * 3 + row] / det;
+    }
+    return out;
+}
+
+constexpr KuhnInv kKuhn = makeKuhnInv();
+
+void kuhnTable(float out[54]) {
+    for (int t = 0; t < 6; t++)
+        for (int col = 0; col < 3; col++)
+            for (int row = 0; row < 3; row++) out[t * 9 + col * 3 + row] = float(kKuhn.v[t][col][row]);
+}
+
+// a0 k0 s + a1 k1 s + a2 k2 s for constant k in {-1, 0, 1}, summed left to
+// right with the zero terms left out. The reference multiplies by the full
+// matrix B = K s; a product with an exact zero is a signed zero and adding it
+// changes nothing but the sign of an exact-zero sum, so this is the same
+// value with a third of the arithmetic.
+template <int K>
+__device__ __forceinline__ float kscale(float s, float ns) {
+    return K > 0 ? s : ns;
+}
+
+template <int K0, int K1, int K2>
+__device__ __forceinline__ V sparse3(V a0, V a1, V a2, float s, float ns) {
+    if constexpr (K0 != 0) {
+        V acc = a0 * kscale<K0>(s, ns);
+        if constexpr (K1 != 0) acc = acc + a1 * kscale<K1>(s, ns);
+        if constexpr (K2 != 0) acc = acc + a2 * kscale<K2>(s, ns);
+        return acc;
+    } else if constexpr (K1 != 0) {
+        V acc = a1 * kscale<K1>(s, ns);
+        if constexpr (K2 != 0) acc = acc + a2 * kscale<K2>(s, ns);
+        return acc;
+    } else {
+        return a2 * kscale<K2>(s, ns);
+    }
+}
+
+// A * B with B = K_t s: column j is sum_k A.c[k] B[j][k].
+template <int t>
+__device__ __forceinline__ M timesB(const M& A, float s, float ns) {
+    return M{{sparse3<kKuhn.v[t][0][0], kKuhn.v[t][0][1], kKuhn.v[t][0][2]>(A.c[0], A.c[1], A.c[2], s, ns),
+              sparse3<kKuhn.v[t][1][0], kKuhn.v[t][1][1], kKuhn.v[t][1][2]>(A.c[0], A.c[1], A.c[2], s, ns),
+              sparse3<kKuhn.v[t][2][0], kKuhn.v[t][2][1], kKuhn.v[t][2][2]>(A.c[0], A.c[1], A.c[2], s, ns)}};
+}
+
+// A * transpose(B): column j is sum_k A.c[k] B[k][j].
+template <int t>
+__device__ __forceinline__ M timesBt(const M& A, float s, float ns) {
+    return M{{sparse3<kKuhn.v[t][0][0], kKuhn.v[t][1][0], kKuhn.v[t][2][0]>(A.c[0], A.c[1], A.c[2], s, ns),
+              sparse3<kKuhn.v[t][0][1], kKuhn.v[t][1][1], kKuhn.v[t][2][1]>(A.c[0], A.c[1], A.c[2], s, ns),
+              sparse3<kKuhn.v[t][0][2], kKuhn.v[t][1][2], kKuhn.v[t][2][2]>(A.c[0], A.c[1], A.c[2], s, ns)}};
+}
+
+// xpbdCouple.wgsl:58-71.
+__device__ __forceinline__ void couple(float cx, float cy, float ax, float ay, float relax, float rx, float ry, float gx,
+                                       float gy, float gz, float& lx, float& ly) {
+    const float stiffened = 1.0f + relax;
+    const float a00 = gx * stiffened + ax;
+    const float a01 = gy * stiffened;
+    const float a11 = gz * stiffened + ay;
+    const float det = a00 * a11 - a01 * a01;
+    if (det < 1e-20f) {
+        lx = 0.0f;
+        ly = 0.0f;
+        return;
+    }
+    const float bx = -(cx + rx * relax);
+    const float by = -(cy + ry * relax);
+    lx = (a11 * bx - a01 * by) / det;
+    ly = (a00 * by - a01 * bx) / det;
+}
+
+// project.wgsl:75-153, tetrahedron t of the cell held in registers.
+template <int t>
+__device__ __forceinline__ void projectTet(V (&p)[8], const V (&prev)[8], const float (&w)[8], float s, float ns,
+                                           float alphaDev, float alphaHyd, float gamma, float relax) {
+    constexpr int i0 = kTet(t, 0), i1 = kTet(t, 1), i2 = kTet(t, 2), i3 = kTet(t, 3);
+    const float w0 = w[i0], w1 = w[i1], w2 = w[i2], w3 = w[i3];
+    if (w0 + w1 + w2 + w3 == 0.0f) return;
+    const V base = p[i0];
+    const M F = timesB<t>(M{{p[i1] - base, p[i2] - base, p[i3] - base}}, s, ns);
+    const float cDev = sqrtf(dot(F.c[0], F.c[0]) + dot(F.c[1], F.c[1]) + dot(F.c[2], F.c[2]));
+    const float cHyd = determinant(F) - gamma;
+    const float inv = cDev > 1e-9f ? 1.0f / cDev : 0.0f;
+    const M mDev = timesBt<t>(F * inv, s, ns);
+    const M mHyd = timesBt<t>(M{{cross(F.c[1], F.c[2]), cross(F.c[2], F.c[0]), cross(F.c[0], F.c[1])}}, s, ns);
+    const V d1 = mDev.c[0], d2 = mDev.c[1], d3 = mDev.c[2];
+    const V d0 = -(d1 + d2 + d3);
+    const V h1 = mHyd.c[0], h2 = mHyd.c[1], h3 = mHyd.c[2];
+    const V h0 = -(h1 + h2 + h3);
+    const float gx = w0 * dot(d0, d0) + w1 * dot(d1, d1) + w2 * dot(d2, d2) + w3 * dot(d3, d3);
+    const float gy = w0 * dot(d0, h0) + w1 * dot(d1, h1) + w2 * dot(d2, h2) + w3 * dot(d3, h3);
+    const float gz = w0 * dot(h0, h0) + w1 * dot(h1, h1) + w2 * dot(h2, h2) + w3 * dot(h3, h3);
+    const V x0 = p[i0] - prev[i0];
+    const V x1 = p[i1] - prev[i1];
+    const V x2 = p[i2] - prev[i2];
+    const V x3 = p[i3] - prev[i3];
+    const float rx = dot(d0, x0) + dot(d1, x1) + dot(d2, x2) + dot(d3, x3);
+    const float ry = dot(h0, x0) + dot(h1, x1) + dot(h2, x2) + dot(h3, x3);
+    float lx, ly;
+    couple(cDev, cHyd, alphaDev, alphaHyd, relax, rx, ry, gx, gy, gz, lx, ly);
+    p[i0] = p[i0] + (d0 * lx + h0 * ly) * w0;
+    p[i1] = p[i1] + (d1 * lx + h1 * ly) * w1;
+    p[i2] = p[i2] + (d2 * lx + h2 * ly) * w2;
+    p[i3] = p[i3] + (d3 * lx + h3 * ly) * w3;
+}
+
+// ------------------------------------------------------------- kernels --
+
+// predict.wgsl:19-36 over the active nodes.
+__global__ void predictKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ active,
+                              float4* __restrict__ pos, float4* __restrict__ prev, float4* __restrict__ vel) {
+    pdlWait();
+    pdlLaunchNext();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= fp->activeCount) return;
+    const uint32_t n = active[i];
+    const float4 P = pos[n];
+    if (P.w == 0.0f) return;
+    const float dt = fp->dt;
+    const V g = mk(fp->gx, fp->gy, fp->gz);
+    const V v = xyz(vel[n]) + g * dt;
+    const V p = xyz(P);
+    prev[n] = withW(p, 0.0f);
+    pos[n] = withW(p + v * dt, P.w);
+    vel[n] = withW(v, 0.0f);
+}
+
+// driveHard.wgsl:15-35 and driveCompliant.wgsl:24-41.
+__global__ void driveKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ driven,
+                            const float4* __restrict__ offsets, float4* __restrict__ pos, float4* __restrict__ prev,
+                            float4* __restrict__ vel) {
+    pdlWait();
+    pdlLaunchNext();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= fp->drivenCount) return;
+    const uint32_t n = driven[i];
+    const float dt = fp->dt;
+    const V goal = mk(fp->grabTarget[0], fp->grabTarget[1], fp->grabTarget[2]) + xyz(offsets[i]);
+    const float4 P = pos[n];
+    if (fp->law == VSIM_DRIVE_HARD) {
+        const V here = xyz(P);
+        const V step = mk(fp->grabVelocity[0], fp->grabVelocity[1], fp->grabVelocity[2]) * dt;
+        const V toGoal = goal - here;
+        const V next = here + (dot(step, step) >= dot(toGoal, toGoal) ? toGoal : step);
+        prev[n] = withW(here, 0.0f);
+        pos[n] = withW(next, P.w);
+        vel[n] = withW((next - here) / dt, 0.0f);
+    } else {
+        const V p = xyz(P);
+        const float dt2 = dt * dt;
+        const float tau2 = fp->responseTime * fp->responseTime;
+        const float frac = dt2 / (dt2 + tau2);
+        pos[n] = withW(p + (goal - p) * frac, P.w);
+    }
+}
+
+// project.wgsl:35-184: one colour pass, one thread per occupied cell.
+// `cells` holds (global node of corner 0, body) per cell of this colour.
+template <bool LIMIT_ONLY>
+__global__ void __launch_bounds__(512) elasticKernel(const uint2* __restrict__ cells, uint32_t count,
+                                                     const DevBody* __restrict__ bodies, float4* __restrict__ pos,
+                                                     const float4* __restrict__ prevState, StretchLengths lens) {
+    pdlWait();
+    pdlLaunchNext();
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= count) return;
+    const uint2 entry = cells[slot];
+    const DevBody* b = bodies + entry.y;
+    const float maxStretch = b->maxStretch;
+    if (LIMIT_ONLY && !(maxStretch > 1.0f)) return;
+    const uint32_t nx = b->nx, nxy = b->nxy, n0 = entry.x;
+    const uint32_t ids[8] = {n0, n0 + 1, n0 + nx, n0 + nx + 1, n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
+    V p[8], prev[8];
+    float w[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const float4 P = pos[ids[c]];
+        p[c] = xyz(P);
+        w[c] = P.w;
+    }
+#pragma unroll
+    for (int c = 0; c < 8; c++) prev[c] = xyz(prevState[ids[c]]);
+
+    if (!LIMIT_ONLY) {
+        const float alphaDev = b->alphaDev, alphaHyd = b->alphaHyd, gamma = b->gamma, relax = b->relax;
+        const float s = b->restScale, ns = -s;
+        projectTet<0>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+        projectTet<1>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+        projectTet<2>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+        projectTet<3>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+        projectTet<4>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+        projectTet<5>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+    }
+
+    // project.wgsl:162-179: unilateral length limit over all 28 corner pairs.
+    if (maxStretch > 1.0f) {
+        const float h = b->h;
+        for (int sweep = 0; sweep < 2; sweep++) {
+#pragma unroll
+            for (int a = 0; a < 8; a++) {
+#pragma unroll
+                for (int bb = a + 1; bb < 8; bb++) {
+                    const V delta = p[bb] - p[a];
+                    const float len = length(delta);
+                    const float maximum = lens.len[__popc(a ^ bb) - 1] * h * maxStretch;
+                    const float weight = w[a] + w[bb];
+                    if (len > maximum && weight > 0.0f) {
+                        const V correction = delta * ((len - maximum) / (len * weight));
+                        p[a] = p[a] + w[a] * correction;
+                        p[bb] = p[bb] - w[bb] * correction;
+                    }
+                }
+            }
+        }
+    }
+
+#pragma unroll
+    for (int c = 0; c < 8; c++) pos[ids[c]] = withW(p[c], w[c]);
+}
+
+// finalize.wgsl:29-42.
+__device__ __forceinline__ V resolvePlane(V p, V prev, V normal, float depth, float friction) {
+    if (depth <= 0.0f) return p;
+    V q = p + normal * depth;
+    const V delta = q - prev;
+    const V tangent = delta - normal * dot(delta, normal);
+    const float len = length(tangent);
+    if (len > 1e-9f) q = q - tangent * fminf(1.0f, friction * depth / len);
+    return q;
+}
+
+// finalize.wgsl:44-74 over the active nodes; the velocity factor
+// exp(-damping dt) is the body's, evaluated once on the host.
+__global__ void finalizeKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ active,
+                               const uint32_t* __restrict__ activeBody, const DevBody* __restrict__ bodies,
+                               float4* __restrict__ pos, const float4* __restrict__ prevState,
+                               float4* __restrict__ vel) {
+    pdlWait();
+    pdlLaunchNext();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= fp->activeCount) return;
+    const uint32_t n = active[i];
+    const float4 P = pos[n];
+    if (P.w == 0.0f) return;
+    const DevBody* b = bodies + activeBody[i];
+    const V prev = xyz(prevState[n]);
+    const float fr = b->friction;
+    const V mn = mk(fp->tankMin[0], fp->tankMin[1], fp->tankMin[2]);
+    const V mx = mk(fp->tankMax[0], fp->tankMax[1], fp->tankMax[2]);
+    V p = xyz(P);
+    p = resolvePlane(p, prev, mk(0.0f, 1.0f, 0.0f), mn.y - p.y, fr);
+    p = resolvePlane(p, prev, mk(1.0f, 0.0f, 0.0f), mn.x - p.x, fr);
+    p = resolvePlane(p, prev, mk(-1.0f, 0.0f, 0.0f), p.x - mx.x, fr);
+    p = resolvePlane(p, prev, mk(0.0f, 0.0f, 1.0f), mn.z - p.z, fr);
+    p = resolvePlane(p, prev, mk(0.0f, 0.0f, -1.0f), p.z - mx.z, fr);
+    pos[n] = withW(p, P.w);
+    V v = (p - prev) / fp->dt;
+    v = v * b->damp;
+    vel[n] = withW(v, 0.0f);
+}
+
+// ------------------------------------------------------------- contact --
+//
+// The reference bins every surface record into a fixed 32-slot bucket with
+// an atomic, then canonicalises each bucket by an insertion sort
+// (bin.wgsl, sort.wgsl). Here the grid is a counting sort: per-bucket
+// counts with the arrival rank of each record, one contiguous segment
+// allocated per occupied bucket, a scatter, and an ascending sort of each
+// segment's first 32 entries -- the same visible set, in the same order, with
+// work proportional to the surface rather than to the grid.
+
+// contacts.wgsl:84-91.
+__device__ __forceinline__ uint32_t bucketOf(const FrameParams* fp, V p, int coord[3]) {
+    const float q[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float last = float(fp->gridDims[a]) - 1.0f;
+        const float f = floorf((q[a] - fp->gridOrigin[a]) / fp->bucket);
+        coord[a] = int(fminf(fmaxf(f, 0.0f), last));
+    }
+    return uint32_t(coord[0]) + fp->gridDims[0] * (uint32_t(coord[1]) + fp->gridDims[1] * uint32_t(coord[2]));
+}
+
+__global__ void binKernel(const FrameParams* __restrict__ fp, const uint4* __restrict__ surf,
+                          const float4* __restrict__ pos, uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
+                          uint32_t* __restrict__ count) {
+    pdlWait();
+    pdlLaunchNext();
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= fp->surfaceCount) return;
+    int coord[3];
+    const uint32_t b = bucketOf(fp, xyz(pos[surf[r].x]), coord);
+    key[r] = b;
+    rank[r] = atomicAdd(&count[b], 1u);
+}
+
+// Each bucket's first-arriving record reserves the bucket's segment; one
+// atomic per block on the shared cursor.
+__global__ void allocKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ key,
+                            const uint32_t* __restrict__ rank, const uint32_t* __restrict__ count,
+                            uint32_t* __restrict__ start, uint32_t* __restrict__ cursor) {
+    pdlWait();
+    pdlLaunchNext();
+    __shared__ uint32_t warpSum[32];
+    __shared__ uint32_t blockBase;
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool first = r < fp->surfaceCount && rank[r] == 0;
+    const uint32_t b = first ? key[r] : 0;
+    const uint32_t need = first ? count[b] : 0;
+    // Block-wide exclusive prefix of `need`.
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = need;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= uint32_t(d)) incl += v;
+    }
+    if (lane == 31) warpSum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t nw = blockDim.x >> 5;
+        uint32_t v = lane < nw ? warpSum[lane] : 0;
+        uint32_t scan = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, scan, d);
+            if (lane >= uint32_t(d)) scan += u;
+        }
+        if (lane < nw) warpSum[lane] = scan - v;
+        if (lane == nw - 1) blockBase = scan > 0 ? atomicAdd(cursor, scan) : 0;
+    }
+    __syncthreads();
+    if (first) start[b] = blockBase + warpSum[warp] + (incl - need);
+}
+
+__global__ void scatterKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ key,
+                              const uint32_t* __restrict__ rank, const uint32_t* __restrict__ start,
+                              uint32_t* __restrict__ entries) {
+    pdlWait();
+    pdlLaunchNext();
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= fp->surfaceCount) return;
+    entries[start[key[r]] + rank[r]] = r;
+}
+
+// sort.wgsl:14-53: the bucket's visible entries -- its kBucketSlots lowest
+// record indices -- in ascending order at the front of its segment.
+__global__ void canonKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ key,
+                            const uint32_t* __restrict__ rank, const uint32_t* __restrict__ start,
+                            const uint32_t* __restrict__ count, uint32_t* __restrict__ entries) {
+    pdlWait();
+    pdlLaunchNext();
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= fp->surfaceCount || rank[r] != 0) return;
+    const uint32_t b = key[r];
+    const uint32_t n = count[b];
+    if (n < 2) return;
+    uint32_t* e = entries + start[b];
+    const uint32_t m = n < kBucketSlots ? n : kBucketSlots;
+    for (uint32_t i = 1; i < m; i++) {
+        const uint32_t v = e[i];
+        uint32_t at = i;
+        while (at > 0 && e[at - 1] > v) {
+            e[at] = e[at - 1];
+            at--;
+        }
+        e[at] = v;
+    }
+    // Past capacity, keep the lowest kBucketSlots in the visible prefix.
+    for (uint32_t i = m; i < n; i++) {
+        const uint32_t v = e[i];
+        if (v >= e[m - 1]) continue;
+        e[i] = e[m - 1];
+        uint32_t at = m - 1;
+        while (at > 0 && e[at - 1] > v) {
+            e[at] = e[at - 1];
+            at--;
+        }
+        e[at] = v;
+    }
+}
+
+// Whether records a and b may touch: the reference drops every same-body
+// pair (collide.wgsl:66); with self contact on, a same-body pair counts when
+// its nodes share no cell (rest grid distance above one on some axis).
+__device__ __forceinline__ bool admitted(uint4 a, uint4 b, uint32_t selfContact) {
+    if (a.y != b.y) return true;
+    if (!selfContact) return false;
+#pragma unroll
+    for (int axis = 0; axis < 3; axis++) {
+        const int ia = int((a.z >> (10 * axis)) & 1023u), ib = int((b.z >> (10 * axis)) & 1023u);
+        if (abs(ia - ib) > 1) return true;
+    }
+    return false;
+}
+
+// collide.wgsl:16-125. With `pairs` set, every counted hit (r, other) is also
+// appended there (capacity-checked), for the pair-set checks.
+template <bool EMIT>
+__global__ void collideKernel(const FrameParams* __restrict__ fp, const uint4* __restrict__ surf,
+                              const DevBody* __restrict__ bodies, const float4* __restrict__ pos,
+                              const float4* __restrict__ prevState, const uint32_t* __restrict__ start,
+                              const uint32_t* __restrict__ count, const uint32_t* __restrict__ entries,
+                              float4* __restrict__ delta, uint32_t* __restrict__ pairs, uint32_t capacity,
+                              unsigned long long* __restrict__ pairCount) {
+    pdlWait();
+    pdlLaunchNext();
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= fp->surfaceCount) return;
+    const uint4 me = surf[r];
+    const uint32_t node = me.x;
+    const float radius = __uint_as_float(me.w);
+    const float4 P = pos[node];
+    const float wi = P.w;
+    const V pi = xyz(P);
+    const V movedI = pi - xyz(prevState[node]);
+    const float frictionI = bodies[me.y].friction;
+    const uint32_t selfContact = fp->selfContact;
+    V sum = mk(0.0f, 0.0f, 0.0f);
+    float hits = 0.0f;
+    int centre[3];
+    bucketOf(fp, pi, centre);
+    const int dims[3] = {int(fp->gridDims[0]), int(fp->gridDims[1]), int(fp->gridDims[2])};
+    for (int dz = -1; dz <= 1; dz++) {
+        const int z = centre[2] + dz;
+        if (z < 0 || z >= dims[2]) continue;
+        for (int dy = -1; dy <= 1; dy++) {
+            const int y = centre[1] + dy;
+            if (y < 0 || y >= dims[1]) continue;
+            for (int dx = -1; dx <= 1; dx++) {
+                const int x = centre[0] + dx;
+                if (x < 0 || x >= dims[0]) continue;
+                const uint32_t bucket = uint32_t(x) + fp->gridDims[0] * (uint32_t(y) + fp->gridDims[1] * uint32_t(z));
+                const uint32_t n = count[bucket];
+                if (n == 0) continue;
+                const uint32_t held = n < kBucketSlots ? n : kBucketSlots;
+                const uint32_t* e = entries + start[bucket];
+                for (uint32_t k = 0; k < held; k++) {
+                    const uint32_t other = e[k];
+                    const uint4 them = surf[other];
+                    if (!admitted(me, them, selfContact)) continue;
+                    const uint32_t mate = them.x;
+                    const float4 Q = pos[mate];
+                    const V pj = xyz(Q);
+                    const V d = pi - pj;
+                    const float dist2 = dot(d, d);
+                    const float reach = radius + __uint_as_float(them.w);
+                    if (dist2 >= reach * reach) continue;
+                    const float wj = Q.w;
+                    const float total = wi + wj;
+                    if (total <= 0.0f) continue;
+                    const float share = wi / total;
+                    const float dist = sqrtf(dist2);
+                    V normal = mk(0.0f, node < mate ? 1.0f : -1.0f, 0.0f);
+                    if (dist > 1e-9f) normal = d / dist;
+                    const float depth = reach - dist;
+                    V correction = normal * (depth * share);
+                    const V sliding = movedI - (pj - xyz(prevState[mate]));
+                    const V tangent = sliding - normal * dot(sliding, normal);
+                    const float slid = length(tangent);
+                    if (slid > 1e-9f) {
+                        const float mu = fminf(frictionI, bodies[them.y].friction);
+                        correction = correction - tangent * (share * fminf(1.0f, mu * depth / slid));
+                    }
+                    sum = sum + correction;
+                    hits = hits + 1.0f;
+                    if (EMIT) {
+                        const unsigned long long at = atomicAdd(pairCount, 1ull);
+                        if (at < capacity) {
+                            pairs[2 * at] = r;
+                            pairs[2 * at + 1] = other;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (!EMIT) delta[r] = withW(sum, hits);
+}
+
+// settle.wgsl:20-36 (gain 1, bodyContact.js:48), then empties the buckets
+// this substep used and the segment cursor, restoring the empty grid.
+__global__ void settleKernel(const FrameParams* __restrict__ fp, const uint4* __restrict__ surf,
+                             const uint32_t* __restrict__ key, const float4* __restrict__ delta,
+                             float4* __restrict__ pos, uint32_t* __restrict__ count, uint32_t* __restrict__ cursor,
+                             int apply) {
+    pdlWait();
+    pdlLaunchNext();
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= fp->surfaceCount) return;
+    if (apply) {
+        const float4 d = delta[r];
+        if (d.w > 0.0f) {
+            const uint32_t node = surf[r].x;
+            const float4 P = pos[node];
+            const V step = xyz(d) * (1.0f / d.w);
+            pos[node] = withW(xyz(P) + step, P.w);
+        }
+    }
+    count[key[r]] = 0;
+    if (r == 0) *cursor = 0;
+}
+
+// ------------------------------------------------------- node utilities --
+
+// pos.w := base[n] for a list of nodes (restoring a released hold).
+__global__ void restoreWKernel(const uint32_t* __restrict__ nodes, uint32_t n, const float* __restrict__ base,
+                               float4* __restrict__ pos) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pos[nodes[i]].w = base[nodes[i]];
+}
+
+// pos.w := 0 for a list of nodes (a hard hold prescribes them).
+__global__ void zeroWKernel(const uint32_t* __restrict__ nodes, uint32_t n, float4* __restrict__ pos) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pos[nodes[i]].w = 0.0f;
+}
+
+// pos.w := base[n] for a node range (after a density change).
+__global__ void refreshWKernel(uint32_t first, uint32_t n, const float* __restrict__ base, float4* __restrict__ pos) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pos[first + i].w = base[first + i];
+}
+
+// pos.xyz := in.xyz keeping w (writing a state from the host).
+__global__ void mergeXyzKernel(const float4* __restrict__ in, uint32_t n, float4* __restrict__ pos) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float4 a = in[i];
+        pos[i] = make_float4(a.x, a.y, a.z, pos[i].w);
+    }
+}
+
+// ------------------------------------------------------------ launchers --
+
+namespace {
+template <class... KArgs, class... Args>
+cudaError_t launch(const LaunchCtx& ctx, void (*kernel)(KArgs...), uint32_t grid, uint32_t block, Args... args) {
+    if (grid == 0) return cudaSuccess;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = ctx.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = ctx.pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+inline uint32_t blocks(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
+}  // namespace
+
+cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount) {
+    return launch(c, predictKernel, blocks(activeCount, 256), 256, s.fp, s.active, s.pos, s.prev, s.vel);
+}
+
+cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drivenCount) {
+    return launch(c, driveKernel, blocks(drivenCount, 256), 256, s.fp, s.driven, s.drivenOffset, s.pos, s.prev, s.vel);
+}
+
+cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint2* cells, uint32_t count,
+                          bool limitOnly, uint32_t block, const StretchLengths& lens) {
+    if (limitOnly)
+        return launch(c, elasticKernel<true>, blocks(count, block), block, cells, count, s.bodies, s.pos,
+                      (const float4*)s.prev, lens);
+    return launch(c, elasticKernel<false>, blocks(count, block), block, cells, count, s.bodies, s.pos,
+                  (const float4*)s.prev, lens);
+}
+
+cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount) {
+    return launch(c, finalizeKernel, blocks(activeCount, 256), 256, s.fp, s.active, s.activeBody, s.bodies, s.pos,
+                  (const float4*)s.prev, s.vel);
+}
+
+cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, uint32_t surfaceCount, ContactMode mode,
+                          uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount) {
+    const uint32_t g = blocks(surfaceCount, 256);
+    cudaError_t e;
+    if ((e = launch(c, binKernel, g, 256, s.fp, s.surf, (const float4*)s.pos, s.key, s.rank, s.count))) return e;
+    if ((e = launch(c, allocKernel, g, 256, s.fp, (const uint32_t*)s.key, (const uint32_t*)s.rank,
+                    (const uint32_t*)s.count, s.start, s.cursor)))
+        return e;
+    if ((e = launch(c, scatterKernel, g, 256, s.fp, (const uint32_t*)s.key, (const uint32_t*)s.rank,
+                    (const uint32_t*)s.start, s.entries)))
+        return e;
+    if ((e = launch(c, canonKernel, g, 256, s.fp, (const uint32_t*)s.key, (const uint32_t*)s.rank,
+                    (const uint32_t*)s.start, (const uint32_t*)s.count, s.entries)))
+        return e;
+    if (mode == ContactMode::Pairs) {
+        if ((e = launch(c, collideKernel<true>, g, 256, s.fp, s.surf, s.bodies, (const float4*)s.pos,
+                        (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count,
+                        (const uint32_t*)s.entries, s.delta, pairs, capacity, pairCount)))
+            return e;
+    } else {
+        if ((e = launch(c, collideKernel<false>, g, 256, s.fp, s.surf, s.bodies, (const float4*)s.pos,
+                        (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count,
+                        (const uint32_t*)s.entries, s.delta, (uint32_t*)nullptr, 0u,
+                        (unsigned long long*)nullptr)))
+            return e;
+    }
+    return launch(c, settleKernel, g, 256, s.fp, s.surf, (const uint32_t*)s.key, (const float4*)s.delta, s.pos,
+                  s.count, s.cursor, mode == ContactMode::Solve ? 1 : 0);
+}
+
+cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos) {
+    if (n == 0) return cudaSuccess;
+    restoreWKernel<<<blocks(n, 256), 256, 0, st>>>(nodes, n, base, pos);
+    return cudaGetLastError();
+}
+
+cudaError_t launchZeroW(cudaStream_t st, const uint32_t* nodes, uint32_t n, float4* pos) {
+    if (n == 0) return cudaSuccess;
+    zeroWKernel<<<blocks(n, 256), 256, 0, st>>>(nodes, n, pos);
+    return cudaGetLastError();
+}
+
+cudaError_t launchRefreshW(cudaStream_t st, uint32_t first, uint32_t n, const float* base, float4* pos) {
+    if (n == 0) return cudaSuccess;
+    refreshWKernel<<<blocks(n, 256), 256, 0, st>>>(first, n, base, pos);
+    return cudaGetLastError();
+}
+
+cudaError_t launchMergeXyz(cudaStream_t st, const float4* in, uint32_t n, float4* pos) {
+    if (n == 0) return cudaSuccess;
+    mergeXyzKernel<<<blocks(n, 256), 256, 0, st>>>(in, n, pos);
+    return cudaGetLastError();
+}
+
+}  // namespace vsim

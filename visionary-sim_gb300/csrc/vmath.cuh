@@ -1,0 +1,58 @@
+// Device vector arithmetic in the reference's evaluation order (WGSL: left
+// to right, `dot` as (x + y) + z, `M * v` as c0 v.x + c1 v.y + c2 v.z).
+//
+// Every translation unit that includes this is compiled with -fmad=false,
+// so each multiply and each add rounds separately, exactly as the CPU
+// restatement of the reference does; together with IEEE division and square
+// root (nvcc's defaults) that makes the kernels' results equal to it.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace vsim {
+
+struct V {
+    float x, y, z;
+};
+
+__device__ __forceinline__ V mk(float x, float y, float z) { return V{x, y, z}; }
+__device__ __forceinline__ V xyz(float4 a) { return V{a.x, a.y, a.z}; }
+__device__ __forceinline__ V operator+(V a, V b) { return V{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V operator-(V a, V b) { return V{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V operator-(V a) { return V{-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ V operator*(V a, float s) { return V{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ V operator*(float s, V a) { return V{s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ V operator/(V a, float s) { return V{a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float length(V a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ V cross(V a, V b) {
+    return V{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+// Column-major 3x3: c[k] is column k.
+struct M {
+    V c[3];
+};
+
+__device__ __forceinline__ M operator*(const M& m, float s) { return M{{m.c[0] * s, m.c[1] * s, m.c[2] * s}}; }
+__device__ __forceinline__ V mul(const M& m, V v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z; }
+// Expansion order of the reference's mat3Determinant (mat3.js:25-31).
+__device__ __forceinline__ float determinant(const M& m) {
+    const float m0 = m.c[0].x, m1 = m.c[0].y, m2 = m.c[0].z;
+    const float m3 = m.c[1].x, m4 = m.c[1].y, m5 = m.c[1].z;
+    const float m6 = m.c[2].x, m7 = m.c[2].y, m8 = m.c[2].z;
+    return m0 * (m4 * m8 - m7 * m5) - m3 * (m1 * m8 - m7 * m2) + m6 * (m1 * m5 - m4 * m2);
+}
+
+__device__ __forceinline__ float4 withW(V p, float w) { return make_float4(p.x, p.y, p.z, w); }
+
+// Programmatic dependent launch: wait for the preceding kernel in the stream
+// (its writes visible) before touching memory, and let the next kernel's
+// launch begin while this one runs. Both are no-ops without the launch
+// attribute.
+__device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdlLaunchNext() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
+}  // namespace vsim

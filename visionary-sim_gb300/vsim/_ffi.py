@@ -1,0 +1,225 @@
+"""ctypes binding of libvsim's C ABI (include/vsim.h).
+
+Loading fails loudly when the library has not been built: there is no
+fallback path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libvsim.so"
+HEADER = Path(__file__).resolve().parents[2] / "include" / "vsim.h"
+
+VSIM_OK = 0
+VSIM_ERR_RANGE = 1
+VSIM_ERR_INVALID = 2
+VSIM_ERR_CUDA = 3
+VSIM_ERR_NOMEM = 4
+VSIM_ERR_DESTROYED = 5
+VSIM_ERR_CAPACITY = 6
+VSIM_ERR_TIMEOUT = 7
+VSIM_DRIVE_HARD = 0
+VSIM_DRIVE_COMPLIANT = 1
+VSIM_MAX_DRIVEN = 4096
+
+MAT_YOUNGS = 1 << 0
+MAT_POISSON = 1 << 1
+MAT_DENSITY = 1 << 2
+MAT_FRICTION = 1 << 3
+MAT_DAMPING = 1 << 4
+MAT_RELAXATION = 1 << 5
+MAT_MAX_STRETCH = 1 << 6
+
+
+class Material(C.Structure):
+    _fields_ = [
+        ("youngs_modulus", C.c_double),
+        ("poisson_ratio", C.c_double),
+        ("density", C.c_double),
+        ("friction", C.c_double),
+        ("damping", C.c_double),
+        ("relaxation", C.c_double),
+        ("max_stretch", C.c_double),
+    ]
+
+
+class BodyDesc(C.Structure):
+    _fields_ = [
+        ("cell_dims", C.c_uint32 * 3),
+        ("origin", C.c_double * 3),
+        ("h", C.c_double),
+        ("occupancy", C.POINTER(C.c_uint8)),
+        ("material", Material),
+        ("static_nodes", C.POINTER(C.c_uint32)),
+        ("static_count", C.c_uint32),
+    ]
+
+
+class Tank(C.Structure):
+    _fields_ = [("min", C.c_double * 3), ("max", C.c_double * 3)]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("body_count", C.c_uint32),
+        ("nodes", C.c_uint32),
+        ("active_nodes", C.c_uint32),
+        ("cells", C.c_uint32),
+        ("contact_nodes", C.c_uint32),
+        ("contact", C.c_int32),
+        ("self_contact", C.c_int32),
+        ("iterations", C.c_uint32),
+        ("steps", C.c_uint64),
+        ("last_steps", C.c_uint32),
+        ("max_steps_per_frame", C.c_uint32),
+        ("step_duration", C.c_double),
+        ("simulated_time", C.c_double),
+        ("backlog_time", C.c_double),
+        ("frame_dropped_time", C.c_double),
+        ("dropped_time", C.c_double),
+        ("overloaded", C.c_int32),
+        ("cfl", C.c_double),
+        ("limited_by", C.c_int32),
+        ("driven", C.c_uint32),
+        ("drive_capacity", C.c_uint32),
+    ]
+
+
+class ClockReport(C.Structure):
+    _fields_ = [
+        ("step_duration", C.c_double),
+        ("max_steps_per_frame", C.c_uint32),
+        ("steps", C.c_uint32),
+        ("elapsed", C.c_double),
+        ("total_steps", C.c_uint64),
+        ("simulated_time", C.c_double),
+        ("backlog_time", C.c_double),
+        ("frame_dropped_time", C.c_double),
+        ("dropped_time", C.c_double),
+        ("overloaded", C.c_int32),
+    ]
+
+
+_P = C.c_void_p
+_F = C.POINTER(C.c_float)
+_D = C.POINTER(C.c_double)
+_U = C.POINTER(C.c_uint32)
+_SZ = C.c_size_t
+
+SIGNATURES = {
+    "vsim_last_error": (C.c_char_p, []),
+    "vsim_abi_version": (C.c_int, []),
+    "vsim_create": (C.c_int, [C.POINTER(BodyDesc), C.c_uint32, C.POINTER(Tank), _P, C.POINTER(_P)]),
+    "vsim_destroy": (C.c_int, [_P]),
+    "vsim_step": (C.c_int, [_P, C.c_double]),
+    "vsim_request_step": (C.c_int, [_P]),
+    "vsim_dispatch": (C.c_int, [_P, C.c_uint32]),
+    "vsim_reset": (C.c_int, [_P]),
+    "vsim_synchronize": (C.c_int, [_P]),
+    "vsim_read_positions": (C.c_int, [_P, _F, _SZ]),
+    "vsim_read_state": (C.c_int, [_P, _F, _F, _F, _SZ]),
+    "vsim_write_state": (C.c_int, [_P, _F, _F, _F, _SZ]),
+    "vsim_node_count": (C.c_uint32, [_P]),
+    "vsim_body_node_offset": (C.c_uint32, [_P, C.c_uint32]),
+    "vsim_read_inv_mass": (C.c_int, [_P, _F, _SZ]),
+    "vsim_hold": (C.c_int, [_P, _U, _F, C.c_uint32]),
+    "vsim_move_grab": (C.c_int, [_P, _D]),
+    "vsim_place_grab": (C.c_int, [_P, _D]),
+    "vsim_release": (C.c_int, [_P]),
+    "vsim_set_drive_law": (C.c_int, [_P, C.c_int]),
+    "vsim_set_drive_response_time": (C.c_int, [_P, C.c_double]),
+    "vsim_set_material": (C.c_int, [_P, C.c_uint32, C.POINTER(Material), C.c_uint32]),
+    "vsim_set_contact": (C.c_int, [_P, C.c_int]),
+    "vsim_set_self_contact": (C.c_int, [_P, C.c_int]),
+    "vsim_set_gravity": (C.c_int, [_P, _D]),
+    "vsim_set_paused": (C.c_int, [_P, C.c_int]),
+    "vsim_set_step_duration": (C.c_int, [_P, C.c_double]),
+    "vsim_set_iterations": (C.c_int, [_P, C.c_uint32]),
+    "vsim_set_graph": (C.c_int, [_P, C.c_int]),
+    "vsim_set_launch_shape": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
+    "vsim_tune": (C.c_int, [_P, C.c_uint32, _U, _U]),
+    "vsim_set_pdl": (C.c_int, [_P, C.c_int]),
+    "vsim_kuhn_rest_inverse": (C.c_int, [_F]),
+    "vsim_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "vsim_cfl_number": (C.c_int, [_P, _D]),
+    "vsim_contact_pairs": (C.c_int, [_P, _U, _SZ, C.POINTER(_SZ)]),
+    "vsim_contact_surface": (C.c_int, [_P, _U, _U, _SZ, C.POINTER(_SZ)]),
+    "vsim_splats_bind": (C.c_int, [_P, C.c_uint32, _F, _F, _F, C.c_uint32]),
+    "vsim_splats_count": (C.c_uint32, [_P]),
+    "vsim_splats_deform": (C.c_int, [_P, _F]),
+    "vsim_splats_sort": (C.c_int, [_P]),
+    "vsim_splats_read": (C.c_int, [_P, _F, _F, _U, _SZ]),
+    "vsim_radix_sort_u32": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P, C.POINTER(_SZ), _P]),
+    "vsim_stable_step_duration": (C.c_int, [C.c_double, _D]),
+    "vsim_clock_create": (C.c_int, [C.c_double, C.c_uint32, C.POINTER(_P)]),
+    "vsim_clock_destroy": (C.c_int, [_P]),
+    "vsim_clock_consume": (C.c_int, [_P, C.c_double, C.c_int, C.POINTER(ClockReport)]),
+    "vsim_clock_idle": (C.c_int, [_P, C.POINTER(ClockReport)]),
+    "vsim_clock_single_step": (C.c_int, [_P, C.POINTER(ClockReport)]),
+    "vsim_clock_set_step_duration": (C.c_int, [_P, C.c_double]),
+    "vsim_clock_reset": (C.c_int, [_P]),
+    "vsim_clock_snapshot": (C.c_int, [_P, C.POINTER(ClockReport)]),
+    "vsim_lame_parameters": (C.c_int, [C.POINTER(Material), _D, _D]),
+    "vsim_element_compliance": (C.c_int, [C.POINTER(Material), C.c_double, _D, _D, _D]),
+    "vsim_collapse_scale": (C.c_double, [C.c_double]),
+    "vsim_wave_speed": (C.c_double, [C.POINTER(Material)]),
+}
+
+
+def header_symbols(header: Path = HEADER) -> list[str]:
+    """Every function the public header declares."""
+    text = header.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(vsim_[a-z0-9_]+)\s*\(", text)))
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded library with every signature declared."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"libvsim.so is not built ({LIB_PATH}); run __graft_entry__.build() first")
+        handle = C.CDLL(str(LIB_PATH))
+        for name, (restype, argtypes) in SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = restype
+            fn.argtypes = argtypes
+        _lib = handle
+    return _lib
+
+
+class VsimError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class VsimRangeError(VsimError, ValueError):
+    """The reference's RangeError."""
+
+
+def check(code: int) -> None:
+    if code == VSIM_OK:
+        return
+    msg = lib().vsim_last_error().decode()
+    if code == VSIM_ERR_RANGE:
+        raise VsimRangeError(code, msg)
+    raise VsimError(code, msg)
+
+
+def fptr(arr):
+    return arr.ctypes.data_as(_F) if arr is not None else None
+
+
+def uptr(arr):
+    return arr.ctypes.data_as(_U) if arr is not None else None
+
+
+def dptr(arr):
+    return arr.ctypes.data_as(_D) if arr is not None else None

@@ -116,7 +116,7 @@ def test_contact_pairs_bit_exact(lib):
     scene = sc.noise_blob(n=20, seed=5, splats=0)
     sim, orc = make(scene)
     pos, prev, vel = orc.state()
-    squashed = squeeze(pos, scene, 0.55)
+    squashed = squeeze(pos, scene, 0.4)
     for s in (sim, orc):
         s.write_state(squashed, pos, vel) if s is sim else s.set_state(squashed, pos, vel)
     gp = sim.contact_pairs()

@@ -1,0 +1,399 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 soft-body solver, one JSON line.
+
+Workload (N=1): one body, a seeded 64^3 value-noise blob (~130k occupied
+cells, 0.016 m cells, E log-uniform 1e4-1e6, nu 0.45, rho 1000) above a
+ground plane with self contact through the grid broadphase, carrying 1M
+Gaussian splats. One step is one rendered frame: 10 substeps of 1/600 s
+(predict, 8 colour passes, contact, finalize) then the deformation of every
+splat and the depth sort of their keys. Metric: cell-updates/s = occupied
+cells x substeps x Gauss-Seidel sweeps / time. Inputs are synthetic and
+seeded (the reference has no dataset for this path).
+
+Timing: W untimed frames, then K frames each bracketed by CUDA events on the
+solver's stream; between timed frames a 512 MiB buffer is written to flush
+the 129 MB L2. `e2e` repeats the frames through the public API with host
+buffers: each step uploads the node state from pinned host memory, runs the
+frame and reads the positions back.
+
+--impl reference times the oracle (the CPU restatement of the reference step,
+all host threads) on the same workload; the reference itself is WGSL for
+WebGPU and has no CPU step that could run.
+
+N>1 (torchrun): the workload does not shard (one body), so every rank runs
+an independent replica; value counts the cells of all replicas over the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for p in (ROOT / "visionary-sim_gb300", ROOT / "oracle"):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+METRIC = "cell-updates/s"
+BYTES_PER_ELASTIC_CELL = 8 * 48  # 8 corner nodes: pos 16 B read, prev 16 B read, pos 16 B written
+VIEW = (0.3, -0.25, -0.92)
+
+
+def peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        d = json.loads(path.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """dram bytes per elastic launch from the committed ncu summary, or None."""
+    path = ROOT / "profiles" / "elastic_pass_blob64.md"
+    if not path.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", path.read_text())
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.device = device_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.device), "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+            self.out.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], [], set()
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, value in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                   parts[5:9]):
+                if value.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def headline_scene(quick: bool):
+    import vsim.scenes as sc
+
+    if quick:
+        return sc.noise_blob(n=24, seed=1, splats=50_000)
+    return sc.noise_blob(n=64, seed=1, splats=1_000_000)
+
+
+def units_per_frame(scene) -> int:
+    return scene.cells * scene.substeps * scene.iterations
+
+
+def run_frame(sim, scene):
+    sim.dispatch(scene.substeps)
+    if sim.splat_count:
+        sim.deform_splats(VIEW)
+        sim.sort_splats()
+
+
+def time_frames(sim, scene, stream, frames: int, flush) -> list:
+    import torch
+
+    times = []
+    for _ in range(frames):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        run_frame(sim, scene)
+        end.record(stream)
+        end.synchronize()
+        times.append(start.elapsed_time(end) / 1e3)
+    return times
+
+
+def roofline(sim, scene, hbm):
+    prof = sim.profile_frame(scene.substeps, splats=True, view_dir=VIEW)
+    ms, launches = prof["elastic"]
+    cells = int(sim.color_counts().sum()) * scene.iterations * scene.substeps
+    per_launch_bytes = cells * BYTES_PER_ELASTIC_CELL / launches
+    per_launch_s = ms / 1e3 / launches
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    traffic = profiled_traffic()
+    share = {k: round(v[0] / sum(x[0] for x in prof.values()), 4) for k, v in prof.items()}
+    return {
+        "bound": "hbm",
+        "kernel": "elasticKernel (one colour pass)",
+        "achieved": round(achieved, 1),
+        "peak": hbm,
+        "unit": "GB/s",
+        "frac": round(achieved / hbm, 4),
+        "traffic": traffic,
+        "bytes_per_launch": round(per_launch_bytes),
+        "avg_launch_us": round(per_launch_s * 1e6, 3),
+    }, {k: {"ms": round(v[0], 4), "launches": v[1]} for k, v in prof.items()}, share
+
+
+def e2e(sim, scene, frames: int):
+    """The same frames through the public API with host buffers: upload the
+    node state from pinned memory, run the frame, read the positions back."""
+    import torch
+
+    n = sim.node_count
+    pinned = [torch.empty((n, 4), dtype=torch.float32, pin_memory=True) for _ in range(4)]
+    pos, prev, vel = sim.read_state()
+    for buf, src in zip(pinned[:3], (pos, prev, vel)):
+        buf.numpy()[:] = src
+    out = pinned[3].numpy()
+    h = [b.numpy() for b in pinned[:3]]
+    from vsim._ffi import check, fptr, lib
+
+    times = []
+    for _ in range(frames):
+        t0 = time.perf_counter()
+        check(lib().vsim_write_state(sim.handle, fptr(h[0]), fptr(h[1]), fptr(h[2]), n))
+        run_frame(sim, scene)
+        check(lib().vsim_read_positions(sim.handle, fptr(out), n))
+        times.append(time.perf_counter() - t0)
+    return times, 3 * n * 16, n * 16
+
+
+def cpu_baseline(scene, budget_s: float = 12.0):
+    import pyoracle
+
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    orc = pyoracle.Oracle(scene, 32)
+    splats = scene.splats.get(0)
+    frames, t0 = 0, time.perf_counter()
+    while True:
+        orc.dispatch(scene.substeps)
+        if splats is not None:
+            m, q, s, *_ = splats
+            _means, _cov, keys = orc.splat_deform(0, m, q, s, VIEW)
+            pyoracle.stable_sort(keys)
+        frames += 1
+        elapsed = time.perf_counter() - t0
+        if elapsed >= budget_s or frames >= 50:
+            break
+    value = units_per_frame(scene) * frames / elapsed
+    return {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{frames} full frames ({scene.substeps} substeps + {len(splats[0]) if splats else 0} "
+                      f"splat deformations and sort) of the bench workload, float oracle, "
+                      f"{elapsed:.1f} s"}
+
+
+def reference_arm(scene, steps: int, warmup: int):
+    """The oracle, all host threads, W untimed then K timed frames of the
+    bench workload (each a full frame: substeps, splat deformation, sort)."""
+    import pyoracle
+
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    orc = pyoracle.Oracle(scene, 32)
+    m, q, s, *_ = scene.splats[0]
+
+    def frame():
+        orc.dispatch(scene.substeps)
+        _means, _cov, keys = orc.splat_deform(0, m, q, s, VIEW)
+        pyoracle.stable_sort(keys)
+
+    for _ in range(warmup):
+        frame()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        frame()
+    elapsed = time.perf_counter() - t0
+    return {"value": units_per_frame(scene) * steps / elapsed, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{steps} timed frames after {warmup} warm-up frames of the bench workload, float oracle, "
+                      f"{elapsed:.1f} s"}
+
+
+def batched_vs_plain(frames: int, quick: bool):
+    """256 uneven boxes: one simulator stepping all of them with a captured
+    graph, against one simulator per body launched kernel by kernel."""
+    import torch
+
+    import vsim.scenes as sc
+    from vsim import Simulator
+
+    scene = sc.box_batch(32 if quick else 256, seed=2)
+    units = units_per_frame(scene)
+    batch = Simulator(scene)
+    singles = []
+    for b in scene.bodies:
+        one = sc.Scene([b], scene.tank, step_duration=scene.step_duration, substeps=scene.substeps, contact=False)
+        sim = Simulator(one)
+        sim.set_graph(False)
+        sim.set_pdl(False)
+        singles.append(sim)
+    for _ in range(2):
+        batch.dispatch(scene.substeps)
+        for s in singles:
+            s.dispatch(scene.substeps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        batch.dispatch(scene.substeps)
+    batch.synchronize()
+    t_batch = (time.perf_counter() - t0) / frames
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        for s in singles:
+            s.dispatch(scene.substeps)
+    for s in singles:
+        s.synchronize()
+    t_plain = (time.perf_counter() - t0) / frames
+    out = {"workload": f"{len(scene.bodies)} boxes, sides log-uniform 4-48 cells, {scene.cells} cells, "
+                       f"ground contact, 10 substeps/frame",
+           "batched": round(units / t_batch), "plain": round(units / t_plain),
+           "ratio": round(t_plain / t_batch, 2), "unit": METRIC}
+    for s in singles:
+        s.destroy()
+    batch.destroy()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="vsim", choices=["vsim", "reference"])
+    ap.add_argument("--quick", action="store_true", help="small workload, for checking the harness")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    scene = headline_scene(args.quick)
+    config = {"workload": ("noise blob %d^3 (%d cells), self contact + ground, %d splats; one frame = %d "
+                           "substeps + splat deformation + depth sort" %
+                           (scene.bodies[0].cell_dims[0], scene.cells, len(scene.splats[0][0]), scene.substeps)),
+              "cells": scene.cells, "substeps": scene.substeps, "iterations": scene.iterations,
+              "splats": len(scene.splats[0][0]), "l2": "flushed between timed frames (512 MiB write)",
+              "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        base = reference_arm(scene, args.steps, args.warmup)
+        line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": METRIC,
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * units_per_frame(scene) / base["value"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": config, "cpu_baseline": base,
+                "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from vsim import Simulator
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream()
+    sim = Simulator(scene, stream=stream.cuda_stream)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        run_frame(sim, scene)
+    sim.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    with ClockSampler(local) as clocks:
+        times = time_frames(sim, scene, stream, args.steps, flush)
+    torch.cuda.synchronize()
+    total = float(sum(times))
+    if world > 1:
+        t = torch.tensor([total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+        dist.barrier()
+    units = units_per_frame(scene) * args.steps * world
+    value = units / total
+    launches = args.steps * (sim.frame_launches(scene.substeps) + sim.splat_launches())
+
+    hbm, peak_kind = peaks()
+    roof, groups, share = roofline(sim, scene, hbm)
+    roof["peak_source"] = f"{peak_kind} hbm_gbs"
+    e2e_times, h2d, d2h = e2e(sim, scene, max(3, args.steps // 2))
+    e2e_value = units_per_frame(scene) / statistics.mean(e2e_times) * world
+
+    detail = {"kernel_groups_one_frame": groups, "time_share": share,
+              "frame_ms": {"min": round(min(times) * 1e3, 4), "median": round(statistics.median(times) * 1e3, 4)}}
+    if rank == 0 and not args.no_batch:
+        detail["batching"] = batched_vs_plain(3, args.quick)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(scene)
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value), "unit": METRIC, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": config, "gpu_launches": launches, "clocks": clocks.summary(), "roofline": roof,
+                "cpu_baseline": cpu,
+                "e2e": {"value": round(e2e_value), "unit": METRIC, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "detail": detail}
+        print(json.dumps(line))
+    sim.destroy()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

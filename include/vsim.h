@@ -263,6 +263,37 @@ int vsim_contact_pairs(vsim_sim* sim, uint32_t* pairs, size_t capacity, size_t* 
 int vsim_contact_surface(vsim_sim* sim, uint32_t* nodes, uint32_t* bodies, size_t capacity,
                          size_t* count);
 
+/* ---- profiling ---------------------------------------------------------- */
+
+/* Kernel groups a frame is made of. */
+#define VSIM_KIND_PREDICT 0
+#define VSIM_KIND_DRIVE 1
+#define VSIM_KIND_ELASTIC 2   /* the colour passes */
+#define VSIM_KIND_LIMIT 3     /* limit-only stretch sweeps */
+#define VSIM_KIND_CONTACT 4   /* bin, segment, scatter, order, collide, settle */
+#define VSIM_KIND_FINALIZE 5
+#define VSIM_KIND_SPLAT 6     /* splat deformation */
+#define VSIM_KIND_SORT 7      /* splat depth sort */
+#define VSIM_KIND_COUNT 8
+
+typedef struct vsim_profile {
+    double ms[VSIM_KIND_COUNT];          /* summed device time per group */
+    uint32_t launches[VSIM_KIND_COUNT];  /* kernels launched per group */
+} vsim_profile;
+
+/* Run one frame of `steps` substeps (plus the splat deformation and sort
+   when `with_splats`) with every kernel launched on its own, bracketed by
+   CUDA events on the handle's stream, and report the device time of each
+   kernel group. The frame advances the simulation like vsim_dispatch. */
+int vsim_profile_frame(vsim_sim* sim, uint32_t steps, int with_splats, const float view_dir[3],
+                       vsim_profile* out);
+/* Occupied cells per colour over all bodies (a colour pass's work). */
+int vsim_color_counts(const vsim_sim* sim, uint32_t out[8]);
+/* Kernels a frame of `steps` substeps launches (splats excluded). */
+uint32_t vsim_frame_launches(const vsim_sim* sim, uint32_t steps);
+/* Kernels one splat deformation plus sort launches. */
+uint32_t vsim_splat_launches(const vsim_sim* sim);
+
 /* ---- splats (sample.wgsl:40-80, covariance.wgsl:30-42) ---------------- */
 
 /*

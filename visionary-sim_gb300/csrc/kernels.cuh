@@ -14,9 +14,10 @@ struct DeviceState {
     float4* prev = nullptr;       // position at the start of the substep
     float4* vel = nullptr;
     float* baseW = nullptr;       // material inverse mass with static nodes zeroed
-    uint32_t* active = nullptr;   // nodes with material that are not static
+    uint32_t* active = nullptr;   // nodes with material (predict and finalize visit these)
     uint32_t* activeBody = nullptr;
-    uint2* cells = nullptr;       // colour-major (corner-0 node, body)
+    int32_t* nodeRecord = nullptr;  // surface record of each node, -1 for none
+    uint4* cells = nullptr;       // colour-major (corner-0 node, body, y stride, z stride)
     DevBody* bodies = nullptr;
     FrameParams* fp = nullptr;
     // contact
@@ -28,6 +29,9 @@ struct DeviceState {
     uint32_t* start = nullptr;    // per bucket
     uint32_t* cursor = nullptr;
     float4* delta = nullptr;
+    uint4* sMeta = nullptr;       // visible bucket entries in bucket order: their records
+    float4* sPos = nullptr;       //   ... and their nodes' positions
+    uint32_t* sRec = nullptr;     //   ... and their record indices
     // drive
     uint32_t* driven = nullptr;
     float4* drivenOffset = nullptr;
@@ -36,6 +40,7 @@ struct DeviceState {
 struct LaunchCtx {
     cudaStream_t stream;
     bool pdl;
+    uint32_t sms;  // multiprocessors of the device
 };
 
 // Rest lengths of the cube's edges, face and body diagonals (stretch.js:5-7),
@@ -50,9 +55,13 @@ void kuhnTable(float out[54]);
 
 cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount);
 cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drivenCount);
-cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint2* cells, uint32_t count,
+cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, uint32_t count,
                           bool limitOnly, uint32_t block, const StretchLengths& lens);
-cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount);
+// The substep's closing pass; with `contact` it first applies the contact
+// corrections and empties the grid, with `predictNext` it goes on into the
+// next substep's prediction.
+cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount, bool contact,
+                           bool predictNext);
 cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, uint32_t surfaceCount, ContactMode mode,
                           uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount);
 cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos);

@@ -61,6 +61,7 @@ struct vsim_sim {
     cudaStream_t stream = nullptr;
     bool ownStream = false;
     cudaStream_t capture = nullptr;
+    uint32_t sms = 1;
 
     // topology
     std::vector<Lattice> lat;
@@ -221,7 +222,7 @@ int syncParams(vsim_sim* s) {
 // The cell list, colour-major over bodies (elasticCells.js:143-163). Inside a
 // colour and body the cells run in lattice order, or brick by brick when
 // `brick` is 4 or 8 (bricks of that many cells per axis).
-void buildCells(vsim_sim* s, std::vector<uint2>& out) {
+void buildCells(vsim_sim* s, std::vector<uint4>& out) {
     out.clear();
     out.reserve(s->cellCount);
     for (int c = 0; c < 8; c++) {
@@ -243,38 +244,104 @@ void buildCells(vsim_sim* s, std::vector<uint2>& out) {
             for (uint32_t cell : order) {
                 const uint32_t i = cell % L.cellDims[0], j = (cell / L.cellDims[0]) % L.cellDims[1],
                                k = cell / (L.cellDims[0] * L.cellDims[1]);
-                out.push_back(make_uint2(s->offsets[b] + i + L.nodeDims[0] * (j + L.nodeDims[1] * k), uint32_t(b)));
+                out.push_back(make_uint4(s->offsets[b] + i + L.nodeDims[0] * (j + L.nodeDims[1] * k), uint32_t(b),
+                                         L.nodeDims[0], L.nodeDims[0] * L.nodeDims[1]));
             }
         }
     }
     s->colorStart[8] = uint32_t(out.size());
 }
 
+// Brackets kernel groups with events on the launching stream.
+struct Profiler {
+    cudaStream_t stream;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    struct Span {
+        int kind;
+        cudaEvent_t a, b;
+        uint32_t launches;
+    };
+    std::vector<Span> spans;
+    cudaEvent_t next() {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    void begin(int kind, uint32_t launches) {
+        Span sp{kind, next(), nullptr, launches};
+        cudaEventRecord(sp.a, stream);
+        spans.push_back(sp);
+    }
+    void end() {
+        spans.back().b = next();
+        cudaEventRecord(spans.back().b, stream);
+    }
+    ~Profiler() {
+        for (cudaEvent_t e : pool) cudaEventDestroy(e);
+    }
+};
+
+constexpr uint32_t kContactKernels = 5;  // bin, segment, scatter, order, collide
+
 // stepper.js:101-108 with simulator.js:83's constraint order.
-cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMode mode = ContactMode::Solve) {
-    const LaunchCtx c{st, s->pdl};
+cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMode mode = ContactMode::Solve,
+                        Profiler* prof = nullptr) {
+    const LaunchCtx c{st, s->pdl, s->sms};
     const StretchLengths lens = stretchLengths();
     const bool limited = anyStretch(s);
     const bool driving = !s->held.empty();
     const bool contact = s->contact && s->surfaceCount > 0;
     cudaError_t e;
-    for (uint32_t step = 0; step < steps; step++) {
+    auto begin = [&](int kind, uint32_t launches) {
+        if (prof) prof->begin(kind, launches);
+    };
+    auto end = [&]() {
+        if (prof) prof->end();
+    };
+    // The first substep's prediction runs on its own; every later one rides
+    // on the closing pass of the substep before it.
+    if (steps > 0) {
+        begin(VSIM_KIND_PREDICT, 1);
         if ((e = launchPredict(c, s->d, s->activeCount))) return e;
-        if (driving && (e = launchDrive(c, s->d, VSIM_MAX_DRIVEN))) return e;
+        end();
+    }
+    for (uint32_t step = 0; step < steps; step++) {
+        if (driving) {
+            begin(VSIM_KIND_DRIVE, 1);
+            if ((e = launchDrive(c, s->d, VSIM_MAX_DRIVEN))) return e;
+            end();
+        }
         for (uint32_t it = 0; it < s->iterations; it++)
             for (int col = 0; col < 8; col++) {
                 const uint32_t n = s->colorStart[col + 1] - s->colorStart[col];
-                if (n && (e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], n, false, s->block, lens))) return e;
+                if (!n) continue;
+                begin(VSIM_KIND_ELASTIC, 1);
+                if ((e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], n, false, s->block, lens))) return e;
+                end();
             }
         if (limited)
             for (int sweep = 0; sweep < 3; sweep++)
                 for (int col = 0; col < 8; col++) {
                     const uint32_t n = s->colorStart[col + 1] - s->colorStart[col];
-                    if (n && (e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], n, true, s->block, lens)))
+                    if (!n) continue;
+                    begin(VSIM_KIND_LIMIT, 1);
+                    if ((e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], n, true, s->block, lens)))
                         return e;
+                    end();
                 }
-        if (contact && (e = launchContact(c, s->d, s->surfaceCount, mode, nullptr, 0, nullptr))) return e;
-        if ((e = launchFinalize(c, s->d, s->activeCount))) return e;
+        if (contact) {
+            begin(VSIM_KIND_CONTACT, kContactKernels);
+            if ((e = launchContact(c, s->d, s->surfaceCount, mode, nullptr, 0, nullptr))) return e;
+            end();
+        }
+        begin(VSIM_KIND_FINALIZE, 1);
+        if ((e = launchFinalize(c, s->d, s->activeCount, contact && mode == ContactMode::Solve, step + 1 < steps)))
+            return e;
+        end();
     }
     return cudaSuccess;
 }
@@ -334,7 +401,7 @@ void freeAll(vsim_sim* s) {
     DeviceState& d = s->d;
     void* ptrs[] = {d.pos, d.prev, d.vel, d.baseW, d.active, d.activeBody, d.cells, d.bodies, d.fp,
                     d.surf, d.key, d.rank, d.entries, d.count, d.start, d.cursor, d.delta, d.driven,
-                    d.drivenOffset, s->staging, s->pairs, s->pairCount, s->sp.embed, s->sp.quat,
+                    d.drivenOffset, d.nodeRecord, d.sMeta, d.sPos, d.sRec, s->staging, s->pairs, s->pairCount, s->sp.embed, s->sp.quat,
                     s->sp.scaleBody, s->sp.bodies, s->sp.meanDepth, s->sp.cov, s->sp.keys, s->sp.order,
                     s->sp.sortTemp};
     for (void* p : ptrs)
@@ -361,6 +428,9 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
     int major = 0;
     CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, s->device), "query device");
     if (major < 10) return fail(VSIM_ERR_INVALID, "libvsim is built for sm_103a (GB300) only");
+    int sms = 1;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device), "query device");
+    s->sms = uint32_t(sms);
     if (tank) {
         s->tank = *tank;
     } else {
@@ -396,12 +466,14 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
     s->baseW.resize(total);
     for (uint64_t i = 0; i < total; i++) s->baseW[i] = s->isStatic[i] ? 0.0f : s->invMass[i];
 
-    // Active nodes: material and not static (predict and finalize skip the rest).
+    // Active nodes: every node with material. Predict and finalize skip those
+    // whose solver inverse mass is zero, as the reference does; the closing
+    // pass still settles and un-bins the static ones on the surface.
     std::vector<uint32_t> active, activeBody;
     for (uint32_t b = 0; b < n; b++)
         for (uint32_t m = 0; m < s->lat[b].nodeCount; m++) {
             const uint32_t node = s->offsets[b] + m;
-            if (s->baseW[node] > 0) {
+            if (s->invMass[node] > 0) {
                 active.push_back(node);
                 activeBody.push_back(b);
             }
@@ -462,6 +534,10 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
     CK(allocN(&d.rank, s->surfaceCount), "allocate contact ranks");
     CK(allocN(&d.entries, s->surfaceCount), "allocate contact entries");
     CK(allocN(&d.delta, s->surfaceCount), "allocate contact deltas");
+    CK(allocN(&d.sMeta, s->surfaceCount), "allocate contact runs");
+    CK(allocN(&d.sPos, s->surfaceCount), "allocate contact runs");
+    CK(allocN(&d.sRec, s->surfaceCount), "allocate contact runs");
+    CK(allocN(&d.nodeRecord, N), "allocate node records");
     CK(allocN(&d.count, s->grid.count()), "allocate contact grid");
     CK(allocN(&d.start, s->grid.count()), "allocate contact grid");
     CK(allocN(&d.cursor, 1), "allocate contact cursor");
@@ -481,8 +557,11 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
             s->restPos[4 * node + 3] = s->baseW[node];
         }
     }
-    std::vector<uint2> cells;
+    std::vector<uint4> cells;
     buildCells(s, cells);
+    std::vector<int32_t> nodeRecord(N, -1);
+    for (uint32_t r = 0; r < s->surfaceCount; r++) nodeRecord[s->surfHost[r].x] = int32_t(r);
+    CK(cudaMemcpyAsync(d.nodeRecord, nodeRecord.data(), N * 4, cudaMemcpyHostToDevice, s->stream), "upload records");
     CK(cudaMemcpyAsync(d.pos, s->restPos.data(), N * 16, cudaMemcpyHostToDevice, s->stream), "upload state");
     CK(cudaMemcpyAsync(d.prev, s->restPos.data(), N * 16, cudaMemcpyHostToDevice, s->stream), "upload state");
     CK(cudaMemsetAsync(d.vel, 0, N * 16, s->stream), "upload state");
@@ -490,7 +569,7 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
     CK(cudaMemcpyAsync(d.active, active.data(), active.size() * 4, cudaMemcpyHostToDevice, s->stream), "upload");
     CK(cudaMemcpyAsync(d.activeBody, activeBody.data(), activeBody.size() * 4, cudaMemcpyHostToDevice, s->stream),
        "upload");
-    CK(cudaMemcpyAsync(d.cells, cells.data(), cells.size() * 8, cudaMemcpyHostToDevice, s->stream), "upload cells");
+    CK(cudaMemcpyAsync(d.cells, cells.data(), cells.size() * 16, cudaMemcpyHostToDevice, s->stream), "upload cells");
     CK(cudaMemcpyAsync(d.surf, s->surfHost.data(), s->surfHost.size() * 16, cudaMemcpyHostToDevice, s->stream),
        "upload surface");
     CK(cudaMemsetAsync(d.count, 0, s->grid.count() * 4, s->stream), "clear grid");
@@ -821,9 +900,9 @@ int vsim_set_launch_shape(vsim_sim* s, uint32_t block, uint32_t brick) {
     s->block = block;
     if (brick != s->brick) {
         s->brick = brick;
-        std::vector<uint2> cells;
+        std::vector<uint4> cells;
         buildCells(s, cells);
-        CK(cudaMemcpyAsync(s->d.cells, cells.data(), cells.size() * 8, cudaMemcpyHostToDevice, s->stream),
+        CK(cudaMemcpyAsync(s->d.cells, cells.data(), cells.size() * 16, cudaMemcpyHostToDevice, s->stream),
            "upload cells");
         CK(cudaStreamSynchronize(s->stream), "upload cells");
     }
@@ -934,7 +1013,7 @@ int vsim_contact_pairs(vsim_sim* s, uint32_t* pairs, size_t capacity, size_t* co
     int rc = syncParams(s);
     if (rc) return rc;
     CK(cudaMemsetAsync(s->pairCount, 0, sizeof(unsigned long long), s->stream), "count pairs");
-    const LaunchCtx c{s->stream, false};
+    const LaunchCtx c{s->stream, false, s->sms};
     CK(launchContact(c, s->d, s->surfaceCount, ContactMode::Pairs, s->pairs, uint32_t(capacity), s->pairCount),
        "list pairs");
     unsigned long long total = 0;
@@ -967,6 +1046,69 @@ int vsim_kuhn_rest_inverse(float out[54]) {
 int vsim_set_pdl(vsim_sim* s, int enabled) {
     SIM_GUARD(s);
     s->pdl = enabled != 0;
+    return VSIM_OK;
+}
+
+int vsim_color_counts(const vsim_sim* s, uint32_t out[8]) {
+    if (!s || !out) return fail(VSIM_ERR_INVALID, "NULL argument");
+    for (int c = 0; c < 8; c++) out[c] = s->colorStart[c + 1] - s->colorStart[c];
+    return VSIM_OK;
+}
+
+uint32_t vsim_frame_launches(const vsim_sim* s, uint32_t steps) {
+    if (!s) return 0;
+    uint32_t colours = 0;
+    for (int c = 0; c < 8; c++) colours += s->colorStart[c + 1] > s->colorStart[c] ? 1 : 0;
+    uint32_t per = 1 + colours * s->iterations;
+    if (!s->held.empty()) per += 1;
+    if (anyStretch(s)) per += 3 * colours;
+    if (s->contact && s->surfaceCount > 0) per += kContactKernels;
+    return steps ? 1 + per * steps : 0;
+}
+
+uint32_t vsim_splat_launches(const vsim_sim* s) {
+    if (!s || s->splatCount == 0) return 0;
+    return 1 + 5 * 4;  // deformation, then four 8-bit passes of five kernels
+}
+
+int vsim_profile_frame(vsim_sim* s, uint32_t steps, int with_splats, const float view_dir[3], vsim_profile* out) {
+    SIM_GUARD(s);
+    if (!out) return fail(VSIM_ERR_INVALID, "out is NULL");
+    std::memset(out, 0, sizeof *out);
+    if (steps < 1) return VSIM_OK;
+    if (!s->held.empty()) {
+        const double frameDt = steps * s->clock.stepDuration;
+        for (int a = 0; a < 3; a++) s->grabVel[a] = (s->grabPos[a] - s->grabPrev[a]) / frameDt;
+        std::memcpy(s->grabPrev, s->grabPos, sizeof s->grabPos);
+        s->frameDirty = true;
+    }
+    int rc = syncParams(s);
+    if (rc) return rc;
+    Profiler prof;
+    prof.stream = s->stream;
+    const bool pdl = s->pdl;
+    s->pdl = false;
+    const cudaError_t enc = encodeFrame(s, s->stream, steps, ContactMode::Solve, &prof);
+    s->pdl = pdl;
+    CK(enc, "profile frame");
+    if (with_splats && s->splatCount) {
+        const float v[3] = {view_dir ? view_dir[0] : 0.0f, view_dir ? view_dir[1] : 0.0f,
+                            view_dir ? view_dir[2] : -1.0f};
+        prof.begin(VSIM_KIND_SPLAT, 1);
+        CK(launchSplatDeform(s->stream, s->sp, s->d.pos, s->splatCount, v[0], v[1], v[2]), "profile splats");
+        prof.end();
+        prof.begin(VSIM_KIND_SORT, 20);
+        CK(radixSortU32(s->sp.keys, s->sp.order, s->splatCount, 32, s->sp.sortTemp, s->sp.sortTempBytes, s->stream),
+           "profile sort");
+        prof.end();
+    }
+    CK(cudaStreamSynchronize(s->stream), "profile frame");
+    for (const auto& sp : prof.spans) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, sp.a, sp.b), "profile timing");
+        out->ms[sp.kind] += ms;
+        out->launches[sp.kind] += sp.launches;
+    }
     return VSIM_OK;
 }
 

@@ -198,20 +198,21 @@ __global__ void driveKernel(const FrameParams* __restrict__ fp, const uint32_t* 
 }
 
 // project.wgsl:35-184: one colour pass, one thread per occupied cell.
-// `cells` holds (global node of corner 0, body) per cell of this colour.
+// `cells` holds (global node of corner 0, body, node stride along y, along z)
+// per cell of this colour, so the corner loads wait on one load only.
 template <bool LIMIT_ONLY>
-__global__ void __launch_bounds__(512) elasticKernel(const uint2* __restrict__ cells, uint32_t count,
+__global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ cells, uint32_t count,
                                                      const DevBody* __restrict__ bodies, float4* __restrict__ pos,
                                                      const float4* __restrict__ prevState, StretchLengths lens) {
     pdlWait();
     pdlLaunchNext();
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= count) return;
-    const uint2 entry = cells[slot];
+    const uint4 entry = cells[slot];
     const DevBody* b = bodies + entry.y;
     const float maxStretch = b->maxStretch;
     if (LIMIT_ONLY && !(maxStretch > 1.0f)) return;
-    const uint32_t nx = b->nx, nxy = b->nxy, n0 = entry.x;
+    const uint32_t nx = entry.z, nxy = entry.w, n0 = entry.x;
     const uint32_t ids[8] = {n0, n0 + 1, n0 + nx, n0 + nx + 1, n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
     V p[8], prev[8];
     float w[8];
@@ -274,16 +275,39 @@ __device__ __forceinline__ V resolvePlane(V p, V prev, V normal, float depth, fl
 
 // finalize.wgsl:44-74 over the active nodes; the velocity factor
 // exp(-damping dt) is the body's, evaluated once on the host.
+//
+// With CONTACT the pass first does what settle.wgsl:20-36 does for a node
+// with a surface record -- apply its averaged contact correction, empty its
+// bucket -- so no separate pass runs between contact and the closing pass.
+// With PREDICT it continues straight into the next substep's
+// predict.wgsl:19-36 from the position and velocity it has just computed,
+// which are the values that pass would read back.
+template <bool CONTACT, bool PREDICT>
 __global__ void finalizeKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ active,
                                const uint32_t* __restrict__ activeBody, const DevBody* __restrict__ bodies,
-                               float4* __restrict__ pos, const float4* __restrict__ prevState,
-                               float4* __restrict__ vel) {
+                               float4* __restrict__ pos, float4* __restrict__ prevState, float4* __restrict__ vel,
+                               const int32_t* __restrict__ nodeRecord, const float4* __restrict__ delta,
+                               const uint32_t* __restrict__ key, uint32_t* __restrict__ count,
+                               uint32_t* __restrict__ cursor) {
     pdlWait();
     pdlLaunchNext();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= fp->activeCount) return;
     const uint32_t n = active[i];
-    const float4 P = pos[n];
+    float4 P = pos[n];
+    if (CONTACT) {
+        if (i == 0) *cursor = 0;
+        const int32_t r = nodeRecord[n];
+        if (r >= 0) {
+            const float4 d = delta[r];
+            if (d.w > 0.0f) {
+                const V step = xyz(d) * (1.0f / d.w);
+                P = withW(xyz(P) + step, P.w);
+                if (P.w == 0.0f) pos[n] = P;
+            }
+            count[key[r]] = 0;
+        }
+    }
     if (P.w == 0.0f) return;
     const DevBody* b = bodies + activeBody[i];
     const V prev = xyz(prevState[n]);
@@ -296,10 +320,19 @@ __global__ void finalizeKernel(const FrameParams* __restrict__ fp, const uint32_
     p = resolvePlane(p, prev, mk(-1.0f, 0.0f, 0.0f), p.x - mx.x, fr);
     p = resolvePlane(p, prev, mk(0.0f, 0.0f, 1.0f), mn.z - p.z, fr);
     p = resolvePlane(p, prev, mk(0.0f, 0.0f, -1.0f), p.z - mx.z, fr);
-    pos[n] = withW(p, P.w);
-    V v = (p - prev) / fp->dt;
+    const float dt = fp->dt;
+    V v = (p - prev) / dt;
     v = v * b->damp;
-    vel[n] = withW(v, 0.0f);
+    if (PREDICT) {
+        const V g = mk(fp->gx, fp->gy, fp->gz);
+        const V v2 = v + g * dt;
+        prevState[n] = withW(p, 0.0f);
+        pos[n] = withW(p + v2 * dt, P.w);
+        vel[n] = withW(v2, 0.0f);
+    } else {
+        pos[n] = withW(p, P.w);
+        vel[n] = withW(v, 0.0f);
+    }
 }
 
 // ------------------------------------------------------------- contact --
@@ -387,19 +420,30 @@ __global__ void scatterKernel(const FrameParams* __restrict__ fp, const uint32_t
 }
 
 // sort.wgsl:14-53: the bucket's visible entries -- its kBucketSlots lowest
-// record indices -- in ascending order at the front of its segment.
+// record indices -- in ascending order at the front of its segment; then
+// their records and positions copied out in that order, so the gather reads
+// each neighbour bucket as one contiguous run.
 __global__ void canonKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ key,
                             const uint32_t* __restrict__ rank, const uint32_t* __restrict__ start,
-                            const uint32_t* __restrict__ count, uint32_t* __restrict__ entries) {
+                            const uint32_t* __restrict__ count, uint32_t* __restrict__ entries,
+                            const uint4* __restrict__ surf, const float4* __restrict__ pos, uint4* __restrict__ sMeta,
+                            float4* __restrict__ sPos, uint32_t* __restrict__ sRec) {
     pdlWait();
     pdlLaunchNext();
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= fp->surfaceCount || rank[r] != 0) return;
     const uint32_t b = key[r];
     const uint32_t n = count[b];
-    if (n < 2) return;
-    uint32_t* e = entries + start[b];
+    const uint32_t base = start[b];
+    uint32_t* e = entries + base;
     const uint32_t m = n < kBucketSlots ? n : kBucketSlots;
+    if (n < 2) {
+        const uint4 rec = surf[r];
+        sMeta[base] = rec;
+        sPos[base] = pos[rec.x];
+        sRec[base] = r;
+        return;
+    }
     for (uint32_t i = 1; i < m; i++) {
         const uint32_t v = e[i];
         uint32_t at = i;
@@ -421,6 +465,13 @@ __global__ void canonKernel(const FrameParams* __restrict__ fp, const uint32_t* 
         }
         e[at] = v;
     }
+    for (uint32_t k = 0; k < m; k++) {
+        const uint32_t other = e[k];
+        const uint4 rec = surf[other];
+        sMeta[base + k] = rec;
+        sPos[base + k] = pos[rec.x];
+        sRec[base + k] = other;
+    }
 }
 
 // Whether records a and b may touch: the reference drops every same-body
@@ -437,13 +488,16 @@ __device__ __forceinline__ bool admitted(uint4 a, uint4 b, uint32_t selfContact)
     return false;
 }
 
-// collide.wgsl:16-125. With `pairs` set, every counted hit (r, other) is also
-// appended there (capacity-checked), for the pair-set checks.
+// collide.wgsl:16-125, reading each neighbour bucket's visible entries as
+// the contiguous run canonKernel laid out. With EMIT, every counted hit
+// (r, other) is also appended to `pairs` (capacity-checked), for the
+// pair-set checks.
 template <bool EMIT>
 __global__ void collideKernel(const FrameParams* __restrict__ fp, const uint4* __restrict__ surf,
                               const DevBody* __restrict__ bodies, const float4* __restrict__ pos,
                               const float4* __restrict__ prevState, const uint32_t* __restrict__ start,
-                              const uint32_t* __restrict__ count, const uint32_t* __restrict__ entries,
+                              const uint32_t* __restrict__ count, const uint4* __restrict__ sMeta,
+                              const float4* __restrict__ sPos, const uint32_t* __restrict__ sRec,
                               float4* __restrict__ delta, uint32_t* __restrict__ pairs, uint32_t capacity,
                               unsigned long long* __restrict__ pairCount) {
     pdlWait();
@@ -464,26 +518,29 @@ __global__ void collideKernel(const FrameParams* __restrict__ fp, const uint4* _
     int centre[3];
     bucketOf(fp, pi, centre);
     const int dims[3] = {int(fp->gridDims[0]), int(fp->gridDims[1]), int(fp->gridDims[2])};
-    for (int dz = -1; dz <= 1; dz++) {
-        const int z = centre[2] + dz;
-        if (z < 0 || z >= dims[2]) continue;
-        for (int dy = -1; dy <= 1; dy++) {
-            const int y = centre[1] + dy;
-            if (y < 0 || y >= dims[1]) continue;
-            for (int dx = -1; dx <= 1; dx++) {
-                const int x = centre[0] + dx;
-                if (x < 0 || x >= dims[0]) continue;
-                const uint32_t bucket = uint32_t(x) + fp->gridDims[0] * (uint32_t(y) + fp->gridDims[1] * uint32_t(z));
-                const uint32_t n = count[bucket];
-                if (n == 0) continue;
-                const uint32_t held = n < kBucketSlots ? n : kBucketSlots;
-                const uint32_t* e = entries + start[bucket];
-                for (uint32_t k = 0; k < held; k++) {
-                    const uint32_t other = e[k];
-                    const uint4 them = surf[other];
+    // All 27 bucket counts first (independent loads), then the runs in
+    // the reference's dz, dy, dx order.
+    uint32_t cnt[27], bkt[27];
+#pragma unroll
+    for (int q = 0; q < 27; q++) {
+        const int x = centre[0] + q % 3 - 1, y = centre[1] + (q / 3) % 3 - 1, z = centre[2] + q / 9 - 1;
+        const bool inside = x >= 0 && x < dims[0] && y >= 0 && y < dims[1] && z >= 0 && z < dims[2];
+        bkt[q] = inside ? uint32_t(x) + fp->gridDims[0] * (uint32_t(y) + fp->gridDims[1] * uint32_t(z)) : 0u;
+        cnt[q] = inside ? count[bkt[q]] : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < 27; q++) {
+        {
+            const uint32_t n = cnt[q];
+            if (n == 0) continue;
+            const uint32_t held = n < kBucketSlots ? n : kBucketSlots;
+            const uint32_t at = start[bkt[q]];
+            for (uint32_t k = 0; k < held; k++) {
+                {
+                    const uint4 them = sMeta[at + k];
                     if (!admitted(me, them, selfContact)) continue;
                     const uint32_t mate = them.x;
-                    const float4 Q = pos[mate];
+                    const float4 Q = sPos[at + k];
                     const V pj = xyz(Q);
                     const V d = pi - pj;
                     const float dist2 = dot(d, d);
@@ -508,10 +565,11 @@ __global__ void collideKernel(const FrameParams* __restrict__ fp, const uint4* _
                     sum = sum + correction;
                     hits = hits + 1.0f;
                     if (EMIT) {
-                        const unsigned long long at = atomicAdd(pairCount, 1ull);
-                        if (at < capacity) {
-                            pairs[2 * at] = r;
-                            pairs[2 * at + 1] = other;
+                        const uint32_t other = sRec[at + k];
+                        const unsigned long long slot = atomicAdd(pairCount, 1ull);
+                        if (slot < capacity) {
+                            pairs[2 * slot] = r;
+                            pairs[2 * slot + 1] = other;
                         }
                     }
                 }
@@ -604,8 +662,16 @@ cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drive
     return launch(c, driveKernel, blocks(drivenCount, 256), 256, s.fp, s.driven, s.drivenOffset, s.pos, s.prev, s.vel);
 }
 
-cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint2* cells, uint32_t count,
+// A colour pass of a small scene has too few cells to put a block of the
+// configured size on every SM; smaller blocks spread it over all of them.
+inline uint32_t elasticBlock(uint32_t count, uint32_t block, uint32_t sms) {
+    while (block > 32 && blocks(count, block) < 2 * sms) block /= 2;
+    return block;
+}
+
+cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, uint32_t count,
                           bool limitOnly, uint32_t block, const StretchLengths& lens) {
+    block = elasticBlock(count, block, c.sms);
     if (limitOnly)
         return launch(c, elasticKernel<true>, blocks(count, block), block, cells, count, s.bodies, s.pos,
                       (const float4*)s.prev, lens);
@@ -613,11 +679,20 @@ cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint2*
                   (const float4*)s.prev, lens);
 }
 
-cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount) {
-    return launch(c, finalizeKernel, blocks(activeCount, 256), 256, s.fp, s.active, s.activeBody, s.bodies, s.pos,
-                  (const float4*)s.prev, s.vel);
+cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount, bool contact,
+                           bool predictNext) {
+    auto go = [&](auto kernel) {
+        return launch(c, kernel, blocks(activeCount, 256), 256, s.fp, s.active, s.activeBody, s.bodies, s.pos, s.prev,
+                      s.vel, (const int32_t*)s.nodeRecord, (const float4*)s.delta, (const uint32_t*)s.key, s.count,
+                      s.cursor);
+    };
+    if (contact) return predictNext ? go(finalizeKernel<true, true>) : go(finalizeKernel<true, false>);
+    return predictNext ? go(finalizeKernel<false, true>) : go(finalizeKernel<false, false>);
 }
 
+// Solve mode leaves the corrections in `delta` for the closing pass, which
+// applies them and empties the grid; Pairs mode lists the hits and empties
+// the grid itself.
 cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, uint32_t surfaceCount, ContactMode mode,
                           uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount) {
     const uint32_t g = blocks(surfaceCount, 256);
@@ -630,22 +705,22 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, uint32_t sur
                     (const uint32_t*)s.start, s.entries)))
         return e;
     if ((e = launch(c, canonKernel, g, 256, s.fp, (const uint32_t*)s.key, (const uint32_t*)s.rank,
-                    (const uint32_t*)s.start, (const uint32_t*)s.count, s.entries)))
+                    (const uint32_t*)s.start, (const uint32_t*)s.count, s.entries, (const uint4*)s.surf,
+                    (const float4*)s.pos, s.sMeta, s.sPos, s.sRec)))
         return e;
     if (mode == ContactMode::Pairs) {
         if ((e = launch(c, collideKernel<true>, g, 256, s.fp, s.surf, s.bodies, (const float4*)s.pos,
                         (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count,
-                        (const uint32_t*)s.entries, s.delta, pairs, capacity, pairCount)))
+                        (const uint4*)s.sMeta, (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, pairs,
+                        capacity, pairCount)))
             return e;
-    } else {
-        if ((e = launch(c, collideKernel<false>, g, 256, s.fp, s.surf, s.bodies, (const float4*)s.pos,
-                        (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count,
-                        (const uint32_t*)s.entries, s.delta, (uint32_t*)nullptr, 0u,
-                        (unsigned long long*)nullptr)))
-            return e;
+        return launch(c, settleKernel, g, 256, s.fp, s.surf, (const uint32_t*)s.key, (const float4*)s.delta, s.pos,
+                      s.count, s.cursor, 0);
     }
-    return launch(c, settleKernel, g, 256, s.fp, s.surf, (const uint32_t*)s.key, (const float4*)s.delta, s.pos,
-                  s.count, s.cursor, mode == ContactMode::Solve ? 1 : 0);
+    return launch(c, collideKernel<false>, g, 256, s.fp, s.surf, s.bodies, (const float4*)s.pos,
+                  (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count, (const uint4*)s.sMeta,
+                  (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, (uint32_t*)nullptr, 0u,
+                  (unsigned long long*)nullptr);
 }
 
 cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos) {

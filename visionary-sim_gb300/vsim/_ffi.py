@@ -87,6 +87,13 @@ class Stats(C.Structure):
     ]
 
 
+class Profile(C.Structure):
+    _fields_ = [("ms", C.c_double * 8), ("launches", C.c_uint32 * 8)]
+
+
+KINDS = ("predict", "drive", "elastic", "limit", "contact", "finalize", "splat", "sort")
+
+
 class ClockReport(C.Structure):
     _fields_ = [
         ("step_duration", C.c_double),
@@ -152,6 +159,10 @@ SIGNATURES = {
     "vsim_splats_sort": (C.c_int, [_P]),
     "vsim_splats_read": (C.c_int, [_P, _F, _F, _U, _SZ]),
     "vsim_radix_sort_u32": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P, C.POINTER(_SZ), _P]),
+    "vsim_profile_frame": (C.c_int, [_P, C.c_uint32, C.c_int, _F, C.POINTER(Profile)]),
+    "vsim_color_counts": (C.c_int, [_P, _U]),
+    "vsim_frame_launches": (C.c_uint32, [_P, C.c_uint32]),
+    "vsim_splat_launches": (C.c_uint32, [_P]),
     "vsim_stable_step_duration": (C.c_int, [C.c_double, _D]),
     "vsim_clock_create": (C.c_int, [C.c_double, C.c_uint32, C.POINTER(_P)]),
     "vsim_clock_destroy": (C.c_int, [_P]),

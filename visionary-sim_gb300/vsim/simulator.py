@@ -291,6 +291,26 @@ class Simulator:
         check(lib().vsim_contact_surface(self._h, uptr(nodes), uptr(bodies), n, C.byref(count)))
         return nodes, bodies
 
+    # -- profiling --------------------------------------------------------------
+    def profile_frame(self, steps: int, splats: bool = False, view_dir=(0.0, 0.0, -1.0)) -> dict:
+        """One frame with every kernel group timed by CUDA events:
+        {group: (milliseconds, launches)}."""
+        prof = _ffi.Profile()
+        v = np.asarray(view_dir, np.float32)
+        check(lib().vsim_profile_frame(self._h, int(steps), int(bool(splats)), fptr(v), C.byref(prof)))
+        return {k: (prof.ms[i], prof.launches[i]) for i, k in enumerate(_ffi.KINDS) if prof.launches[i]}
+
+    def color_counts(self) -> np.ndarray:
+        out = np.zeros(8, np.uint32)
+        check(lib().vsim_color_counts(self._h, uptr(out)))
+        return out
+
+    def frame_launches(self, steps: int) -> int:
+        return int(lib().vsim_frame_launches(self._h, int(steps)))
+
+    def splat_launches(self) -> int:
+        return int(lib().vsim_splat_launches(self._h))
+
     # -- splats ----------------------------------------------------------------
     def bind_splats(self, body, means, quats, scales):
         means = np.ascontiguousarray(means, np.float32)

@@ -330,6 +330,21 @@ int vsim_splats_read(vsim_sim* sim, float* means, float* cov6, uint32_t* order, 
 int vsim_radix_sort_u32(const uint32_t* d_keys, uint32_t* d_order, uint32_t n, uint32_t key_bits,
                         void* d_temp, size_t* temp_bytes, void* stream);
 
+/*
+ * The same sort for callers that cannot allocate device memory -- an engine
+ * that owns the whole GPU through its own pool, a frame loop that may not
+ * stall on cudaMalloc, a binding holding only raw device pointers. No
+ * counterpart in the reference. It allocates and frees nothing: its scratch
+ * is a fixed array of about 16 MiB inside this library, held on every GPU
+ * that loads the library until the process exits, and it sorts at most
+ * 1048576 keys (more fails with VSIM_ERR_CAPACITY). The first call on each
+ * device looks up the array's device address; make that first call before
+ * any stream capture. All calls share the array: calls that overlap on the
+ * GPU race, so serialise them. Same results as vsim_radix_sort_u32.
+ */
+int vsim_radix_sort_u32_noalloc(const uint32_t* d_keys, uint32_t* d_order, uint32_t n,
+                                uint32_t key_bits, void* stream);
+
 /* ---- fixed timestep clock (timestep.js:17-180), host only ------------- */
 
 typedef struct vsim_clock vsim_clock;

@@ -1,5 +1,8 @@
 // Gaussian-splat deformation (sample.wgsl:40-80 with covariance.wgsl:18-42)
 // and the stable LSD radix sort behind the depth order.
+#include <mutex>
+#include <string>
+
 #include "kernels.cuh"
 
 namespace vsim {
@@ -100,14 +103,14 @@ constexpr uint32_t kScanChunk = 4096;  // elements per block of the scan
 constexpr uint32_t kScanMaxChunks = 4096;
 
 namespace {
-inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
-inline uint32_t tilesOf(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
+constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr uint32_t tilesOf(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
+constexpr size_t sortTempBytes(uint32_t n) {
+    return 4 * align256(size_t(n) * 4) + align256(256 * size_t(tilesOf(n)) * 4) + align256(kScanMaxChunks * 4);
+}
 }  // namespace
 
-size_t radixSortTempBytes(uint32_t n) {
-    const size_t tiles = tilesOf(n);
-    return 4 * align256(size_t(n) * 4) + align256(256 * tiles * 4) + align256(kScanMaxChunks * 4);
-}
+size_t radixSortTempBytes(uint32_t n) { return sortTempBytes(n); }
 
 __global__ void __launch_bounds__(kSortThreads) sortHistKernel(const uint32_t* __restrict__ keys, uint32_t n,
                                                                uint32_t shift, uint32_t mask, uint32_t tiles,
@@ -323,3 +326,74 @@ cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint
 }
 
 }  // namespace vsim
+
+// ------------------------------------------------- sort without allocating --
+//
+// Some callers cannot allocate device memory: a host engine that owns every
+// byte of the GPU through its own pool and forbids libraries to allocate
+// behind its back, a real-time frame loop that may not risk cudaMalloc's
+// implicit device synchronisation or an allocation stall mid-frame, or a thin
+// binding handed nothing but raw device pointers. For them the sort below
+// takes its scratch from a fixed array compiled into this library instead of
+// from the caller: it allocates nothing and frees nothing.
+//
+// The array holds the scratch of kNoAllocMaxKeys keys (about 16 MiB) and lives
+// on every GPU that loads the library until the process exits. Every call
+// shares it, so calls whose work overlaps on the GPU -- on two streams, or from
+// two threads -- race and corrupt each other's results; serialise them. Each
+// call writes every scratch word it reads before reading it, so nothing has
+// to be cleared between calls.
+
+namespace vsim {
+namespace {
+
+constexpr uint32_t kNoAllocMaxKeys = 1u << 20;
+constexpr size_t kNoAllocScratchBytes = sortTempBytes(kNoAllocMaxKeys);
+
+__device__ __align__(256) static unsigned char g_sortScratch[kNoAllocScratchBytes];
+
+// In host code `g_sortScratch` names a host-side stand-in, not device memory:
+// the device address comes from cudaGetSymbolAddress, looked up once per
+// device with that device current and cached here.
+constexpr int kMaxDevices = 64;
+std::mutex g_scratchLock;
+void* g_scratchAddress[kMaxDevices] = {};
+
+cudaError_t scratchAddress(void** out) {
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return e;
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> hold(g_scratchLock);
+    if (!g_scratchAddress[device]) {
+        void* ptr = nullptr;
+        e = cudaGetSymbolAddress(&ptr, g_sortScratch);
+        if (e != cudaSuccess) return e;
+        g_scratchAddress[device] = ptr;
+    }
+    *out = g_scratchAddress[device];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+}  // namespace vsim
+
+extern "C" int vsim_radix_sort_u32_noalloc(const uint32_t* d_keys, uint32_t* d_order, uint32_t n, uint32_t key_bits,
+                                           void* stream) {
+    using namespace vsim;
+    clearError();
+    if (key_bits < 1 || key_bits > 32) return fail(VSIM_ERR_RANGE, "key_bits must be in [1, 32]");
+    if (n > kNoAllocMaxKeys)
+        return fail(VSIM_ERR_CAPACITY, "vsim_radix_sort_u32_noalloc sorts at most 1048576 keys; use "
+                                       "vsim_radix_sort_u32 with caller-provided scratch for more");
+    if (n == 0) return VSIM_OK;
+    if (!d_keys || !d_order) return fail(VSIM_ERR_INVALID, "keys or order is NULL");
+    void* scratch = nullptr;
+    cudaError_t e = scratchAddress(&scratch);
+    if (e != cudaSuccess) return fail(VSIM_ERR_CUDA, std::string("scratch address: ") + cudaGetErrorString(e));
+    e = radixSortU32(d_keys, d_order, n, key_bits, scratch, kNoAllocScratchBytes, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(VSIM_ERR_CUDA, std::string("radix sort: ") + cudaGetErrorString(e));
+    return VSIM_OK;
+}
+

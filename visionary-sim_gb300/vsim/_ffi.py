@@ -159,6 +159,7 @@ SIGNATURES = {
     "vsim_splats_sort": (C.c_int, [_P]),
     "vsim_splats_read": (C.c_int, [_P, _F, _F, _U, _SZ]),
     "vsim_radix_sort_u32": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P, C.POINTER(_SZ), _P]),
+    "vsim_radix_sort_u32_noalloc": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P]),
     "vsim_profile_frame": (C.c_int, [_P, C.c_uint32, C.c_int, _F, C.POINTER(Profile)]),
     "vsim_color_counts": (C.c_int, [_P, _U]),
     "vsim_frame_launches": (C.c_uint32, [_P, C.c_uint32]),

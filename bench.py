@@ -296,6 +296,107 @@ def batched_vs_plain(frames: int, quick: bool):
     return out
 
 
+def serving_sweep(quick: bool, seconds_per_point: float = 3.0):
+    """Continuous batching under load: a pool of sessions resident on the
+    GPU; requests advance a session k ~ U{1..4} frames, half of them dragging
+    a random surface node along a seeded Bezier curve at 0.5 m/s. Saturation
+    is measured closed-loop (every session always has a request), then
+    Poisson arrivals at fractions of it. Frame latency of a request =
+    (completion - arrival) / k."""
+    import vsim.scenes as sc
+    from vsim.server import Server
+
+    count = 64 if quick else 1000
+    t0 = time.perf_counter()
+    bodies, tank = sc.session_pool(count, seed=3)
+    gen_s = time.perf_counter() - t0
+    server = Server(bodies, tank, budget_bytes=150e9)
+    admitted = server.admitted
+    rng = np.random.default_rng(7)
+    drags = {}
+
+    def request(session):
+        frames = int(rng.integers(1, 5))
+        drag = None
+        if rng.random() < 0.5:
+            if session not in drags:
+                drags[session] = sc.drag_request(bodies[session], rng)
+            node, control, speed = drags[session]
+            drag = (node, control, speed)
+        return frames, drag
+
+    # Saturation: keep every session busy.
+    arrival = {}
+    for s in range(admitted):
+        f, d = request(s)
+        arrival[server.submit(s, f, d)] = server.clock()
+    start = server.clock()
+    frames_done, requests_done, ticks = 0, 0, 0
+    while server.clock() - start < seconds_per_point:
+        server.tick()
+        ticks += 1
+        for c in server.poll():
+            requests_done += 1
+            frames_done += c["frames"]
+            f, d = request(c["session"])
+            arrival[server.submit(c["session"], f, d)] = server.clock()
+    sat_elapsed = server.clock() - start
+    sat_rate = requests_done / sat_elapsed
+    stats0 = server.stats()
+    while server.stats()["pending"]:
+        server.tick()
+        server.poll()
+    cells0 = server.stats()["cell_updates"]
+
+    points = []
+    for frac in (0.25, 0.5, 0.7, 0.9):
+        lam = frac * sat_rate
+        arrival = {}
+        lat, req_lat = [], []
+        t = server.clock()
+        next_arrival = t + rng.exponential(1 / lam)
+        end = t + seconds_per_point
+        stepped = []
+        c_before = server.stats()["cell_updates"]
+        t_begin = t
+        while True:
+            now = server.clock()
+            while next_arrival <= now and next_arrival < end:
+                s = int(rng.integers(0, admitted))
+                f, d = request(s)
+                arrival[server.submit(s, f, d)] = next_arrival
+                next_arrival += rng.exponential(1 / lam)
+            if server.stats()["pending"]:
+                stepped.append(server.tick())
+            elif next_arrival >= end:
+                break
+            else:
+                time.sleep(max(0.0, min(next_arrival - server.clock(), 0.001)))
+            for c in server.poll():
+                total = c["completed"] - arrival.pop(c["request"])
+                req_lat.append(total)
+                lat.append(total / c["frames"])
+        elapsed = server.clock() - t_begin
+        points.append({"load": frac, "offered_req_per_s": round(lam, 1),
+                       "frame_latency_ms": {"p50": round(1e3 * float(np.percentile(lat, 50)), 3),
+                                            "p99": round(1e3 * float(np.percentile(lat, 99)), 3)},
+                       "request_latency_ms": {"p50": round(1e3 * float(np.percentile(req_lat, 50)), 3),
+                                              "p99": round(1e3 * float(np.percentile(req_lat, 99)), 3)},
+                       "requests": len(lat),
+                       "sessions_per_tick": round(float(np.mean(stepped)), 1) if stepped else 0,
+                       "cell_updates_per_s": round((server.stats()["cell_updates"] - c_before) / elapsed)})
+    st = server.stats()
+    server.destroy()
+    return {"workload": f"{admitted} sessions ({count} offered), noise blobs on 8^3-64^3 grids, "
+                        f"{sum(b.cell_count for b in bodies[:admitted])} cells resident, "
+                        f"{st['resident_bytes'] / 1e9:.2f} GB of the 150 GB budget; k ~ U{{1..4}} frames, "
+                        f"50% with a Bezier drag at 0.5 m/s",
+            "saturation": {"requests_per_s": round(sat_rate, 1),
+                           "session_frames_per_s": round(frames_done / sat_elapsed, 1),
+                           "ticks": ticks, "cell_updates_per_s": round(stats0["cell_updates"] / sat_elapsed)},
+            "sweep": points, "pool_generation_s": round(gen_s, 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -305,6 +406,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="small workload, for checking the harness")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -377,6 +479,8 @@ def main():
               "frame_ms": {"min": round(min(times) * 1e3, 4), "median": round(statistics.median(times) * 1e3, 4)}}
     if rank == 0 and not args.no_batch:
         detail["batching"] = batched_vs_plain(3, args.quick)
+    if rank == 0 and not args.no_serve:
+        detail["serving"] = serving_sweep(args.quick)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(scene)

@@ -137,8 +137,23 @@ int vsim_abi_version(void);
  */
 int vsim_create(const vsim_body_desc* bodies, uint32_t body_count,
                 const vsim_tank* tank, void* stream, vsim_sim** out);
+/* Flags of vsim_create_ex. */
+#define VSIM_CREATE_ISOLATED 1u  /* bodies never touch each other: each bins its
+                                    surface into its own contact grid around it,
+                                    and only same-body (self) contact exists */
+
+/* vsim_create with options. With VSIM_CREATE_ISOLATED every body is an
+   independent world (no counterpart in the reference, whose bodies all share
+   one grid, bodyContact.js:343): what a batch of unrelated bodies or a pool
+   of serving sessions needs. */
+int vsim_create_ex(const vsim_body_desc* bodies, uint32_t body_count,
+                   const vsim_tank* tank, void* stream, uint32_t flags, vsim_sim** out);
 /* `destroy()`; idempotent on a NULL handle. */
 int vsim_destroy(vsim_sim* sim);
+/* Which bodies take part in subsequent frames (`active[b]` nonzero), NULL for
+   all. A body that sits out is left exactly as it is. No counterpart in the
+   reference. */
+int vsim_set_bodies_active(vsim_sim* sim, const uint8_t* active, uint32_t count);
 
 /* ---- stepping (simulator.js:239-318, :495-500) ----------------------- */
 
@@ -344,6 +359,73 @@ int vsim_radix_sort_u32(const uint32_t* d_keys, uint32_t* d_order, uint32_t n, u
  */
 int vsim_radix_sort_u32_noalloc(const uint32_t* d_keys, uint32_t* d_order, uint32_t n,
                                 uint32_t key_bits, void* stream);
+
+/* ---- serving: many sessions stepped in shared frames ------------------ */
+/*
+ * No counterpart in the reference (one simulator per page). A server holds a
+ * pool of sessions -- one body each, isolated from one another -- resident on
+ * the device, admitted in order while their state fits an HBM budget.
+ * Requests ask a session to advance some frames, optionally dragging one of
+ * its nodes (hard law) toward a target moving along a cubic Bezier curve.
+ * Every tick runs one frame for every session with a pending request, in one
+ * batched launch sequence: a request submitted while others are running
+ * joins at the next frame boundary (continuous batching). A session's
+ * result does not depend on which other sessions share its frames.
+ */
+typedef struct vsim_server vsim_server;
+
+typedef struct vsim_server_config {
+    double hbm_budget_bytes;  /* admit sessions while their device state fits; 0 = no limit */
+    double step_duration;     /* seconds per substep */
+    uint32_t substeps;        /* substeps per frame */
+    int32_t self_contact;     /* same-body contact inside each session */
+} vsim_server_config;
+
+typedef struct vsim_drag {
+    uint32_t node;            /* session-local node to hold */
+    float control[4][3];      /* cubic Bezier control points of the target's path */
+    double speed;             /* metres per second along the path */
+} vsim_drag;
+
+typedef struct vsim_completion {
+    uint64_t request;
+    uint32_t session;
+    uint32_t frames;
+    double submitted;         /* server clock, seconds */
+    double completed;
+    uint64_t first_tick;      /* tick that ran the request's first frame */
+    uint64_t last_tick;
+} vsim_completion;
+
+typedef struct vsim_server_stats {
+    uint32_t sessions;        /* admitted */
+    uint32_t rejected;        /* not admitted: over the budget */
+    double resident_bytes;    /* device bytes the admitted sessions hold */
+    uint64_t ticks;
+    uint64_t session_frames;  /* frames run, summed over sessions */
+    uint64_t cell_updates;    /* occupied cells x substeps, summed over frames run */
+    uint32_t pending;         /* requests queued or running */
+} vsim_server_stats;
+
+int vsim_server_create(const vsim_body_desc* sessions, uint32_t count, const vsim_tank* tank,
+                       const vsim_server_config* config, void* stream, vsim_server** out);
+int vsim_server_destroy(vsim_server* server);
+/* Sessions 0 .. admitted-1 are resident; the rest did not fit the budget. */
+uint32_t vsim_server_admitted(const vsim_server* server);
+/* Seconds on the server's monotonic clock. */
+double vsim_server_clock(const vsim_server* server);
+/* Queue `frames` frames for `session` (FIFO per session); drag may be NULL. */
+int vsim_server_submit(vsim_server* server, uint32_t session, uint32_t frames, const vsim_drag* drag,
+                       uint64_t* request);
+/* Run one frame for every session with a pending request and wait for it;
+   *stepped receives how many sessions it advanced (0: nothing to do). */
+int vsim_server_tick(vsim_server* server, uint32_t* stepped);
+/* Requests completed since the last poll (at most `capacity`). */
+int vsim_server_poll(vsim_server* server, vsim_completion* out, uint32_t capacity, uint32_t* count);
+int vsim_server_get_stats(const vsim_server* server, vsim_server_stats* out);
+uint32_t vsim_server_node_count(const vsim_server* server, uint32_t session);
+/* The session's node positions, xyzw, w = 0. */
+int vsim_server_read_positions(vsim_server* server, uint32_t session, float* xyzw, size_t node_count);
 
 /* ---- fixed timestep clock (timestep.js:17-180), host only ------------- */
 

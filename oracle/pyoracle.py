@@ -37,6 +37,7 @@ def lib():
         L = C.CDLL(str(LIB_PATH))
         sig = {
             "vo_create": (C.c_int, [_P, C.c_uint32, _P, C.c_int, C.POINTER(_P)]),
+            "vo_create_ex": (C.c_int, [_P, C.c_uint32, _P, C.c_int, C.c_uint32, C.POINTER(_P)]),
             "vo_destroy": (None, [_P]),
             "vo_set_threads": (None, [C.c_int]),
             "vo_max_threads": (C.c_int, []),
@@ -115,8 +116,9 @@ class Oracle:
 
         self._descs = scenes.Descs(scene)
         h = C.c_void_p()
-        rc = lib().vo_create(C.cast(self._descs.bodies, _P), self._descs.count, C.cast(C.byref(self._descs.tank), _P),
-                             precision, C.byref(h))
+        flags = 1 if getattr(scene, "isolated", False) else 0
+        rc = lib().vo_create_ex(C.cast(self._descs.bodies, _P), self._descs.count,
+                                C.cast(C.byref(self._descs.tank), _P), precision, flags, C.byref(h))
         if rc != 0:
             raise RuntimeError(f"vo_create failed with {rc}")
         self._h = h

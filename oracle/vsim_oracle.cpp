@@ -174,9 +174,17 @@ struct Sim {
     // contact
     std::vector<uint32_t> sNode, sBody, sCoord;
     std::vector<T> sRadius;
-    double gridOrigin[3] = {0, 0, 0};
-    double bucketSize = 0;
-    uint32_t gridDims[3] = {1, 1, 1};
+    // Contact grids: one shared by every body, or one per body when the
+    // bodies are isolated (never touch each other).
+    struct OGrid {
+        double origin[3];
+        double bucket;
+        uint32_t dims[3];
+        size_t base;
+    };
+    std::vector<OGrid> grids;
+    size_t bucketTotal = 0;
+    bool isolated = false;
     bool contact = true, selfContact = false;
     // drive
     std::vector<uint32_t> driven;
@@ -252,7 +260,8 @@ void gridLayout(const double mn[3], const double mx[3], double bucket, double or
 }
 
 template <class T>
-int build(Sim<T>& s, const vsim_body_desc* descs, uint32_t n, const vsim_tank* tank) {
+int build(Sim<T>& s, const vsim_body_desc* descs, uint32_t n, const vsim_tank* tank, bool isolated) {
+    s.isolated = isolated;
     s.bodies.resize(n);
     s.params.resize(n);
     for (int a = 0; a < 3; a++) {
@@ -351,9 +360,29 @@ int build(Sim<T>& s, const vsim_body_desc* descs, uint32_t n, const vsim_tank* t
             hi[a] = std::max(hi[a], body.origin[a] + body.cellDims[a] * body.h);
         }
     }
+    typename Sim<T>::OGrid g{};
     double edge;
-    gridLayout(s.tankMin, s.tankMax, widest * 2, s.gridOrigin, edge, s.gridDims);
-    const double buckets = double(s.gridDims[0]) * s.gridDims[1] * s.gridDims[2];
+    if (s.isolated) {
+        // Each body's own grid: its rest box padded by a quarter of its
+        // extent (at least four cells) per side, clipped to the tank, buckets
+        // one cell.
+        for (uint32_t b = 0; b < n; b++) {
+            const Body& body = s.bodies[b];
+            double mn[3], mx[3];
+            for (int a = 0; a < 3; a++) {
+                const double pad = std::max(0.25 * body.cellDims[a] * body.h, 8 * body.h * CONTACT_RADIUS_CELLS);
+                mn[a] = std::max(s.tankMin[a], body.origin[a] - pad);
+                mx[a] = std::min(s.tankMax[a], body.origin[a] + body.cellDims[a] * body.h + pad);
+            }
+            gridLayout(mn, mx, body.h * CONTACT_RADIUS_CELLS * 2, g.origin, g.bucket, g.dims);
+            g.base = s.bucketTotal;
+            s.bucketTotal += size_t(g.dims[0]) * g.dims[1] * g.dims[2];
+            s.grids.push_back(g);
+        }
+        return VSIM_OK;
+    }
+    gridLayout(s.tankMin, s.tankMax, widest * 2, g.origin, edge, g.dims);
+    const double buckets = double(g.dims[0]) * g.dims[1] * g.dims[2];
     bool finite = true;
     for (int a = 0; a < 3; a++) finite = finite && std::isfinite(s.tankMin[a]) && std::isfinite(s.tankMax[a]);
     if (!finite || !(buckets <= GRID_LIMIT)) {
@@ -366,9 +395,12 @@ int build(Sim<T>& s, const vsim_body_desc* descs, uint32_t n, const vsim_tank* t
             mn[a] = std::max(s.tankMin[a], lo[a] - pad);
             mx[a] = std::min(s.tankMax[a], hi[a] + pad);
         }
-        gridLayout(mn, mx, widest * 2, s.gridOrigin, edge, s.gridDims);
+        gridLayout(mn, mx, widest * 2, g.origin, edge, g.dims);
     }
-    s.bucketSize = edge;
+    g.bucket = edge;
+    g.base = 0;
+    s.bucketTotal = size_t(g.dims[0]) * g.dims[1] * g.dims[2];
+    s.grids.push_back(g);
     return VSIM_OK;
 }
 
@@ -543,16 +575,23 @@ void colorPass(Sim<T>& s, int color, bool limitOnly, T dt, const FrameConsts<T>&
 
 // contacts.wgsl:84-91 (gridCoord, bucketAt), evaluated in T.
 template <class T>
-inline uint32_t bucketOf(const Sim<T>& s, V3<T> p, uint32_t coord[3]) {
-    const T o[3] = {asT<T>(s.gridOrigin[0]), asT<T>(s.gridOrigin[1]), asT<T>(s.gridOrigin[2])};
-    const T size = asT<T>(s.bucketSize);
+inline const typename Sim<T>::OGrid& gridOf(const Sim<T>& s, uint32_t body) {
+    return s.grids[s.isolated ? body : 0];
+}
+
+// Index into the bucket arrays: the grid's base plus its linear index.
+template <class T>
+inline size_t bucketOf(const Sim<T>& s, uint32_t body, V3<T> p, uint32_t coord[3]) {
+    const typename Sim<T>::OGrid& g = gridOf(s, body);
+    const T o[3] = {asT<T>(g.origin[0]), asT<T>(g.origin[1]), asT<T>(g.origin[2])};
+    const T size = asT<T>(g.bucket);
     const T q[3] = {p.x, p.y, p.z};
     for (int a = 0; a < 3; a++) {
-        const T last = T(s.gridDims[a]) - T(1);
+        const T last = T(g.dims[a]) - T(1);
         const T f = std::floor((q[a] - o[a]) / size);
         coord[a] = uint32_t(std::min(std::max(f, T(0)), last));
     }
-    return coord[0] + s.gridDims[0] * (coord[1] + s.gridDims[1] * coord[2]);
+    return g.base + coord[0] + size_t(g.dims[0]) * (coord[1] + size_t(g.dims[1]) * coord[2]);
 }
 
 // Whether records a and b may touch. The reference drops every same-body
@@ -560,7 +599,7 @@ inline uint32_t bucketOf(const Sim<T>& s, V3<T> p, uint32_t coord[3]) {
 // when its nodes share no cell (rest grid distance above one on some axis).
 template <class T>
 inline bool admitted(const Sim<T>& s, uint32_t a, uint32_t b) {
-    if (s.sBody[a] != s.sBody[b]) return true;
+    if (s.sBody[a] != s.sBody[b]) return !s.isolated;
     if (!s.selfContact) return false;
     const uint32_t ca = s.sCoord[a], cb = s.sCoord[b];
     for (int axis = 0; axis < 3; axis++) {
@@ -580,14 +619,14 @@ struct Binned {
 template <class T>
 Binned<T> binAll(const Sim<T>& s) {
     Binned<T> g;
-    const size_t buckets = size_t(s.gridDims[0]) * s.gridDims[1] * s.gridDims[2];
+    const size_t buckets = s.bucketTotal;
     const size_t S = s.sNode.size();
-    std::vector<uint32_t> key(S);
+    std::vector<size_t> key(S);
     g.count.assign(buckets, 0);
     g.start.assign(buckets, 0);
     for (size_t r = 0; r < S; r++) {
         uint32_t coord[3];
-        key[r] = bucketOf(s, s.pos[s.sNode[r]], coord);
+        key[r] = bucketOf(s, s.sBody[r], s.pos[s.sNode[r]], coord);
         g.count[key[r]]++;
     }
     uint32_t run = 0;
@@ -614,8 +653,9 @@ inline void gather(const Sim<T>& s, const Binned<T>& g, uint32_t r, V3<T>& sum, 
     sum = V3<T>{0, 0, 0};
     hits = T(0);
     uint32_t centre[3];
-    bucketOf(s, pi, centre);
-    const int dims[3] = {int(s.gridDims[0]), int(s.gridDims[1]), int(s.gridDims[2])};
+    bucketOf(s, body, pi, centre);
+    const typename Sim<T>::OGrid& grid = gridOf(s, body);
+    const int dims[3] = {int(grid.dims[0]), int(grid.dims[1]), int(grid.dims[2])};
     for (int dz = -1; dz <= 1; dz++) {
         const int z = int(centre[2]) + dz;
         if (z < 0 || z >= dims[2]) continue;
@@ -625,7 +665,7 @@ inline void gather(const Sim<T>& s, const Binned<T>& g, uint32_t r, V3<T>& sum, 
             for (int dx = -1; dx <= 1; dx++) {
                 const int x = int(centre[0]) + dx;
                 if (x < 0 || x >= dims[0]) continue;
-                const uint32_t bucket = uint32_t(x) + s.gridDims[0] * (uint32_t(y) + s.gridDims[1] * uint32_t(z));
+                const size_t bucket = grid.base + uint32_t(x) + size_t(grid.dims[0]) * (uint32_t(y) + size_t(grid.dims[1]) * uint32_t(z));
                 const uint32_t held = std::min(g.count[bucket], BUCKET_SLOTS);
                 for (uint32_t k = 0; k < held; k++) {
                     const uint32_t other = g.entries[g.start[bucket] + k];
@@ -858,17 +898,23 @@ void copyIn(const float* from, std::vector<V3<T>>& to) {
 extern "C" {
 
 int vo_create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, int precision, vo_sim** out) {
+    return vo_create_ex(bodies, n, tank, precision, 0, out);
+}
+
+int vo_create_ex(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, int precision, uint32_t flags,
+                 vo_sim** out) {
     if (!out || (precision != 32 && precision != 64)) return VSIM_ERR_INVALID;
+    const bool isolated = (flags & VSIM_CREATE_ISOLATED) != 0;
     Handle* h = new (std::nothrow) Handle{precision, nullptr};
     if (!h) return VSIM_ERR_NOMEM;
     int rc;
     if (precision == 32) {
         auto* s = new Sim<float>();
-        rc = build(*s, bodies, n, tank);
+        rc = build(*s, bodies, n, tank, isolated);
         h->sim = s;
     } else {
         auto* s = new Sim<double>();
-        rc = build(*s, bodies, n, tank);
+        rc = build(*s, bodies, n, tank, isolated);
         h->sim = s;
     }
     *out = reinterpret_cast<vo_sim*>(h);
@@ -1132,10 +1178,10 @@ int vo_contact_grid(const vo_sim* s, double origin[3], double* bucket, uint32_t 
     DISPATCH_T(s, {
         const Sim<T>& sim = simOf<T>(s);
         for (int a = 0; a < 3; a++) {
-            origin[a] = sim.gridOrigin[a];
-            dims[a] = sim.gridDims[a];
+            origin[a] = sim.grids[0].origin[a];
+            dims[a] = sim.grids[0].dims[a];
         }
-        *bucket = sim.bucketSize;
+        *bucket = sim.grids[0].bucket;
     });
     return VSIM_OK;
 }

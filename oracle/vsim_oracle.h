@@ -35,6 +35,10 @@ typedef struct vo_sim vo_sim;
 /* precision: 32 or 64. */
 int vo_create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, int precision,
               vo_sim** out);
+/* With flags = VSIM_CREATE_ISOLATED each body has its own contact grid and
+   different bodies never touch (vsim_create_ex). */
+int vo_create_ex(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, int precision, uint32_t flags,
+                 vo_sim** out);
 void vo_destroy(vo_sim* s);
 void vo_set_threads(int threads);
 int vo_max_threads(void);

@@ -1,0 +1,153 @@
+"""Isolated bodies, partial frames and the session server, on the GPU.
+
+- Isolated scenes (every body its own contact grid) equal the oracle's
+  isolated mode frame by frame.
+- A body that sits a frame out is untouched; the bodies that ran equal the
+  oracle run of each alone.
+- Serving: a request's result is the same whether its session ran alone or
+  among others (continuous batching does not change arithmetic), and a
+  served session equals the oracle stepping that body alone.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lib(vsimlib, gpu):
+    return vsimlib
+
+
+def small_pool(count, seed=5):
+    import vsim.scenes as sc
+
+    return sc.session_pool(count, seed=seed, min_n=6, max_n=14)
+
+
+def test_isolated_batch_matches_oracle(lib):
+    import pyoracle
+    import vsim.scenes as sc
+    from vsim import Simulator
+
+    bodies, tank = small_pool(5)
+    scene = sc.Scene(bodies, tank, step_duration=1 / 600, substeps=10, contact=True, self_contact=True,
+                     isolated=True)
+    sim, orc = Simulator(scene), pyoracle.Oracle(scene, 32)
+    for frame in range(6):
+        sim.dispatch(10)
+        orc.dispatch(10)
+        g, o = sim.read_state(), orc.state()
+        for a, b in zip(g, o):
+            assert np.array_equal(a, b), f"frame {frame}"
+
+
+def test_inactive_bodies_are_untouched(lib):
+    import pyoracle
+    import vsim.scenes as sc
+    from vsim import Simulator
+
+    bodies, tank = small_pool(4, seed=9)
+    scene = sc.Scene(bodies, tank, step_duration=1 / 600, substeps=10, contact=True, self_contact=True,
+                     isolated=True)
+    sim = Simulator(scene)
+    before = sim.read_state()
+    active = [True, False, True, False]
+    sim.set_bodies_active(active)
+    for _ in range(3):
+        sim.dispatch(10)
+    after = sim.read_state()
+    for b, on in enumerate(active):
+        lo, hi = sim.offsets[b], sim.offsets[b] + bodies[b].node_count
+        if not on:
+            for x, y in zip(before, after):
+                assert np.array_equal(x[lo:hi], y[lo:hi])
+            continue
+        alone = sc.Scene([bodies[b]], tank, step_duration=1 / 600, substeps=10, contact=True, self_contact=True,
+                         isolated=True)
+        orc = pyoracle.Oracle(alone, 32)
+        for _ in range(3):
+            orc.dispatch(10)
+        for x, y in zip(after, orc.state()):
+            assert np.array_equal(x[lo:hi], y)
+
+
+def serve(bodies, tank, requests, budget=150e9):
+    """Submit all `requests` (session, frames, drag) then tick until done;
+    returns the server (for reads) and the completions."""
+    from vsim.server import Server
+
+    server = Server(bodies, tank, budget_bytes=budget)
+    for session, frames, drag in requests:
+        server.submit(session, frames, drag)
+    done = []
+    while server.stats()["pending"]:
+        server.tick()
+        done += server.poll()
+    return server, done
+
+
+def test_served_result_same_alone_and_in_the_mix(lib):
+    import vsim.scenes as sc
+
+    bodies, tank = small_pool(6, seed=11)
+    rng = np.random.default_rng(3)
+    drag0 = sc.drag_request(bodies[0], rng)
+    alone, _ = serve(bodies, tank, [(0, 4, drag0)])
+    mix_requests = [(0, 4, drag0)]
+    for s in range(1, 6):
+        mix_requests.append((s, int(rng.integers(1, 5)), sc.drag_request(bodies[s], rng) if s % 2 else None))
+    mixed, done = serve(bodies, tank, mix_requests)
+    assert len(done) == 6
+    assert np.array_equal(alone.read_positions(0), mixed.read_positions(0))
+    # Sessions without a request stayed at rest in the solo run.
+    for s in range(1, 6):
+        assert not np.array_equal(alone.read_positions(s), mixed.read_positions(s))
+
+
+def test_requests_join_at_frame_boundaries(lib):
+    """A request submitted while another runs starts at the next tick and
+    shares frames with it; both finish with the frames they asked for."""
+    bodies, tank = small_pool(3, seed=13)
+    from vsim.server import Server
+
+    server = Server(bodies, tank)
+    first = server.submit(0, 4)
+    server.tick()
+    second = server.submit(1, 2)
+    server.tick()
+    server.tick()
+    done = {c["request"]: c for c in server.poll()}
+    assert second in done and first not in done
+    assert done[second]["first_tick"] == 1 and done[second]["last_tick"] == 2
+    server.tick()
+    done = {c["request"]: c for c in server.poll()}
+    assert done[first]["first_tick"] == 0 and done[first]["last_tick"] == 3
+    assert server.stats()["session_frames"] == 6
+
+
+def test_served_session_matches_oracle(lib):
+    import pyoracle
+    import vsim.scenes as sc
+
+    bodies, tank = small_pool(3, seed=17)
+    server, _ = serve(bodies, tank, [(1, 5, None), (2, 2, None)])
+    alone = sc.Scene([bodies[1]], tank, step_duration=1 / 600, substeps=10, contact=True, self_contact=True,
+                     isolated=True)
+    orc = pyoracle.Oracle(alone, 32)
+    for _ in range(5):
+        orc.dispatch(10)
+    assert np.array_equal(server.read_positions(1), orc.state()[0])
+
+
+def test_budget_admission(lib):
+    from vsim.server import Server
+
+    bodies, tank = small_pool(8, seed=19)
+    everyone = Server(bodies, tank)
+    assert everyone.admitted == 8
+    per = everyone.stats()["resident_bytes"] / 8
+    tight = Server(bodies, tank, budget_bytes=per * 3)
+    st = tight.stats()
+    assert 1 <= tight.admitted < 8 and st["rejected"] == 8 - tight.admitted
+    assert st["resident_bytes"] <= per * 3

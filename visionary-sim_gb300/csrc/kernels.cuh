@@ -17,6 +17,8 @@ struct DeviceState {
     uint32_t* active = nullptr;   // nodes with material (predict and finalize visit these)
     uint32_t* activeBody = nullptr;
     int32_t* nodeRecord = nullptr;  // surface record of each node, -1 for none
+    uint32_t* bodyActive = nullptr;  // 1 where a body takes part in this frame
+    float4* grabs = nullptr;      // per body: drive target, drive target velocity
     uint4* cells = nullptr;       // colour-major (corner-0 node, body, y stride, z stride)
     DevBody* bodies = nullptr;
     FrameParams* fp = nullptr;
@@ -43,6 +45,35 @@ struct LaunchCtx {
     uint32_t sms;  // multiprocessors of the device
 };
 
+// The items one launch covers: all of [0, count) (one thread each), or, with
+// `chunks`, one block per (first item, item count) entry -- the ranges of
+// the bodies a frame steps, so idle bodies cost no threads at all.
+struct Work {
+    const uint2* chunks;
+    uint32_t count;
+};
+
+__device__ __forceinline__ bool workItem(const Work& w, uint32_t& item) {
+    if (w.chunks) {
+        const uint2 c = w.chunks[blockIdx.x];
+        if (threadIdx.x >= c.y) return false;
+        item = c.x + threadIdx.x;
+        return true;
+    }
+    item = blockIdx.x * blockDim.x + threadIdx.x;
+    return item < w.count;
+}
+
+// One launch: its work, grid and block.
+struct Span {
+    Work work;
+    uint32_t grid;
+    uint32_t block;
+};
+
+// Chunks of at most kChunk items per block.
+constexpr uint32_t kChunk = 128;
+
 // Rest lengths of the cube's edges, face and body diagonals (stretch.js:5-7),
 // as f32; indexed by the number of axes the two corners differ in, minus one.
 struct StretchLengths {
@@ -53,16 +84,22 @@ enum class ContactMode { Solve, Pairs };
 
 void kuhnTable(float out[54]);
 
-cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount);
+// Dense spans: `count` items, blocks of `block` threads.
+Span denseSpan(uint32_t count, uint32_t block);
+// A colour pass's span over `count` cells: blocks shrink for small passes
+// so that every SM gets a share.
+Span elasticSpan(uint32_t count, uint32_t block, uint32_t sms);
+
+cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, const Span& nodes);
 cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drivenCount);
-cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, uint32_t count,
-                          bool limitOnly, uint32_t block, const StretchLengths& lens);
+cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, const Span& span,
+                          bool limitOnly, const StretchLengths& lens);
 // The substep's closing pass; with `contact` it first applies the contact
 // corrections and empties the grid, with `predictNext` it goes on into the
 // next substep's prediction.
-cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount, bool contact,
+cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span& nodes, bool contact,
                            bool predictNext);
-cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, uint32_t surfaceCount, ContactMode mode,
+cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& records, ContactMode mode,
                           uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount);
 cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos);
 cudaError_t launchZeroW(cudaStream_t st, const uint32_t* nodes, uint32_t n, float4* pos);

@@ -1,0 +1,338 @@
+// Serving: a pool of sessions resident on the device, stepped in shared
+// frames. No counterpart in the reference (its Simulator serves one page).
+//
+// All admitted sessions live in one simulator created with isolated bodies
+// (each session is a body with its own contact grid), so a frame's kernels
+// run over every session at once. A tick picks the sessions with a pending
+// request, marks them active (the rest sit the frame out untouched), sets
+// their drag targets, runs one frame and retires the requests it finished.
+// Requests that arrive while a frame runs are queued and join at the next
+// tick: batching is per frame, continuously, not per request.
+//
+// A session's arithmetic never reads another session's data: bodies own
+// disjoint node ranges, their contact grids are disjoint, and inactive bodies
+// are skipped by every kernel. So a request's result is the same whether it
+// ran alone or among others.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <new>
+
+#include "sim_internal.cuh"
+
+using namespace vsim;
+
+namespace {
+
+struct Request {
+    uint64_t id = 0;
+    uint32_t session = 0;
+    uint32_t frames = 0;
+    uint32_t done = 0;
+    bool drag = false;
+    vsim_drag path{};
+    double t = 0;  // curve parameter of the drag target
+    double submitted = 0;
+    uint64_t firstTick = 0;
+};
+
+// Cubic Bezier position and derivative.
+void bezier(const float c[4][3], double t, double p[3], double dp[3]) {
+    const double u = 1 - t;
+    for (int a = 0; a < 3; a++) {
+        p[a] = u * u * u * c[0][a] + 3 * u * u * t * c[1][a] + 3 * u * t * t * c[2][a] + t * t * t * c[3][a];
+        dp[a] = 3 * u * u * (c[1][a] - c[0][a]) + 6 * u * t * (c[2][a] - c[1][a]) + 3 * t * t * (c[3][a] - c[2][a]);
+    }
+}
+
+}  // namespace
+
+struct vsim_server {
+    vsim_sim* sim = nullptr;
+    uint32_t admitted = 0, rejected = 0;
+    double residentBytes = 0;
+    uint32_t substeps = 10;
+    double stepDuration = 1.0 / 600;
+    std::vector<std::deque<Request>> queue;
+    std::vector<uint32_t> cells;       // occupied cells per session
+    std::vector<int64_t> held;         // global node each session holds, -1 for none
+    std::vector<double> prevTarget;    // 3 per session
+    std::vector<vsim_completion> completed;
+    uint64_t ticks = 0, nextId = 1, sessionFrames = 0, cellUpdates = 0;
+    uint32_t pending = 0;
+    std::chrono::steady_clock::time_point origin = std::chrono::steady_clock::now();
+    cudaEvent_t frameDone = nullptr;
+};
+
+namespace {
+
+double seconds(const vsim_server* s) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - s->origin).count();
+}
+
+// Device bytes one isolated session holds (what admission charges).
+double sessionBytes(const Lattice& L, const Grid& g) {
+    const double nodes = L.nodeCount, surface = double(L.surface.size());
+    return nodes * (3 * 16 + 4 * 4)            // pos, prev, vel; mass, active list, body, record
+           + double(L.cellCount) * 16          // cell records
+           + surface * (16 + 4 + 4 + 4 + 16 + 16 + 16 + 4)  // record, key, rank, entry, correction, runs
+           + double(g.count()) * 8             // bucket counts and starts
+           + sizeof(DevBody) + 2 * 16 + 4;     // constants, drag target, activity
+}
+
+int destroyServer(vsim_server* s) {
+    if (s->sim) {
+        DeviceGuard guard(s->sim->device);
+        cudaStreamSynchronize(s->sim->stream);
+        if (s->frameDone) cudaEventDestroy(s->frameDone);
+        freeSim(s->sim);
+        delete s->sim;
+    }
+    delete s;
+    return VSIM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vsim_server_create(const vsim_body_desc* sessions, uint32_t count, const vsim_tank* tank,
+                       const vsim_server_config* config, void* stream, vsim_server** out) {
+    clearError();
+    if (!out || !config) return fail(VSIM_ERR_INVALID, "out or config is NULL");
+    *out = nullptr;
+    if (count > 0 && !sessions) return fail(VSIM_ERR_INVALID, "sessions is NULL");
+    if (!std::isfinite(config->step_duration) || config->step_duration <= 0)
+        return fail(VSIM_ERR_RANGE, "step_duration must be a finite positive number");
+    if (config->substeps < 1) return fail(VSIM_ERR_RANGE, "substeps must be at least 1");
+    vsim_server* s = new (std::nothrow) vsim_server();
+    if (!s) return fail(VSIM_ERR_NOMEM, "out of host memory");
+    s->substeps = config->substeps;
+    s->stepDuration = config->step_duration;
+    vsim_tank world;
+    for (int a = 0; a < 3; a++) {
+        world.min[a] = tank ? tank->min[a] : -INFINITY;
+        world.max[a] = tank ? tank->max[a] : INFINITY;
+    }
+    // Admission: sessions in order while their device state fits the budget.
+    try {
+        for (uint32_t i = 0; i < count; i++) {
+            Lattice L;
+            int rc = buildLattice(sessions[i], L);
+            if (rc) {
+                destroyServer(s);
+                return rc;
+            }
+            const double bytes = sessionBytes(L, bodyGrid(L, world));
+            if (config->hbm_budget_bytes > 0 && s->residentBytes + bytes > config->hbm_budget_bytes) break;
+            s->residentBytes += bytes;
+            s->cells.push_back(L.cellCount);
+            s->admitted++;
+        }
+    } catch (const std::bad_alloc&) {
+        destroyServer(s);
+        return fail(VSIM_ERR_NOMEM, "out of host memory");
+    }
+    s->rejected = count - s->admitted;
+    s->sim = new (std::nothrow) vsim_sim();
+    if (!s->sim) {
+        destroyServer(s);
+        return fail(VSIM_ERR_NOMEM, "out of host memory");
+    }
+    int rc;
+    try {
+        rc = createSim(sessions, s->admitted, &world, stream, true, s->sim);
+    } catch (const std::bad_alloc&) {
+        rc = fail(VSIM_ERR_NOMEM, "out of host memory");
+    }
+    if (rc) {
+        destroyServer(s);
+        return rc;
+    }
+    vsim_sim* sim = s->sim;
+    DeviceGuard guard(sim->device);
+    sim->clock.stepDuration = s->stepDuration;
+    sim->stepOverridden = true;
+    sim->selfContact = config->self_contact != 0;
+    sim->perBodyGrab = true;
+    std::fill(sim->activeHost.begin(), sim->activeHost.end(), 0u);
+    sim->tablesDirty = sim->paramsDirty = sim->frameDirty = true;
+    s->queue.resize(s->admitted);
+    s->held.assign(s->admitted, -1);
+    s->prevTarget.assign(3 * size_t(s->admitted), 0.0);
+    if (cudaEventCreateWithFlags(&s->frameDone, cudaEventDisableTiming) != cudaSuccess) {
+        destroyServer(s);
+        return fail(VSIM_ERR_CUDA, "create event");
+    }
+    *out = s;
+    return VSIM_OK;
+}
+
+int vsim_server_destroy(vsim_server* server) {
+    if (!server) return VSIM_OK;
+    return destroyServer(server);
+}
+
+uint32_t vsim_server_admitted(const vsim_server* s) { return s ? s->admitted : 0; }
+
+double vsim_server_clock(const vsim_server* s) { return s ? seconds(s) : 0.0; }
+
+int vsim_server_submit(vsim_server* s, uint32_t session, uint32_t frames, const vsim_drag* drag, uint64_t* request) {
+    clearError();
+    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
+    if (session >= s->admitted) return fail(VSIM_ERR_RANGE, "session is not resident");
+    if (frames < 1) return fail(VSIM_ERR_RANGE, "frames must be at least 1");
+    Request r;
+    r.id = s->nextId++;
+    r.session = session;
+    r.frames = frames;
+    r.submitted = seconds(s);
+    if (drag) {
+        const vsim_sim* sim = s->sim;
+        if (drag->node >= sim->lat[session].nodeCount) return fail(VSIM_ERR_RANGE, "drag node outside the session");
+        const uint32_t global = sim->offsets[session] + drag->node;
+        if (sim->invMass[global] <= 0 || sim->isStatic[global])
+            return fail(VSIM_ERR_INVALID, "[drive] drag node is empty or static");
+        if (!std::isfinite(drag->speed) || drag->speed < 0) return fail(VSIM_ERR_RANGE, "drag speed must be finite");
+        r.drag = true;
+        r.path = *drag;
+    }
+    s->queue[session].push_back(r);
+    s->pending++;
+    if (request) *request = r.id;
+    return VSIM_OK;
+}
+
+int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
+    clearError();
+    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
+    if (stepped) *stepped = 0;
+    vsim_sim* sim = s->sim;
+    DeviceGuard guard(sim->device);
+    const double frameDt = s->substeps * s->stepDuration;
+
+    // The sessions this frame runs, and the nodes their drags hold.
+    bool holdChanged = false;
+    uint32_t active = 0;
+    for (uint32_t i = 0; i < s->admitted; i++) {
+        const bool busy = !s->queue[i].empty();
+        const int64_t want = busy && s->queue[i].front().drag
+                                 ? int64_t(sim->offsets[i] + s->queue[i].front().path.node)
+                                 : int64_t(-1);
+        if (want != s->held[i]) {
+            holdChanged = true;
+            s->held[i] = want;
+            if (want >= 0) {  // a fresh drag starts on its curve (the grab's placement)
+                double p[3], dp[3];
+                bezier(s->queue[i].front().path.control, 0.0, p, dp);
+                for (int a = 0; a < 3; a++) s->prevTarget[3 * i + a] = p[a];
+            }
+        }
+        const uint32_t flag = busy ? 1u : 0u;
+        if (sim->activeHost[i] != flag) {
+            sim->activeHost[i] = flag;
+            sim->tablesDirty = true;
+        }
+        active += flag;
+    }
+    if (active == 0) return VSIM_OK;
+    if (holdChanged) {
+        std::vector<uint32_t> nodes;
+        for (uint32_t i = 0; i < s->admitted; i++)
+            if (s->held[i] >= 0) nodes.push_back(uint32_t(s->held[i]));
+        const std::vector<float> zero(3 * nodes.size(), 0.0f);
+        const int rc = nodes.empty() ? releaseNodes(sim) : holdNodes(sim, nodes.data(), zero.data(), uint32_t(nodes.size()));
+        if (rc) return rc;
+    }
+    // Drag targets advance one frame along their curves at their speed;
+    // velocity is this frame's motion over its duration (simulator.js:309-315).
+    for (uint32_t i = 0; i < s->admitted; i++) {
+        if (s->held[i] < 0) continue;
+        Request& r = s->queue[i].front();
+        double p[3], dp[3];
+        bezier(r.path.control, r.t, p, dp);
+        const double rate = std::sqrt(dp[0] * dp[0] + dp[1] * dp[1] + dp[2] * dp[2]);
+        r.t = std::min(1.0, r.t + r.path.speed * frameDt / std::max(rate, 1e-9));
+        bezier(r.path.control, r.t, p, dp);
+        float4 target = make_float4(float(p[0]), float(p[1]), float(p[2]), 0.0f);
+        float4 velocity = make_float4(float((p[0] - s->prevTarget[3 * i]) / frameDt),
+                                      float((p[1] - s->prevTarget[3 * i + 1]) / frameDt),
+                                      float((p[2] - s->prevTarget[3 * i + 2]) / frameDt), 0.0f);
+        for (int a = 0; a < 3; a++) s->prevTarget[3 * i + a] = p[a];
+        sim->grabsHost[2 * i] = target;
+        sim->grabsHost[2 * i + 1] = velocity;
+        sim->tablesDirty = true;
+    }
+    // Launch over the active sessions' ranges only.
+    std::vector<uint32_t> activeBodies;
+    activeBodies.reserve(active);
+    for (uint32_t i = 0; i < s->admitted; i++)
+        if (sim->activeHost[i]) activeBodies.push_back(i);
+    int rc = planBodies(sim, activeBodies);
+    if (rc) return rc;
+    rc = runFrame(sim, s->substeps);
+    if (rc) return rc;
+    CK(cudaEventRecord(s->frameDone, sim->stream), "serve frame");
+    CK(cudaEventSynchronize(s->frameDone), "serve frame");
+    const double now = seconds(s);
+    for (uint32_t i = 0; i < s->admitted; i++) {
+        if (!sim->activeHost[i]) continue;
+        Request& r = s->queue[i].front();
+        if (r.done == 0) r.firstTick = s->ticks;
+        r.done++;
+        s->sessionFrames++;
+        s->cellUpdates += uint64_t(s->cells[i]) * s->substeps;
+        if (r.done == r.frames) {
+            s->completed.push_back(vsim_completion{r.id, r.session, r.frames, r.submitted, now, r.firstTick, s->ticks});
+            s->queue[i].pop_front();
+            s->pending--;
+        }
+    }
+    s->ticks++;
+    if (stepped) *stepped = active;
+    return VSIM_OK;
+}
+
+int vsim_server_poll(vsim_server* s, vsim_completion* out, uint32_t capacity, uint32_t* count) {
+    clearError();
+    if (!s || !count) return fail(VSIM_ERR_INVALID, "NULL argument");
+    const uint32_t n = std::min<uint32_t>(capacity, uint32_t(s->completed.size()));
+    if (n && out) std::copy(s->completed.begin(), s->completed.begin() + n, out);
+    s->completed.erase(s->completed.begin(), s->completed.begin() + n);
+    *count = n;
+    return VSIM_OK;
+}
+
+int vsim_server_get_stats(const vsim_server* s, vsim_server_stats* out) {
+    if (!s || !out) return fail(VSIM_ERR_INVALID, "NULL argument");
+    out->sessions = s->admitted;
+    out->rejected = s->rejected;
+    out->resident_bytes = s->residentBytes;
+    out->ticks = s->ticks;
+    out->session_frames = s->sessionFrames;
+    out->cell_updates = s->cellUpdates;
+    out->pending = s->pending;
+    return VSIM_OK;
+}
+
+uint32_t vsim_server_node_count(const vsim_server* s, uint32_t session) {
+    return s && session < s->admitted ? s->sim->lat[session].nodeCount : 0;
+}
+
+int vsim_server_read_positions(vsim_server* s, uint32_t session, float* xyzw, size_t node_count) {
+    clearError();
+    if (!s || !xyzw) return fail(VSIM_ERR_INVALID, "NULL argument");
+    if (session >= s->admitted) return fail(VSIM_ERR_RANGE, "session is not resident");
+    vsim_sim* sim = s->sim;
+    DeviceGuard guard(sim->device);
+    if (node_count != sim->lat[session].nodeCount) return fail(VSIM_ERR_CAPACITY, "node_count does not match");
+    CK(cudaMemcpyAsync(xyzw, sim->d.pos + sim->offsets[session], node_count * 16, cudaMemcpyDeviceToHost, sim->stream),
+       "read session");
+    CK(cudaStreamSynchronize(sim->stream), "read session");
+    for (size_t n = 0; n < node_count; n++) xyzw[4 * n + 3] = 0.0f;
+    return VSIM_OK;
+}
+
+}  // extern "C"

@@ -10,105 +10,13 @@
 #include <new>
 #include <numeric>
 
-#include "kernels.cuh"
+#include "sim_internal.cuh"
 
 using namespace vsim;
 
-namespace {
-
-
-// Restores the caller's current device when a call returns.
-struct DeviceGuard {
-    int previous = -1;
-    explicit DeviceGuard(int device) {
-        if (cudaGetDevice(&previous) != cudaSuccess) previous = -1;
-        if (previous != device) cudaSetDevice(device);
-    }
-    ~DeviceGuard() {
-        int now = -1;
-        if (previous >= 0 && cudaGetDevice(&now) == cudaSuccess && now != previous) cudaSetDevice(previous);
-    }
-};
-
-int cudaFail(cudaError_t e, const char* what) {
-    return fail(VSIM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-#define CK(expr, what)                                       \
-    do {                                                     \
-        cudaError_t _e = (expr);                             \
-        if (_e != cudaSuccess) return cudaFail(_e, what);    \
-    } while (0)
-
-template <class T>
-cudaError_t allocN(T** p, size_t n) {
-    *p = nullptr;
-    if (n == 0) n = 1;
-    return cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
-}
+namespace vsim {
 
 __global__ void setParamsKernel(FrameParams* dst, FrameParams src) { *dst = src; }
-
-}  // namespace
-
-struct GraphEntry {
-    uint64_t key;
-    cudaGraphExec_t exec;
-};
-
-struct vsim_sim {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool ownStream = false;
-    cudaStream_t capture = nullptr;
-    uint32_t sms = 1;
-
-    // topology
-    std::vector<Lattice> lat;
-    std::vector<vsim_material> mat;
-    std::vector<uint32_t> offsets;
-    std::vector<uint8_t> isStatic;
-    std::vector<float> invMass;  // material inverse mass (Particles.invMass)
-    std::vector<float> baseW;    // invMass with static nodes zeroed
-    std::vector<float> restPos;  // xyzw per node, w = baseW
-    uint32_t nodeCount = 0, activeCount = 0, cellCount = 0, surfaceCount = 0;
-    uint32_t colorStart[9] = {};
-    std::vector<uint4> surfHost;
-    vsim_tank tank{};
-    Grid grid{};
-
-    // settings
-    double gravity[3] = {0, -9.81, 0};
-    bool paused = false, pendingStep = false;
-    bool contact = true, selfContact = false;
-    uint32_t iterations = 1;
-    bool useGraph = true, pdl = true;
-    uint32_t block = 256, brick = 0;
-    Clock clock;
-    bool stepOverridden = false;
-
-    // drive
-    std::vector<uint32_t> held;
-    int law = VSIM_DRIVE_HARD;
-    double responseTime = kResponseTime;
-    double grabPos[3] = {0, 0, 0}, grabPrev[3] = {0, 0, 0};
-    double grabVel[3] = {0, 0, 0};
-
-    // device
-    DeviceState d;
-    float4* staging = nullptr;
-    uint32_t* pairs = nullptr;
-    size_t pairsCapacity = 0;
-    unsigned long long* pairCount = nullptr;
-    SplatState sp;
-    uint32_t splatCount = 0;
-    std::vector<std::vector<float>> splatMeans, splatQuats, splatScales;  // per body, host copies
-    FrameParams fpHost{};
-    bool paramsDirty = true, frameDirty = true;
-    std::vector<GraphEntry> graphs;
-};
-
-namespace {
 
 StretchLengths stretchLengths() {
     StretchLengths s;
@@ -171,6 +79,13 @@ void bodyParams(const vsim_sim* s, std::vector<DevBody>& out) {
         const float damping = float(m.damping);
         const float arg = -damping * dt;
         d.damp = float(std::exp(double(arg)));
+        const size_t g = s->isolated ? b : 0;
+        for (int a = 0; a < 3; a++) {
+            d.gridOrigin[a] = float(s->grids[g].origin[a]);
+            d.gridDims[a] = s->grids[g].dims[a];
+        }
+        d.bucket = float(s->grids[g].bucket);
+        d.gridBase = s->gridBase[g];
     }
 }
 
@@ -186,21 +101,33 @@ void frameParams(vsim_sim* s) {
         f.tankMax[a] = float(s->tank.max[a]);
         f.grabTarget[a] = float(s->grabPos[a]);
         f.grabVelocity[a] = float(s->grabVel[a]);
-        f.gridOrigin[a] = float(s->grid.origin[a]);
-        f.gridDims[a] = s->grid.dims[a];
     }
     f.invDt2 = 1.0f / (f.dt * f.dt);
     f.responseTime = float(s->responseTime);
     f.drivenCount = uint32_t(s->held.size());
     f.law = uint32_t(s->law);
-    f.bucket = float(s->grid.bucket);
     f.surfaceCount = s->surfaceCount;
+    f.perBodyGrab = s->perBodyGrab ? 1u : 0u;
     f.selfContact = s->selfContact ? 1u : 0u;
     f.activeCount = s->activeCount;
 }
 
 // Uploads what changed since the last frame, in stream order.
 int syncParams(vsim_sim* s) {
+    if (s->tablesDirty) {
+        // Through pinned staging; the staging may still feed a copy queued
+        // by an earlier frame, so let the stream drain before rewriting it
+        // (these tables change between frames, not during a run of them).
+        CK(cudaStreamSynchronize(s->stream), "upload body activity");
+        std::copy(s->activeHost.begin(), s->activeHost.end(), s->activePinned);
+        std::copy(s->grabsHost.begin(), s->grabsHost.end(), s->grabsPinned);
+        CK(cudaMemcpyAsync(s->d.bodyActive, s->activePinned, s->activeHost.size() * 4, cudaMemcpyHostToDevice,
+                           s->stream),
+           "upload body activity");
+        CK(cudaMemcpyAsync(s->d.grabs, s->grabsPinned, s->grabsHost.size() * 16, cudaMemcpyHostToDevice, s->stream),
+           "upload drive targets");
+        s->tablesDirty = false;
+    }
     if (s->paramsDirty) {
         std::vector<DevBody> bodies;
         bodyParams(s, bodies);
@@ -227,7 +154,9 @@ void buildCells(vsim_sim* s, std::vector<uint4>& out) {
     out.reserve(s->cellCount);
     for (int c = 0; c < 8; c++) {
         s->colorStart[c] = uint32_t(out.size());
+        s->colourBodyStart[c].assign(s->lat.size() + 1, 0);
         for (size_t b = 0; b < s->lat.size(); b++) {
+            s->colourBodyStart[c][b] = uint32_t(out.size()) - s->colorStart[c];
             const Lattice& L = s->lat[b];
             std::vector<uint32_t> order(L.cellsByColor[c]);
             if (s->brick > 1) {
@@ -248,8 +177,45 @@ void buildCells(vsim_sim* s, std::vector<uint4>& out) {
                                          L.nodeDims[0], L.nodeDims[0] * L.nodeDims[1]));
             }
         }
+        s->colourBodyStart[c][s->lat.size()] = uint32_t(out.size()) - s->colorStart[c];
     }
     s->colorStart[8] = uint32_t(out.size());
+}
+
+// Spans over every body.
+void buildDensePlan(vsim_sim* s) {
+    FramePlan& p = s->dense;
+    p.chunked = false;
+    p.nodes = denseSpan(s->activeCount, 256);
+    for (int c = 0; c < 8; c++) p.colour[c] = elasticSpan(s->colorStart[c + 1] - s->colorStart[c], s->block, s->sms);
+    p.records = denseSpan(s->surfaceCount, 256);
+}
+
+void useDensePlan(vsim_sim* s) { s->plan = s->dense; }
+
+// One (first, count) chunk per block over the given bodies' ranges.
+int planBodies(vsim_sim* s, const std::vector<uint32_t>& bodies) {
+    size_t at = 0;
+    auto emit = [&](const std::vector<uint32_t>& start, Span& span) {
+        const size_t first = at;
+        for (uint32_t b : bodies)
+            for (uint32_t i = start[b]; i < start[b + 1]; i += kChunk) {
+                if (at == s->chunkCapacity) return false;
+                s->chunkPinned[at++] = make_uint2(i, std::min(kChunk, start[b + 1] - i));
+            }
+        span = Span{Work{s->chunkDev + first, 0}, uint32_t(at - first), kChunk};
+        return true;
+    };
+    FramePlan p;
+    p.chunked = true;
+    bool ok = emit(s->nodeBodyStart, p.nodes);
+    for (int c = 0; c < 8 && ok; c++) ok = emit(s->colourBodyStart[c], p.colour[c]);
+    ok = ok && emit(s->recordBodyStart, p.records);
+    if (!ok) return fail(VSIM_ERR_CAPACITY, "chunk table too small");
+    CK(cudaMemcpyAsync(s->chunkDev, s->chunkPinned, at * sizeof(uint2), cudaMemcpyHostToDevice, s->stream),
+       "upload work chunks");
+    s->plan = p;
+    return VSIM_OK;
 }
 
 // Brackets kernel groups with events on the launching stream.
@@ -304,9 +270,10 @@ cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMod
     };
     // The first substep's prediction runs on its own; every later one rides
     // on the closing pass of the substep before it.
+    const FramePlan& plan = s->plan;
     if (steps > 0) {
         begin(VSIM_KIND_PREDICT, 1);
-        if ((e = launchPredict(c, s->d, s->activeCount))) return e;
+        if ((e = launchPredict(c, s->d, plan.nodes))) return e;
         end();
     }
     for (uint32_t step = 0; step < steps; step++) {
@@ -317,29 +284,28 @@ cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMod
         }
         for (uint32_t it = 0; it < s->iterations; it++)
             for (int col = 0; col < 8; col++) {
-                const uint32_t n = s->colorStart[col + 1] - s->colorStart[col];
-                if (!n) continue;
+                if (!plan.colour[col].grid) continue;
                 begin(VSIM_KIND_ELASTIC, 1);
-                if ((e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], n, false, s->block, lens))) return e;
+                if ((e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], plan.colour[col], false, lens)))
+                    return e;
                 end();
             }
         if (limited)
             for (int sweep = 0; sweep < 3; sweep++)
                 for (int col = 0; col < 8; col++) {
-                    const uint32_t n = s->colorStart[col + 1] - s->colorStart[col];
-                    if (!n) continue;
+                    if (!plan.colour[col].grid) continue;
                     begin(VSIM_KIND_LIMIT, 1);
-                    if ((e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], n, true, s->block, lens)))
+                    if ((e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], plan.colour[col], true, lens)))
                         return e;
                     end();
                 }
-        if (contact) {
+        if (contact && plan.records.grid) {
             begin(VSIM_KIND_CONTACT, kContactKernels);
-            if ((e = launchContact(c, s->d, s->surfaceCount, mode, nullptr, 0, nullptr))) return e;
+            if ((e = launchContact(c, s->d, plan.records, mode, nullptr, 0, nullptr))) return e;
             end();
         }
         begin(VSIM_KIND_FINALIZE, 1);
-        if ((e = launchFinalize(c, s->d, s->activeCount, contact && mode == ContactMode::Solve, step + 1 < steps)))
+        if ((e = launchFinalize(c, s->d, plan.nodes, contact && mode == ContactMode::Solve, step + 1 < steps)))
             return e;
         end();
     }
@@ -365,7 +331,9 @@ void dropGraphs(vsim_sim* s) {
 int runFrame(vsim_sim* s, uint32_t steps) {
     int rc = syncParams(s);
     if (rc) return rc;
-    if (!s->useGraph) {
+    // A chunked plan changes every frame: launch it directly (with
+    // programmatic dependent launch) rather than capture it.
+    if (!s->useGraph || s->plan.chunked) {
         CK(encodeFrame(s, s->stream, steps), "launch substep");
         return VSIM_OK;
     }
@@ -396,16 +364,20 @@ int runFrame(vsim_sim* s, uint32_t steps) {
     return VSIM_OK;
 }
 
-void freeAll(vsim_sim* s) {
+void freeSim(vsim_sim* s) {
     dropGraphs(s);
     DeviceState& d = s->d;
     void* ptrs[] = {d.pos, d.prev, d.vel, d.baseW, d.active, d.activeBody, d.cells, d.bodies, d.fp,
                     d.surf, d.key, d.rank, d.entries, d.count, d.start, d.cursor, d.delta, d.driven,
-                    d.drivenOffset, d.nodeRecord, d.sMeta, d.sPos, d.sRec, s->staging, s->pairs, s->pairCount, s->sp.embed, s->sp.quat,
+                    d.drivenOffset, d.nodeRecord, d.sMeta, d.sPos, d.sRec, d.bodyActive, d.grabs,
+                    s->chunkDev, s->staging, s->pairs, s->pairCount, s->sp.embed, s->sp.quat,
                     s->sp.scaleBody, s->sp.bodies, s->sp.meanDepth, s->sp.cov, s->sp.keys, s->sp.order,
                     s->sp.sortTemp};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    void* pinned[] = {s->chunkPinned, s->activePinned, s->grabsPinned};
+    for (void* p : pinned)
+        if (p) cudaFreeHost(p);
     if (s->capture) cudaStreamDestroy(s->capture);
     if (s->ownStream && s->stream) cudaStreamDestroy(s->stream);
 }
@@ -422,7 +394,23 @@ int zeroHeld(vsim_sim* s) {
     return VSIM_OK;
 }
 
-int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void* stream, vsim_sim* s) {
+// An isolated body's contact grid: its rest box padded by a quarter of its
+// extent (at least four buckets) per side, clipped to the tank. A node that
+// leaves it is binned at the rim, which costs gather time, never a contact.
+Grid bodyGrid(const Lattice& L, const vsim_tank& tank) {
+    vsim_tank box;
+    for (int a = 0; a < 3; a++) {
+        const double pad = std::max(0.25 * L.cellDims[a] * L.h, 8 * L.h * kContactRadiusCells);
+        box.min[a] = std::max(tank.min[a], L.origin[a] - pad);
+        box.max[a] = std::min(tank.max[a], L.origin[a] + L.cellDims[a] * L.h + pad);
+    }
+    const double zero[3] = {0, 0, 0};
+    return contactGrid(box, L.h * kContactRadiusCells, zero, zero);
+}
+
+int createSim(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void* stream, bool isolated,
+              vsim_sim* s) {
+    s->isolated = isolated;
     if (n > 0 && !bodies) return fail(VSIM_ERR_INVALID, "bodies is NULL");
     CK(cudaGetDevice(&s->device), "query device");
     int major = 0;
@@ -470,7 +458,9 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
     // whose solver inverse mass is zero, as the reference does; the closing
     // pass still settles and un-bins the static ones on the surface.
     std::vector<uint32_t> active, activeBody;
-    for (uint32_t b = 0; b < n; b++)
+    s->nodeBodyStart.assign(size_t(n) + 1, 0);
+    for (uint32_t b = 0; b < n; b++) {
+        s->nodeBodyStart[b] = uint32_t(active.size());
         for (uint32_t m = 0; m < s->lat[b].nodeCount; m++) {
             const uint32_t node = s->offsets[b] + m;
             if (s->invMass[node] > 0) {
@@ -478,14 +468,18 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
                 activeBody.push_back(b);
             }
         }
+    }
+    s->nodeBodyStart[n] = uint32_t(active.size());
     s->activeCount = uint32_t(active.size());
 
     // Surface records (bodyContact.js:325-340), radius h/2.
     double widest = 0;
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    s->recordBodyStart.assign(size_t(n) + 1, 0);
     for (uint32_t b = 0; b < n; b++) {
         const Lattice& L = s->lat[b];
         const float radius = float(L.h * kContactRadiusCells);
+        s->recordBodyStart[b] = uint32_t(s->surfHost.size());
         for (uint32_t node : L.surface) {
             const uint32_t i = node % L.nodeDims[0], j = (node / L.nodeDims[0]) % L.nodeDims[1],
                            k = node / (L.nodeDims[0] * L.nodeDims[1]);
@@ -501,8 +495,20 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
         }
     }
     s->surfaceCount = uint32_t(s->surfHost.size());
-    s->grid = contactGrid(s->tank, widest, lo, hi);
-    if (double(s->grid.count()) > 4.0 * kGridLimit) return fail(VSIM_ERR_RANGE, "contact grid too large");
+    s->recordBodyStart[n] = s->surfaceCount;
+    if (!s->isolated) {
+        s->grids.push_back(contactGrid(s->tank, widest, lo, hi));
+    } else {
+        for (uint32_t b = 0; b < n; b++) s->grids.push_back(bodyGrid(s->lat[b], s->tank));
+    }
+    for (const Grid& g : s->grids) {
+        s->gridBase.push_back(uint32_t(s->bucketTotal));
+        s->bucketTotal += g.count();
+    }
+    if (double(s->bucketTotal) > 16.0 * kGridLimit) return fail(VSIM_ERR_RANGE, "contact grids too large");
+    s->activeHost.assign(n ? n : 1, 1u);
+    s->grabsHost.assign(2 * size_t(n ? n : 1), make_float4(0, 0, 0, 0));
+    s->tablesDirty = true;
 
     // Clock (simulator.js:88).
     s->clock.stepDuration = stableStepDuration(waveRateOf(s, nullptr));
@@ -538,12 +544,16 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
     CK(allocN(&d.sPos, s->surfaceCount), "allocate contact runs");
     CK(allocN(&d.sRec, s->surfaceCount), "allocate contact runs");
     CK(allocN(&d.nodeRecord, N), "allocate node records");
-    CK(allocN(&d.count, s->grid.count()), "allocate contact grid");
-    CK(allocN(&d.start, s->grid.count()), "allocate contact grid");
+    CK(allocN(&d.count, s->bucketTotal), "allocate contact grid");
+    CK(allocN(&d.start, s->bucketTotal), "allocate contact grid");
+    CK(allocN(&d.bodyActive, s->activeHost.size()), "allocate body activity");
+    CK(allocN(&d.grabs, s->grabsHost.size()), "allocate drive targets");
     CK(allocN(&d.cursor, 1), "allocate contact cursor");
     CK(allocN(&d.driven, VSIM_MAX_DRIVEN), "allocate drive");
     CK(allocN(&d.drivenOffset, VSIM_MAX_DRIVEN), "allocate drive");
     CK(allocN(&s->pairCount, 1), "allocate pair counter");
+    CK(cudaMallocHost(&s->activePinned, s->activeHost.size() * 4), "allocate staging");
+    CK(cudaMallocHost(&s->grabsPinned, s->grabsHost.size() * 16), "allocate staging");
 
     // Initial state (particles.js:67-102).
     s->restPos.assign(4 * N, 0.0f);
@@ -559,6 +569,21 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
     }
     std::vector<uint4> cells;
     buildCells(s, cells);
+    buildDensePlan(s);
+    useDensePlan(s);
+    if (isolated) {
+        // Room for a chunk table over every body at once.
+        size_t chunks = 0;
+        auto count = [&](const std::vector<uint32_t>& start) {
+            for (uint32_t b = 0; b < n; b++) chunks += (start[b + 1] - start[b] + kChunk - 1) / kChunk;
+        };
+        count(s->nodeBodyStart);
+        for (int c = 0; c < 8; c++) count(s->colourBodyStart[c]);
+        count(s->recordBodyStart);
+        s->chunkCapacity = chunks;
+        CK(allocN(&s->chunkDev, chunks), "allocate work chunks");
+        CK(cudaMallocHost(&s->chunkPinned, std::max<size_t>(chunks, 1) * sizeof(uint2)), "allocate staging");
+    }
     std::vector<int32_t> nodeRecord(N, -1);
     for (uint32_t r = 0; r < s->surfaceCount; r++) nodeRecord[s->surfHost[r].x] = int32_t(r);
     CK(cudaMemcpyAsync(d.nodeRecord, nodeRecord.data(), N * 4, cudaMemcpyHostToDevice, s->stream), "upload records");
@@ -572,7 +597,7 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
     CK(cudaMemcpyAsync(d.cells, cells.data(), cells.size() * 16, cudaMemcpyHostToDevice, s->stream), "upload cells");
     CK(cudaMemcpyAsync(d.surf, s->surfHost.data(), s->surfHost.size() * 16, cudaMemcpyHostToDevice, s->stream),
        "upload surface");
-    CK(cudaMemsetAsync(d.count, 0, s->grid.count() * 4, s->stream), "clear grid");
+    CK(cudaMemsetAsync(d.count, 0, s->bucketTotal * 4, s->stream), "clear grid");
     CK(cudaMemsetAsync(d.cursor, 0, 4, s->stream), "clear grid");
     s->paramsDirty = true;
     int rc = syncParams(s);
@@ -584,34 +609,43 @@ int create(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void
     return VSIM_OK;
 }
 
-#define SIM_GUARD(s)                                                                  \
-    if (!(s)) return fail(VSIM_ERR_INVALID, "simulator handle is NULL");              \
-    DeviceGuard _guard((s)->device);                                                  \
-    clearError()
-
-}  // namespace
+}  // namespace vsim
 
 extern "C" {
 
-int vsim_create(const vsim_body_desc* bodies, uint32_t body_count, const vsim_tank* tank, void* stream,
-                vsim_sim** out) {
+int vsim_create_ex(const vsim_body_desc* bodies, uint32_t body_count, const vsim_tank* tank, void* stream,
+                   uint32_t flags, vsim_sim** out) {
     clearError();
     if (!out) return fail(VSIM_ERR_INVALID, "out is NULL");
     *out = nullptr;
+    if (flags & ~uint32_t(VSIM_CREATE_ISOLATED)) return fail(VSIM_ERR_INVALID, "unknown creation flags");
     vsim_sim* s = new (std::nothrow) vsim_sim();
     if (!s) return fail(VSIM_ERR_NOMEM, "out of host memory");
     int rc;
     try {
-        rc = create(bodies, body_count, tank, stream, s);
+        rc = createSim(bodies, body_count, tank, stream, (flags & VSIM_CREATE_ISOLATED) != 0, s);
     } catch (const std::bad_alloc&) {
         rc = fail(VSIM_ERR_NOMEM, "out of host memory");
     }
     if (rc != VSIM_OK) {
-        freeAll(s);
+        freeSim(s);
         delete s;
         return rc;
     }
     *out = s;
+    return VSIM_OK;
+}
+
+int vsim_create(const vsim_body_desc* bodies, uint32_t body_count, const vsim_tank* tank, void* stream,
+                vsim_sim** out) {
+    return vsim_create_ex(bodies, body_count, tank, stream, 0, out);
+}
+
+int vsim_set_bodies_active(vsim_sim* s, const uint8_t* active, uint32_t count) {
+    SIM_GUARD(s);
+    if (count != s->lat.size()) return fail(VSIM_ERR_CAPACITY, "count does not match the body count");
+    for (uint32_t b = 0; b < count; b++) s->activeHost[b] = active ? (active[b] ? 1u : 0u) : 1u;
+    s->tablesDirty = true;
     return VSIM_OK;
 }
 
@@ -620,7 +654,7 @@ int vsim_destroy(vsim_sim* sim) {
     {
         DeviceGuard guard(sim->device);
         cudaStreamSynchronize(sim->stream);
-        freeAll(sim);
+        freeSim(sim);
     }
     delete sim;
     return VSIM_OK;
@@ -734,6 +768,54 @@ int vsim_read_inv_mass(vsim_sim* s, float* inv_mass, size_t node_count) {
     return VSIM_OK;
 }
 
+}  // extern "C"
+
+namespace vsim {
+
+uint32_t bodyOfNode(const vsim_sim* s, uint32_t node) {
+    // pick.js:77-83, by bisection over the ascending body offsets.
+    const auto it = std::upper_bound(s->offsets.begin(), s->offsets.end(), node);
+    return uint32_t(it - s->offsets.begin()) - 1;
+}
+
+int holdNodes(vsim_sim* s, const uint32_t* nodes, const float* offsets, uint32_t count) {
+    if (count == 0) return releaseNodes(s);
+    const uint32_t kept = std::min<uint32_t>(count, VSIM_MAX_DRIVEN);
+    int rc = restoreHeld(s);
+    if (rc) return rc;
+    std::vector<float4> off(kept);
+    s->heldBody.resize(kept);
+    for (uint32_t i = 0; i < kept; i++) {
+        const uint32_t body = bodyOfNode(s, nodes[i]);
+        float bits;
+        std::memcpy(&bits, &body, 4);
+        s->heldBody[i] = body;
+        off[i] = make_float4(offsets[3 * i], offsets[3 * i + 1], offsets[3 * i + 2], bits);
+    }
+    CK(cudaMemcpyAsync(s->d.driven, nodes, kept * 4, cudaMemcpyHostToDevice, s->stream), "upload hold");
+    CK(cudaMemcpyAsync(s->d.drivenOffset, off.data(), kept * 16, cudaMemcpyHostToDevice, s->stream), "upload hold");
+    // Copies from pageable memory return once the data is staged, so `off`
+    // may go out of scope; everything after them is in stream order.
+    s->held.assign(nodes, nodes + kept);
+    rc = zeroHeld(s);
+    if (rc) return rc;
+    s->frameDirty = true;
+    return kept < count ? fail(VSIM_OK, "hold truncated to VSIM_MAX_DRIVEN nodes") : VSIM_OK;
+}
+
+int releaseNodes(vsim_sim* s) {
+    int rc = restoreHeld(s);
+    if (rc) return rc;
+    s->held.clear();
+    s->heldBody.clear();
+    s->frameDirty = true;
+    return VSIM_OK;
+}
+
+}  // namespace vsim
+
+extern "C" {
+
 // kinematicDrive.js:155-191.
 int vsim_hold(vsim_sim* s, const uint32_t* nodes, const float* offsets, uint32_t count) {
     SIM_GUARD(s);
@@ -742,20 +824,7 @@ int vsim_hold(vsim_sim* s, const uint32_t* nodes, const float* offsets, uint32_t
         if (nodes[i] >= s->nodeCount) return fail(VSIM_ERR_RANGE, "held node outside the scene");
         if (s->isStatic[nodes[i]]) return fail(VSIM_ERR_INVALID, "[drive] cannot hold a static prescribed node");
     }
-    if (count == 0) return vsim_release(s);
-    const uint32_t kept = std::min<uint32_t>(count, VSIM_MAX_DRIVEN);
-    int rc = restoreHeld(s);
-    if (rc) return rc;
-    std::vector<float4> off(kept);
-    for (uint32_t i = 0; i < kept; i++) off[i] = make_float4(offsets[3 * i], offsets[3 * i + 1], offsets[3 * i + 2], 0);
-    CK(cudaMemcpyAsync(s->d.driven, nodes, kept * 4, cudaMemcpyHostToDevice, s->stream), "upload hold");
-    CK(cudaMemcpyAsync(s->d.drivenOffset, off.data(), kept * 16, cudaMemcpyHostToDevice, s->stream), "upload hold");
-    s->held.assign(nodes, nodes + kept);
-    rc = zeroHeld(s);
-    if (rc) return rc;
-    CK(cudaStreamSynchronize(s->stream), "upload hold");
-    s->frameDirty = true;
-    return kept < count ? fail(VSIM_OK, "hold truncated to VSIM_MAX_DRIVEN nodes") : VSIM_OK;
+    return holdNodes(s, nodes, offsets, count);
 }
 
 int vsim_move_grab(vsim_sim* s, const double position[3]) {
@@ -775,11 +844,7 @@ int vsim_place_grab(vsim_sim* s, const double position[3]) {
 
 int vsim_release(vsim_sim* s) {
     SIM_GUARD(s);
-    int rc = restoreHeld(s);
-    if (rc) return rc;
-    s->held.clear();
-    s->frameDirty = true;
-    return VSIM_OK;
+    return releaseNodes(s);
 }
 
 int vsim_set_drive_law(vsim_sim* s, int law) {
@@ -906,6 +971,8 @@ int vsim_set_launch_shape(vsim_sim* s, uint32_t block, uint32_t brick) {
            "upload cells");
         CK(cudaStreamSynchronize(s->stream), "upload cells");
     }
+    buildDensePlan(s);
+    if (!s->plan.chunked) useDensePlan(s);
     return VSIM_OK;
 }
 
@@ -1014,7 +1081,7 @@ int vsim_contact_pairs(vsim_sim* s, uint32_t* pairs, size_t capacity, size_t* co
     if (rc) return rc;
     CK(cudaMemsetAsync(s->pairCount, 0, sizeof(unsigned long long), s->stream), "count pairs");
     const LaunchCtx c{s->stream, false, s->sms};
-    CK(launchContact(c, s->d, s->surfaceCount, ContactMode::Pairs, s->pairs, uint32_t(capacity), s->pairCount),
+    CK(launchContact(c, s->d, s->dense.records, ContactMode::Pairs, s->pairs, uint32_t(capacity), s->pairCount),
        "list pairs");
     unsigned long long total = 0;
     CK(cudaMemcpyAsync(&total, s->pairCount, sizeof total, cudaMemcpyDeviceToHost, s->stream), "count pairs");

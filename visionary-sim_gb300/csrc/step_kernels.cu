@@ -150,12 +150,13 @@ __device__ __forceinline__ void projectTet(V (&p)[8], const V (&prev)[8], const 
 // ------------------------------------------------------------- kernels --
 
 // predict.wgsl:19-36 over the active nodes.
-__global__ void predictKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ active,
+__global__ void predictKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ active,
+                              const uint32_t* __restrict__ activeBody, const uint32_t* __restrict__ bodyActive,
                               float4* __restrict__ pos, float4* __restrict__ prev, float4* __restrict__ vel) {
     pdlWait();
     pdlLaunchNext();
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= fp->activeCount) return;
+    uint32_t i;
+    if (!workItem(work, i) || !bodyActive[activeBody[i]]) return;
     const uint32_t n = active[i];
     const float4 P = pos[n];
     if (P.w == 0.0f) return;
@@ -169,20 +170,32 @@ __global__ void predictKernel(const FrameParams* __restrict__ fp, const uint32_t
 }
 
 // driveHard.wgsl:15-35 and driveCompliant.wgsl:24-41.
+// Each driven record carries its body in offsets.w; the target is the scene's
+// single grab target, or with perBodyGrab the body's own row of `grabs`.
 __global__ void driveKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ driven,
-                            const float4* __restrict__ offsets, float4* __restrict__ pos, float4* __restrict__ prev,
+                            const float4* __restrict__ offsets, const uint32_t* __restrict__ bodyActive,
+                            const float4* __restrict__ grabs, float4* __restrict__ pos, float4* __restrict__ prev,
                             float4* __restrict__ vel) {
     pdlWait();
     pdlLaunchNext();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= fp->drivenCount) return;
+    const float4 off = offsets[i];
+    const uint32_t body = __float_as_uint(off.w);
+    if (!bodyActive[body]) return;
     const uint32_t n = driven[i];
     const float dt = fp->dt;
-    const V goal = mk(fp->grabTarget[0], fp->grabTarget[1], fp->grabTarget[2]) + xyz(offsets[i]);
+    V target = mk(fp->grabTarget[0], fp->grabTarget[1], fp->grabTarget[2]);
+    V velocity = mk(fp->grabVelocity[0], fp->grabVelocity[1], fp->grabVelocity[2]);
+    if (fp->perBodyGrab) {
+        target = xyz(grabs[2 * body]);
+        velocity = xyz(grabs[2 * body + 1]);
+    }
+    const V goal = target + xyz(off);
     const float4 P = pos[n];
     if (fp->law == VSIM_DRIVE_HARD) {
         const V here = xyz(P);
-        const V step = mk(fp->grabVelocity[0], fp->grabVelocity[1], fp->grabVelocity[2]) * dt;
+        const V step = velocity * dt;
         const V toGoal = goal - here;
         const V next = here + (dot(step, step) >= dot(toGoal, toGoal) ? toGoal : step);
         prev[n] = withW(here, 0.0f);
@@ -201,14 +214,16 @@ __global__ void driveKernel(const FrameParams* __restrict__ fp, const uint32_t* 
 // `cells` holds (global node of corner 0, body, node stride along y, along z)
 // per cell of this colour, so the corner loads wait on one load only.
 template <bool LIMIT_ONLY>
-__global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ cells, uint32_t count,
-                                                     const DevBody* __restrict__ bodies, float4* __restrict__ pos,
+__global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ cells, Work work,
+                                                     const DevBody* __restrict__ bodies,
+                                                     const uint32_t* __restrict__ bodyActive, float4* __restrict__ pos,
                                                      const float4* __restrict__ prevState, StretchLengths lens) {
     pdlWait();
     pdlLaunchNext();
-    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= count) return;
+    uint32_t slot;
+    if (!workItem(work, slot)) return;
     const uint4 entry = cells[slot];
+    if (!bodyActive[entry.y]) return;
     const DevBody* b = bodies + entry.y;
     const float maxStretch = b->maxStretch;
     if (LIMIT_ONLY && !(maxStretch > 1.0f)) return;
@@ -283,20 +298,22 @@ __device__ __forceinline__ V resolvePlane(V p, V prev, V normal, float depth, fl
 // predict.wgsl:19-36 from the position and velocity it has just computed,
 // which are the values that pass would read back.
 template <bool CONTACT, bool PREDICT>
-__global__ void finalizeKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ active,
+__global__ void finalizeKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ active,
                                const uint32_t* __restrict__ activeBody, const DevBody* __restrict__ bodies,
                                float4* __restrict__ pos, float4* __restrict__ prevState, float4* __restrict__ vel,
                                const int32_t* __restrict__ nodeRecord, const float4* __restrict__ delta,
                                const uint32_t* __restrict__ key, uint32_t* __restrict__ count,
-                               uint32_t* __restrict__ cursor) {
+                               uint32_t* __restrict__ cursor, const uint32_t* __restrict__ bodyActive) {
     pdlWait();
     pdlLaunchNext();
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= fp->activeCount) return;
+    if (CONTACT && blockIdx.x == 0 && threadIdx.x == 0) *cursor = 0;
+    uint32_t i;
+    if (!workItem(work, i)) return;
+    const uint32_t bodyIndex = activeBody[i];
+    if (!bodyActive[bodyIndex]) return;
     const uint32_t n = active[i];
     float4 P = pos[n];
     if (CONTACT) {
-        if (i == 0) *cursor = 0;
         const int32_t r = nodeRecord[n];
         if (r >= 0) {
             const float4 d = delta[r];
@@ -309,7 +326,7 @@ __global__ void finalizeKernel(const FrameParams* __restrict__ fp, const uint32_
         }
     }
     if (P.w == 0.0f) return;
-    const DevBody* b = bodies + activeBody[i];
+    const DevBody* b = bodies + bodyIndex;
     const V prev = xyz(prevState[n]);
     const float fr = b->friction;
     const V mn = mk(fp->tankMin[0], fp->tankMin[1], fp->tankMin[2]);
@@ -345,42 +362,53 @@ __global__ void finalizeKernel(const FrameParams* __restrict__ fp, const uint32_
 // segment's first 32 entries -- the same visible set, in the same order, with
 // work proportional to the surface rather than to the grid.
 
-// contacts.wgsl:84-91.
-__device__ __forceinline__ uint32_t bucketOf(const FrameParams* fp, V p, int coord[3]) {
+// contacts.wgsl:84-91, in the body's grid; returns the bucket's index in the
+// bucket arrays (the grid's base plus its linear index).
+__device__ __forceinline__ uint32_t bucketOf(const DevBody* b, V p, int coord[3]) {
     const float q[3] = {p.x, p.y, p.z};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const float last = float(fp->gridDims[a]) - 1.0f;
-        const float f = floorf((q[a] - fp->gridOrigin[a]) / fp->bucket);
+        const float last = float(b->gridDims[a]) - 1.0f;
+        const float f = floorf((q[a] - b->gridOrigin[a]) / b->bucket);
         coord[a] = int(fminf(fmaxf(f, 0.0f), last));
     }
-    return uint32_t(coord[0]) + fp->gridDims[0] * (uint32_t(coord[1]) + fp->gridDims[1] * uint32_t(coord[2]));
+    return b->gridBase + uint32_t(coord[0]) + b->gridDims[0] * (uint32_t(coord[1]) + b->gridDims[1] * uint32_t(coord[2]));
 }
 
-__global__ void binKernel(const FrameParams* __restrict__ fp, const uint4* __restrict__ surf,
+constexpr uint32_t kIdle = 0xffffffffu;  // key and rank of a record whose body sits out the frame
+
+__global__ void binKernel(const FrameParams* __restrict__ fp, Work work, const uint4* __restrict__ surf,
+                          const DevBody* __restrict__ bodies, const uint32_t* __restrict__ bodyActive,
                           const float4* __restrict__ pos, uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
                           uint32_t* __restrict__ count) {
     pdlWait();
     pdlLaunchNext();
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= fp->surfaceCount) return;
+    uint32_t r;
+    if (!workItem(work, r)) return;
+    const uint4 rec = surf[r];
+    if (!bodyActive[rec.y]) {
+        key[r] = kIdle;
+        rank[r] = kIdle;
+        return;
+    }
     int coord[3];
-    const uint32_t b = bucketOf(fp, xyz(pos[surf[r].x]), coord);
+    const uint32_t b = bucketOf(bodies + rec.y, xyz(pos[rec.x]), coord);
     key[r] = b;
     rank[r] = atomicAdd(&count[b], 1u);
 }
 
 // Each bucket's first-arriving record reserves the bucket's segment; one
 // atomic per block on the shared cursor.
-__global__ void allocKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ key,
+__global__ void allocKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ key,
                             const uint32_t* __restrict__ rank, const uint32_t* __restrict__ count,
                             uint32_t* __restrict__ start, uint32_t* __restrict__ cursor) {
     pdlWait();
     pdlLaunchNext();
     __shared__ uint32_t warpSum[32];
     __shared__ uint32_t blockBase;
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool first = r < fp->surfaceCount && rank[r] == 0;
+    uint32_t r = 0;
+    const bool has = workItem(work, r);
+    const bool first = has && rank[r] == 0;
     const uint32_t b = first ? key[r] : 0;
     const uint32_t need = first ? count[b] : 0;
     // Block-wide exclusive prefix of `need`.
@@ -409,13 +437,13 @@ __global__ void allocKernel(const FrameParams* __restrict__ fp, const uint32_t* 
     if (first) start[b] = blockBase + warpSum[warp] + (incl - need);
 }
 
-__global__ void scatterKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ key,
+__global__ void scatterKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ key,
                               const uint32_t* __restrict__ rank, const uint32_t* __restrict__ start,
                               uint32_t* __restrict__ entries) {
     pdlWait();
     pdlLaunchNext();
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= fp->surfaceCount) return;
+    uint32_t r;
+    if (!workItem(work, r) || key[r] == kIdle) return;
     entries[start[key[r]] + rank[r]] = r;
 }
 
@@ -423,15 +451,15 @@ __global__ void scatterKernel(const FrameParams* __restrict__ fp, const uint32_t
 // record indices -- in ascending order at the front of its segment; then
 // their records and positions copied out in that order, so the gather reads
 // each neighbour bucket as one contiguous run.
-__global__ void canonKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ key,
+__global__ void canonKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ key,
                             const uint32_t* __restrict__ rank, const uint32_t* __restrict__ start,
                             const uint32_t* __restrict__ count, uint32_t* __restrict__ entries,
                             const uint4* __restrict__ surf, const float4* __restrict__ pos, uint4* __restrict__ sMeta,
                             float4* __restrict__ sPos, uint32_t* __restrict__ sRec) {
     pdlWait();
     pdlLaunchNext();
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= fp->surfaceCount || rank[r] != 0) return;
+    uint32_t r;
+    if (!workItem(work, r) || rank[r] != 0) return;
     const uint32_t b = key[r];
     const uint32_t n = count[b];
     const uint32_t base = start[b];
@@ -493,8 +521,9 @@ __device__ __forceinline__ bool admitted(uint4 a, uint4 b, uint32_t selfContact)
 // (r, other) is also appended to `pairs` (capacity-checked), for the
 // pair-set checks.
 template <bool EMIT>
-__global__ void collideKernel(const FrameParams* __restrict__ fp, const uint4* __restrict__ surf,
-                              const DevBody* __restrict__ bodies, const float4* __restrict__ pos,
+__global__ void collideKernel(const FrameParams* __restrict__ fp, Work work, const uint4* __restrict__ surf,
+                              const DevBody* __restrict__ bodies, const uint32_t* __restrict__ bodyActive,
+                              const float4* __restrict__ pos,
                               const float4* __restrict__ prevState, const uint32_t* __restrict__ start,
                               const uint32_t* __restrict__ count, const uint4* __restrict__ sMeta,
                               const float4* __restrict__ sPos, const uint32_t* __restrict__ sRec,
@@ -502,9 +531,11 @@ __global__ void collideKernel(const FrameParams* __restrict__ fp, const uint4* _
                               unsigned long long* __restrict__ pairCount) {
     pdlWait();
     pdlLaunchNext();
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= fp->surfaceCount) return;
+    uint32_t r;
+    if (!workItem(work, r)) return;
     const uint4 me = surf[r];
+    const DevBody* grid = bodies + me.y;
+    if (!bodyActive[me.y]) return;
     const uint32_t node = me.x;
     const float radius = __uint_as_float(me.w);
     const float4 P = pos[node];
@@ -516,8 +547,9 @@ __global__ void collideKernel(const FrameParams* __restrict__ fp, const uint4* _
     V sum = mk(0.0f, 0.0f, 0.0f);
     float hits = 0.0f;
     int centre[3];
-    bucketOf(fp, pi, centre);
-    const int dims[3] = {int(fp->gridDims[0]), int(fp->gridDims[1]), int(fp->gridDims[2])};
+    bucketOf(grid, pi, centre);
+    const int dims[3] = {int(grid->gridDims[0]), int(grid->gridDims[1]), int(grid->gridDims[2])};
+    const uint32_t base = grid->gridBase;
     // All 27 bucket counts first (independent loads), then the runs in
     // the reference's dz, dy, dx order.
     uint32_t cnt[27], bkt[27];
@@ -525,7 +557,7 @@ __global__ void collideKernel(const FrameParams* __restrict__ fp, const uint4* _
     for (int q = 0; q < 27; q++) {
         const int x = centre[0] + q % 3 - 1, y = centre[1] + (q / 3) % 3 - 1, z = centre[2] + q / 9 - 1;
         const bool inside = x >= 0 && x < dims[0] && y >= 0 && y < dims[1] && z >= 0 && z < dims[2];
-        bkt[q] = inside ? uint32_t(x) + fp->gridDims[0] * (uint32_t(y) + fp->gridDims[1] * uint32_t(z)) : 0u;
+        bkt[q] = inside ? base + uint32_t(x) + uint32_t(dims[0]) * (uint32_t(y) + uint32_t(dims[1]) * uint32_t(z)) : 0u;
         cnt[q] = inside ? count[bkt[q]] : 0u;
     }
 #pragma unroll
@@ -581,14 +613,16 @@ __global__ void collideKernel(const FrameParams* __restrict__ fp, const uint4* _
 
 // settle.wgsl:20-36 (gain 1, bodyContact.js:48), then empties the buckets
 // this substep used and the segment cursor, restoring the empty grid.
-__global__ void settleKernel(const FrameParams* __restrict__ fp, const uint4* __restrict__ surf,
+__global__ void settleKernel(const FrameParams* __restrict__ fp, Work work, const uint4* __restrict__ surf,
                              const uint32_t* __restrict__ key, const float4* __restrict__ delta,
                              float4* __restrict__ pos, uint32_t* __restrict__ count, uint32_t* __restrict__ cursor,
                              int apply) {
     pdlWait();
     pdlLaunchNext();
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= fp->surfaceCount) return;
+    uint32_t r;
+    const bool has = workItem(work, r);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *cursor = 0;
+    if (!has) return;
     if (apply) {
         const float4 d = delta[r];
         if (d.w > 0.0f) {
@@ -598,8 +632,7 @@ __global__ void settleKernel(const FrameParams* __restrict__ fp, const uint4* __
             pos[node] = withW(xyz(P) + step, P.w);
         }
     }
-    count[key[r]] = 0;
-    if (r == 0) *cursor = 0;
+    if (key[r] != kIdle) count[key[r]] = 0;
 }
 
 // ------------------------------------------------------- node utilities --
@@ -654,37 +687,39 @@ cudaError_t launch(const LaunchCtx& ctx, void (*kernel)(KArgs...), uint32_t grid
 inline uint32_t blocks(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
 }  // namespace
 
-cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount) {
-    return launch(c, predictKernel, blocks(activeCount, 256), 256, s.fp, s.active, s.pos, s.prev, s.vel);
-}
-
-cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drivenCount) {
-    return launch(c, driveKernel, blocks(drivenCount, 256), 256, s.fp, s.driven, s.drivenOffset, s.pos, s.prev, s.vel);
-}
+Span denseSpan(uint32_t count, uint32_t block) { return Span{Work{nullptr, count}, blocks(count, block), block}; }
 
 // A colour pass of a small scene has too few cells to put a block of the
 // configured size on every SM; smaller blocks spread it over all of them.
-inline uint32_t elasticBlock(uint32_t count, uint32_t block, uint32_t sms) {
+Span elasticSpan(uint32_t count, uint32_t block, uint32_t sms) {
     while (block > 32 && blocks(count, block) < 2 * sms) block /= 2;
-    return block;
+    return denseSpan(count, block);
 }
 
-cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, uint32_t count,
-                          bool limitOnly, uint32_t block, const StretchLengths& lens) {
-    block = elasticBlock(count, block, c.sms);
+cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, const Span& n) {
+    return launch(c, predictKernel, n.grid, n.block, s.fp, n.work, s.active, s.activeBody,
+                  (const uint32_t*)s.bodyActive, s.pos, s.prev, s.vel);
+}
+
+cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drivenCount) {
+    return launch(c, driveKernel, blocks(drivenCount, 256), 256, s.fp, s.driven, s.drivenOffset,
+                  (const uint32_t*)s.bodyActive, (const float4*)s.grabs, s.pos, s.prev, s.vel);
+}
+
+cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, const Span& sp,
+                          bool limitOnly, const StretchLengths& lens) {
     if (limitOnly)
-        return launch(c, elasticKernel<true>, blocks(count, block), block, cells, count, s.bodies, s.pos,
-                      (const float4*)s.prev, lens);
-    return launch(c, elasticKernel<false>, blocks(count, block), block, cells, count, s.bodies, s.pos,
-                  (const float4*)s.prev, lens);
+        return launch(c, elasticKernel<true>, sp.grid, sp.block, cells, sp.work, s.bodies,
+                      (const uint32_t*)s.bodyActive, s.pos, (const float4*)s.prev, lens);
+    return launch(c, elasticKernel<false>, sp.grid, sp.block, cells, sp.work, s.bodies,
+                  (const uint32_t*)s.bodyActive, s.pos, (const float4*)s.prev, lens);
 }
 
-cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, uint32_t activeCount, bool contact,
-                           bool predictNext) {
+cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span& n, bool contact, bool predictNext) {
     auto go = [&](auto kernel) {
-        return launch(c, kernel, blocks(activeCount, 256), 256, s.fp, s.active, s.activeBody, s.bodies, s.pos, s.prev,
+        return launch(c, kernel, n.grid, n.block, s.fp, n.work, s.active, s.activeBody, s.bodies, s.pos, s.prev,
                       s.vel, (const int32_t*)s.nodeRecord, (const float4*)s.delta, (const uint32_t*)s.key, s.count,
-                      s.cursor);
+                      s.cursor, (const uint32_t*)s.bodyActive);
     };
     if (contact) return predictNext ? go(finalizeKernel<true, true>) : go(finalizeKernel<true, false>);
     return predictNext ? go(finalizeKernel<false, true>) : go(finalizeKernel<false, false>);
@@ -693,34 +728,37 @@ cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, uint32_t ac
 // Solve mode leaves the corrections in `delta` for the closing pass, which
 // applies them and empties the grid; Pairs mode lists the hits and empties
 // the grid itself.
-cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, uint32_t surfaceCount, ContactMode mode,
+cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& r, ContactMode mode,
                           uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount) {
-    const uint32_t g = blocks(surfaceCount, 256);
+    const uint32_t g = r.grid, b = r.block;
+    const Work w = r.work;
     cudaError_t e;
-    if ((e = launch(c, binKernel, g, 256, s.fp, s.surf, (const float4*)s.pos, s.key, s.rank, s.count))) return e;
-    if ((e = launch(c, allocKernel, g, 256, s.fp, (const uint32_t*)s.key, (const uint32_t*)s.rank,
+    if ((e = launch(c, binKernel, g, b, s.fp, w, s.surf, (const DevBody*)s.bodies, (const uint32_t*)s.bodyActive,
+                    (const float4*)s.pos, s.key, s.rank, s.count)))
+        return e;
+    if ((e = launch(c, allocKernel, g, b, s.fp, w, (const uint32_t*)s.key, (const uint32_t*)s.rank,
                     (const uint32_t*)s.count, s.start, s.cursor)))
         return e;
-    if ((e = launch(c, scatterKernel, g, 256, s.fp, (const uint32_t*)s.key, (const uint32_t*)s.rank,
+    if ((e = launch(c, scatterKernel, g, b, s.fp, w, (const uint32_t*)s.key, (const uint32_t*)s.rank,
                     (const uint32_t*)s.start, s.entries)))
         return e;
-    if ((e = launch(c, canonKernel, g, 256, s.fp, (const uint32_t*)s.key, (const uint32_t*)s.rank,
+    if ((e = launch(c, canonKernel, g, b, s.fp, w, (const uint32_t*)s.key, (const uint32_t*)s.rank,
                     (const uint32_t*)s.start, (const uint32_t*)s.count, s.entries, (const uint4*)s.surf,
                     (const float4*)s.pos, s.sMeta, s.sPos, s.sRec)))
         return e;
     if (mode == ContactMode::Pairs) {
-        if ((e = launch(c, collideKernel<true>, g, 256, s.fp, s.surf, s.bodies, (const float4*)s.pos,
-                        (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count,
+        if ((e = launch(c, collideKernel<true>, g, b, s.fp, w, s.surf, s.bodies, (const uint32_t*)s.bodyActive,
+                        (const float4*)s.pos, (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count,
                         (const uint4*)s.sMeta, (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, pairs,
                         capacity, pairCount)))
             return e;
-        return launch(c, settleKernel, g, 256, s.fp, s.surf, (const uint32_t*)s.key, (const float4*)s.delta, s.pos,
+        return launch(c, settleKernel, g, b, s.fp, w, s.surf, (const uint32_t*)s.key, (const float4*)s.delta, s.pos,
                       s.count, s.cursor, 0);
     }
-    return launch(c, collideKernel<false>, g, 256, s.fp, s.surf, s.bodies, (const float4*)s.pos,
-                  (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count, (const uint4*)s.sMeta,
-                  (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, (uint32_t*)nullptr, 0u,
-                  (unsigned long long*)nullptr);
+    return launch(c, collideKernel<false>, g, b, s.fp, w, s.surf, s.bodies, (const uint32_t*)s.bodyActive,
+                  (const float4*)s.pos, (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count,
+                  (const uint4*)s.sMeta, (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, (uint32_t*)nullptr,
+                  0u, (unsigned long long*)nullptr);
 }
 
 cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos) {

@@ -101,8 +101,14 @@ struct DevBody {
     float friction;
     float damp;       // exp(-damping dt), finalize.wgsl:72
     float pad1, pad2, pad3;
+    // The contact grid this body bins into (contacts.wgsl:84-91): shared by
+    // every body of a scene, or the body's own when bodies must never meet.
+    float gridOrigin[3];
+    float bucket;
+    uint32_t gridDims[3];
+    uint32_t gridBase;  // index of the grid's first bucket in the bucket arrays
 };
-static_assert(sizeof(DevBody) == 64, "DevBody is one 64-byte record");
+static_assert(sizeof(DevBody) == 96, "DevBody is one 96-byte record");
 
 // Scalars every substep kernel reads, refreshed by one small copy per frame.
 struct FrameParams {
@@ -116,13 +122,10 @@ struct FrameParams {
     uint32_t drivenCount;
     float grabVelocity[3];
     uint32_t law;
-    float gridOrigin[3];
-    float bucket;
-    uint32_t gridDims[3];
     uint32_t surfaceCount;
     uint32_t selfContact;
     uint32_t activeCount;
-    uint32_t pad[2];
+    uint32_t perBodyGrab;  // drive targets come from the per-body table, not grabTarget
 };
 
 }  // namespace vsim

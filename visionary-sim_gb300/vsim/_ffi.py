@@ -109,6 +109,29 @@ class ClockReport(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_double), ("step_duration", C.c_double), ("substeps", C.c_uint32),
+                ("self_contact", C.c_int32)]
+
+
+class Drag(C.Structure):
+    _fields_ = [("node", C.c_uint32), ("control", (C.c_float * 3) * 4), ("speed", C.c_double)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("request", C.c_uint64), ("session", C.c_uint32), ("frames", C.c_uint32),
+                ("submitted", C.c_double), ("completed", C.c_double), ("first_tick", C.c_uint64),
+                ("last_tick", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("sessions", C.c_uint32), ("rejected", C.c_uint32), ("resident_bytes", C.c_double),
+                ("ticks", C.c_uint64), ("session_frames", C.c_uint64), ("cell_updates", C.c_uint64),
+                ("pending", C.c_uint32)]
+
+
+VSIM_CREATE_ISOLATED = 1
+
 _P = C.c_void_p
 _F = C.POINTER(C.c_float)
 _D = C.POINTER(C.c_double)
@@ -120,6 +143,19 @@ SIGNATURES = {
     "vsim_abi_version": (C.c_int, []),
     "vsim_create": (C.c_int, [C.POINTER(BodyDesc), C.c_uint32, C.POINTER(Tank), _P, C.POINTER(_P)]),
     "vsim_destroy": (C.c_int, [_P]),
+    "vsim_create_ex": (C.c_int, [C.POINTER(BodyDesc), C.c_uint32, C.POINTER(Tank), _P, C.c_uint32, C.POINTER(_P)]),
+    "vsim_set_bodies_active": (C.c_int, [_P, C.POINTER(C.c_uint8), C.c_uint32]),
+    "vsim_server_create": (C.c_int, [C.POINTER(BodyDesc), C.c_uint32, C.POINTER(Tank), C.POINTER(ServerConfig), _P,
+                                     C.POINTER(_P)]),
+    "vsim_server_destroy": (C.c_int, [_P]),
+    "vsim_server_admitted": (C.c_uint32, [_P]),
+    "vsim_server_clock": (C.c_double, [_P]),
+    "vsim_server_submit": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(Drag), C.POINTER(C.c_uint64)]),
+    "vsim_server_tick": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
+    "vsim_server_poll": (C.c_int, [_P, C.POINTER(Completion), C.c_uint32, C.POINTER(C.c_uint32)]),
+    "vsim_server_get_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "vsim_server_node_count": (C.c_uint32, [_P, C.c_uint32]),
+    "vsim_server_read_positions": (C.c_int, [_P, C.c_uint32, _F, _SZ]),
     "vsim_step": (C.c_int, [_P, C.c_double]),
     "vsim_request_step": (C.c_int, [_P]),
     "vsim_dispatch": (C.c_int, [_P, C.c_uint32]),

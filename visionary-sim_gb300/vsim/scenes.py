@@ -64,6 +64,7 @@ class Scene:
     iterations: int = 1
     contact: bool = True
     self_contact: bool = False
+    isolated: bool = False  # bodies never touch each other (own contact grids)
     splats: dict = field(default_factory=dict)  # body -> (means, quats, scales, opacity, rgb)
 
     @property
@@ -244,6 +245,49 @@ def box_batch(count: int = 256, seed: int = 2, splats_per_body: int = 0, spacing
         if splats_per_body:
             scene.splats[b] = splats_in(body, splats_per_body, seed * 100003 + b)
     return scene
+
+
+def surface_nodes(body: Body) -> np.ndarray:
+    """Body-local boundary nodes: some but not all of the eight incident
+    cells occupied (lattice.js:128-158)."""
+    cx, cy, cz = body.cell_dims
+    occ = np.zeros((cz + 2, cy + 2, cx + 2), np.int32)
+    occ[1:-1, 1:-1, 1:-1] = body.occupancy.reshape(cz, cy, cx)
+    filled = (occ[:-1, :-1, :-1] + occ[:-1, :-1, 1:] + occ[:-1, 1:, :-1] + occ[:-1, 1:, 1:] +
+              occ[1:, :-1, :-1] + occ[1:, :-1, 1:] + occ[1:, 1:, :-1] + occ[1:, 1:, 1:])
+    return np.flatnonzero((filled > 0) & (filled < 8)).astype(np.uint32)
+
+
+def session_pool(count: int = 1000, seed: int = 3, min_n: int = 8, max_n: int = 64):
+    """Serving sessions: seeded noise blobs on n^3 grids, n log-uniform in
+    [min_n, max_n], materials as the single large body's (E log-uniform
+    1e4-1e6, nu 0.45, rho 1000), each resting above the ground at the
+    origin. Returns (bodies, tank)."""
+    rng = np.random.default_rng(seed)
+    bodies = []
+    for s in range(count):
+        n = int(round(float(log_uniform(rng, min_n, max_n))))
+        occ = noise_occupancy(n, seed * 1_000_003 + s)
+        mat = dict(DEFAULT_MATERIAL, youngs_modulus=float(log_uniform(rng, 1e4, 1e6)), poisson_ratio=0.45,
+                   density=1000.0)
+        half = n * H / 2
+        bodies.append(Body((n, n, n), (-half, 2 * H, -half), H, occ, mat))
+    extent = max_n * H
+    tank = ((-extent, 0.0, -extent), (extent, 2 * extent, extent))
+    return bodies, tank
+
+
+def drag_request(body: Body, rng, speed: float = 0.5):
+    """A drag: a random surface node of `body` pulled along a seeded cubic
+    Bezier starting at the node's rest position, at `speed` m/s."""
+    nodes = surface_nodes(body)
+    node = int(nodes[rng.integers(0, nodes.size)])
+    nx, ny, _ = body.node_dims
+    ijk = np.array([node % nx, (node // nx) % ny, node // (nx * ny)], float)
+    p0 = np.asarray(body.origin) + ijk * body.h
+    steps = rng.normal(scale=0.05, size=(3, 3))
+    control = np.vstack([p0, p0 + steps[0], p0 + steps[0] + steps[1], p0 + steps.sum(axis=0)])
+    return node, control.astype(np.float32), speed
 
 
 def blob_and_sheet(n: int = 192, seed: int = 4, splats: int = 20_000_000) -> Scene:

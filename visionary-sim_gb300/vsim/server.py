@@ -1,0 +1,86 @@
+"""Python surface of libvsim's session server (vsim_server_* in
+include/vsim.h): a pool of sessions resident on the device, stepped in
+shared frames with requests joining at every frame boundary."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import check, fptr, lib
+from .scenes import Descs, Scene
+
+
+class Server:
+    def __init__(self, bodies, tank, budget_bytes: float = 150e9, step_duration: float = 1 / 600,
+                 substeps: int = 10, self_contact: bool = True, stream=None):
+        self._descs = Descs(Scene(list(bodies), tank))
+        cfg = _ffi.ServerConfig(float(budget_bytes), float(step_duration), int(substeps), int(bool(self_contact)))
+        handle = C.c_void_p()
+        check(lib().vsim_server_create(self._descs.bodies, self._descs.count, C.byref(self._descs.tank),
+                                       C.byref(cfg), C.c_void_p(stream), C.byref(handle)))
+        self._h = handle
+        self.bodies = list(bodies)
+        self.admitted = int(lib().vsim_server_admitted(handle))
+        self._buf = (_ffi.Completion * 4096)()
+
+    def destroy(self):
+        if self._h:
+            lib().vsim_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def clock(self) -> float:
+        return float(lib().vsim_server_clock(self._h))
+
+    def submit(self, session: int, frames: int, drag=None) -> int:
+        """Queue `frames` frames for `session`; drag = (node, control 4x3, speed)."""
+        rid = C.c_uint64()
+        d = None
+        if drag is not None:
+            node, control, speed = drag
+            d = _ffi.Drag()
+            d.node = int(node)
+            ctl = np.asarray(control, np.float32).reshape(4, 3)
+            for i in range(4):
+                for a in range(3):
+                    d.control[i][a] = float(ctl[i, a])
+            d.speed = float(speed)
+        check(lib().vsim_server_submit(self._h, int(session), int(frames), C.byref(d) if d is not None else None,
+                                       C.byref(rid)))
+        return int(rid.value)
+
+    def tick(self) -> int:
+        stepped = C.c_uint32()
+        check(lib().vsim_server_tick(self._h, C.byref(stepped)))
+        return int(stepped.value)
+
+    def poll(self) -> list:
+        out = []
+        while True:
+            n = C.c_uint32()
+            check(lib().vsim_server_poll(self._h, self._buf, len(self._buf), C.byref(n)))
+            for i in range(n.value):
+                c = self._buf[i]
+                out.append({"request": c.request, "session": c.session, "frames": c.frames,
+                            "submitted": c.submitted, "completed": c.completed, "first_tick": c.first_tick,
+                            "last_tick": c.last_tick})
+            if n.value < len(self._buf):
+                return out
+
+    def stats(self) -> dict:
+        s = _ffi.ServerStats()
+        check(lib().vsim_server_get_stats(self._h, C.byref(s)))
+        return {name: getattr(s, name) for name, _ in s._fields_}
+
+    def read_positions(self, session: int) -> np.ndarray:
+        n = int(lib().vsim_server_node_count(self._h, int(session)))
+        out = np.zeros((n, 4), np.float32)
+        check(lib().vsim_server_read_positions(self._h, int(session), fptr(out), n))
+        return out

@@ -83,8 +83,9 @@ class Simulator:
     def __init__(self, scene: Scene, stream=None):
         self._descs = Descs(scene)
         handle = C.c_void_p()
-        check(lib().vsim_create(self._descs.bodies, self._descs.count, C.byref(self._descs.tank),
-                                C.c_void_p(stream), C.byref(handle)))
+        flags = _ffi.VSIM_CREATE_ISOLATED if scene.isolated else 0
+        check(lib().vsim_create_ex(self._descs.bodies, self._descs.count, C.byref(self._descs.tank),
+                                   C.c_void_p(stream), flags, C.byref(handle)))
         self._h = handle
         self.scene = scene
         self.node_count = int(lib().vsim_node_count(handle))
@@ -215,6 +216,14 @@ class Simulator:
             fields |= bits[k]
         check(lib().vsim_set_material(self._h, int(body), C.byref(m), fields))
         check(lib().vsim_read_inv_mass(self._h, fptr(self.inv_mass), self.node_count))
+
+    def set_bodies_active(self, active):
+        """Which bodies take part in the following frames (None: all)."""
+        if active is None:
+            check(lib().vsim_set_bodies_active(self._h, None, len(self.scene.bodies)))
+            return
+        flags = np.ascontiguousarray(np.asarray(active, bool), np.uint8)
+        check(lib().vsim_set_bodies_active(self._h, flags.ctypes.data_as(C.POINTER(C.c_uint8)), int(flags.size)))
 
     def set_contact(self, enabled: bool):
         check(lib().vsim_set_contact(self._h, int(bool(enabled))))

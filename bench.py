@@ -33,6 +33,7 @@ import re
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -75,7 +76,7 @@ class ClockSampler:
     def __init__(self, device_index: int):
         self.device = device_index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"vsim_clocks_{os.getpid()}.csv"
 
     def __enter__(self):
         try:
@@ -296,6 +297,79 @@ def batched_vs_plain(frames: int, quick: bool):
     return out
 
 
+def stress(quick: bool, hbm: float, frames: int = 3):
+    """The stress workload: a 192^3 noise blob with a 192 x 192 x 2 sheet above it
+    (E 5e5, nu 0.48), ground, self and body contact, 20 substeps of 2
+    Gauss-Seidel sweeps per frame, 20M splats deformed and depth-sorted."""
+    import torch
+
+    import vsim.scenes as sc
+    from vsim import Simulator
+
+    t0 = time.perf_counter()
+    scene = sc.blob_and_sheet(n=48 if quick else 192, seed=4, splats=200_000 if quick else 20_000_000)
+    gen_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    sim = Simulator(scene, stream=stream.cuda_stream)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    run_frame(sim, scene)
+    sim.synchronize()
+    times = time_frames(sim, scene, stream, frames, flush)
+    prof = sim.profile_frame(scene.substeps, splats=True, view_dir=VIEW)
+    ms, launches = prof["elastic"]
+    cells = int(sim.color_counts().sum()) * scene.iterations * scene.substeps
+    per_launch = cells * BYTES_PER_ELASTIC_CELL / launches
+    achieved = per_launch / (ms / 1e3 / launches) / 1e9
+    n_splats = sim.splat_count
+    sort_ms, sort_launches = prof.get("sort", (0.0, 0))
+    splat_ms, _ = prof.get("splat", (0.0, 0))
+    out = {"workload": f"blob {scene.bodies[0].cell_dims[0]}^3 + sheet, {scene.cells} cells, "
+                       f"{sim.node_count} node slots, {scene.substeps} substeps x {scene.iterations} sweeps, "
+                       f"{n_splats} splats",
+           "value": round(units_per_frame(scene) * frames / sum(times)), "unit": METRIC,
+           "frame_ms": round(1e3 * statistics.median(times), 3),
+           "elastic_pass": {"achieved_gbs": round(achieved, 1), "frac_of_measured_hbm": round(achieved / hbm, 4),
+                            "bytes_per_launch": round(per_launch), "avg_launch_us": round(1e3 * ms / launches, 2)},
+           "splat_deform_gbs": round(92 * n_splats / (splat_ms / 1e3) / 1e9, 1) if splat_ms else None,
+           "sort_keys_per_s": round(n_splats / (sort_ms / 1e3)) if sort_ms else None,
+           "kernel_groups_one_frame": {k: {"ms": round(v[0], 3), "launches": v[1]} for k, v in prof.items()},
+           "scene_generation_s": round(gen_s, 1)}
+    sim.destroy()
+    del flush
+    return out
+
+
+def drift(frames: int = 300):
+    """The 16 x 4 x 4 bar for `frames` frames on the GPU against the oracle
+    in double precision from the same start: the float trajectory's
+    departure from the exact arithmetic (reported, not gated; the configs'
+    CFL numbers are above 1, so trajectories are sensitive)."""
+    import pyoracle
+    import vsim.scenes as sc
+    from vsim import Simulator
+
+    scene = sc.single_box()
+    sim = Simulator(scene)
+    ref = pyoracle.Oracle(scene, 64)
+    diag = float(np.linalg.norm(np.asarray(scene.bodies[0].cell_dims) * scene.bodies[0].h))
+    worst, at = 0.0, 0
+    for f in range(frames):
+        sim.dispatch(scene.substeps)
+        ref.dispatch(scene.substeps)
+        if f % 10 == 9 or f == frames - 1:
+            g = sim.read_positions()[:, :3].astype(np.float64)
+            r = ref.state_f64()[0][:, :3]
+            err = float(np.max(np.abs(g - r))) / max(float(np.max(np.abs(r))), diag)
+            if err > worst:
+                worst, at = err, f + 1
+    g = sim.read_positions()[:, :3].astype(np.float64)
+    r = ref.state_f64()[0][:, :3]
+    sim.destroy()
+    return {"workload": "16x4x4 bar, pinned end, 10 substeps/frame", "frames": frames,
+            "max_relative_error": worst, "at_frame": at,
+            "final_max_abs_m": float(np.max(np.abs(g - r)))}
+
+
 def serving_sweep(quick: bool, seconds_per_point: float = 3.0):
     """Continuous batching under load: a pool of sessions resident on the
     GPU; requests advance a session k ~ U{1..4} frames, half of them dragging
@@ -407,6 +481,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-stress", action="store_true")
+    ap.add_argument("--stress-only", action="store_true", help="only the stress workload's frames (for captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -443,6 +519,9 @@ def main():
     from vsim import Simulator
 
     torch.cuda.set_device(local)
+    if args.stress_only:
+        print(json.dumps({"stress": stress(args.quick, peaks()[0], frames=args.steps)}))
+        return
     if world > 1:
         import torch.distributed as dist
 
@@ -481,6 +560,10 @@ def main():
         detail["batching"] = batched_vs_plain(3, args.quick)
     if rank == 0 and not args.no_serve:
         detail["serving"] = serving_sweep(args.quick)
+    if rank == 0 and not args.no_stress:
+        detail["stress"] = stress(args.quick, hbm)
+    if rank == 0:
+        detail["drift_vs_fp64"] = drift(30 if args.quick else 300)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(scene)

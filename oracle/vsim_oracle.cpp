@@ -4,8 +4,15 @@
 // Each function follows one reference file, cited beside it, operation by
 // operation and in the same evaluation order (left to right, WGSL's order for
 // vector and matrix products), so that a float build of this file and a GPU
-// kernel written to the same order agree bit for bit. Build with
-// -ffp-contract=off: a fused multiply-add would change the rounding.
+// kernel written to the same order agree bit for bit.
+//
+// Rounding: WGSL leaves contraction to the shader compiler, so the
+// reference's own rounding differs from GPU to GPU. This restatement fixes
+// one evaluation: a multiply followed by an add is fused (std::fma, one
+// rounding) exactly where written below -- in dot products, matrix-vector
+// products, cross products, the determinant, the Gram sums, the XPBD block
+// and the position updates -- and every other operation rounds on its own.
+// Build with -ffp-contract=off so the compiler fuses nothing else.
 //
 // Paths are relative to the reference project root.
 #include "vsim_oracle.h"
@@ -38,11 +45,15 @@ template <class T> inline V3<T> operator-(V3<T> a) { return {-a.x, -a.y, -a.z}; 
 template <class T> inline V3<T> operator*(V3<T> a, T s) { return {a.x * s, a.y * s, a.z * s}; }
 template <class T> inline V3<T> operator*(T s, V3<T> a) { return {s * a.x, s * a.y, s * a.z}; }
 template <class T> inline V3<T> operator/(V3<T> a, T s) { return {a.x / s, a.y / s, a.z / s}; }
-// WGSL dot: (x + y) + z.
-template <class T> inline T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// a * s + acc, fused per component.
+template <class T> inline V3<T> fma3(V3<T> a, T s, V3<T> acc) {
+    return {std::fma(a.x, s, acc.x), std::fma(a.y, s, acc.y), std::fma(a.z, s, acc.z)};
+}
+// dot: x first, then y and z fused in.
+template <class T> inline T dot(V3<T> a, V3<T> b) { return std::fma(a.z, b.z, std::fma(a.y, b.y, a.x * b.x)); }
 template <class T> inline T length(V3<T> a) { return std::sqrt(dot(a, a)); }
 template <class T> inline V3<T> cross(V3<T> a, V3<T> b) {
-    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return {std::fma(a.y, b.z, -(a.z * b.y)), std::fma(a.z, b.x, -(a.x * b.z)), std::fma(a.x, b.y, -(a.y * b.x))};
 }
 
 // Column-major 3x3, c[k] is column k (WGSL mat3x3f).
@@ -52,8 +63,8 @@ struct M3 {
 };
 
 template <class T> inline M3<T> operator*(M3<T> m, T s) { return {{m.c[0] * s, m.c[1] * s, m.c[2] * s}}; }
-// M * v = c0 v.x + c1 v.y + c2 v.z, summed left to right.
-template <class T> inline V3<T> mul(M3<T> m, V3<T> v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z; }
+// M * v = c0 v.x + c1 v.y + c2 v.z, summed left to right, fused.
+template <class T> inline V3<T> mul(M3<T> m, V3<T> v) { return fma3(m.c[2], v.z, fma3(m.c[1], v.y, m.c[0] * v.x)); }
 template <class T> inline M3<T> mul(M3<T> a, M3<T> b) { return {{mul(a, b.c[0]), mul(a, b.c[1]), mul(a, b.c[2])}}; }
 template <class T> inline M3<T> transpose(M3<T> m) {
     return {{v3(m.c[0].x, m.c[1].x, m.c[2].x), v3(m.c[0].y, m.c[1].y, m.c[2].y),
@@ -64,7 +75,10 @@ template <class T> inline T determinant(M3<T> m) {
     const T m0 = m.c[0].x, m1 = m.c[0].y, m2 = m.c[0].z;
     const T m3 = m.c[1].x, m4 = m.c[1].y, m5 = m.c[1].z;
     const T m6 = m.c[2].x, m7 = m.c[2].y, m8 = m.c[2].z;
-    return m0 * (m4 * m8 - m7 * m5) - m3 * (m1 * m8 - m7 * m2) + m6 * (m1 * m5 - m4 * m2);
+    const T t1 = std::fma(m4, m8, -(m7 * m5));
+    const T t2 = std::fma(m1, m8, -(m7 * m2));
+    const T t3 = std::fma(m1, m5, -(m4 * m2));
+    return std::fma(m6, t3, std::fma(m0, t1, -(m3 * t2)));
 }
 
 // ------------------------------------------------------------ constants --
@@ -448,19 +462,31 @@ void drive(Sim<T>& s, T dt) {
 template <class T>
 inline void xpbdCouple(T cx, T cy, T ax, T ay, T relax, T rx, T ry, T gx, T gy, T gz, T& lx, T& ly) {
     const T stiffened = T(1) + relax;
-    const T a00 = gx * stiffened + ax;
+    const T a00 = std::fma(gx, stiffened, ax);
     const T a01 = gy * stiffened;
-    const T a11 = gz * stiffened + ay;
-    const T det = a00 * a11 - a01 * a01;
+    const T a11 = std::fma(gz, stiffened, ay);
+    const T det = std::fma(a00, a11, -(a01 * a01));
     if (det < T(1e-20)) {
         lx = T(0);
         ly = T(0);
         return;
     }
-    const T bx = -(cx + rx * relax);
-    const T by = -(cy + ry * relax);
-    lx = (a11 * bx - a01 * by) / det;
-    ly = (a00 * by - a01 * bx) / det;
+    const T bx = -std::fma(rx, relax, cx);
+    const T by = -std::fma(ry, relax, cy);
+    lx = std::fma(a11, bx, -(a01 * by)) / det;
+    ly = std::fma(a00, by, -(a01 * bx)) / det;
+}
+
+// sum_i w_i dot(a_i, b_i) over a tetrahedron's four nodes, fused.
+template <class T>
+inline T weighted4(T w0, T w1, T w2, T w3, T e0, T e1, T e2, T e3) {
+    return std::fma(w3, e3, std::fma(w2, e2, std::fma(w1, e1, w0 * e0)));
+}
+
+// p + (d lx + h ly) w, fused.
+template <class T>
+inline V3<T> moved(V3<T> p, V3<T> d, V3<T> h, T lx, T ly, T w) {
+    return fma3(fma3(h, ly, d * lx), w, p);
 }
 
 // project.wgsl:90-152: one Kuhn tetrahedron of a cell, in place.
@@ -483,9 +509,9 @@ inline void projectTet(V3<T>* p, const V3<T>* prev, const T* w, const uint32_t t
     const V3<T> d0 = -(d1 + d2 + d3);
     const V3<T> h1 = mHyd.c[0], h2 = mHyd.c[1], h3 = mHyd.c[2];
     const V3<T> h0 = -(h1 + h2 + h3);
-    const T gx = w0 * dot(d0, d0) + w1 * dot(d1, d1) + w2 * dot(d2, d2) + w3 * dot(d3, d3);
-    const T gy = w0 * dot(d0, h0) + w1 * dot(d1, h1) + w2 * dot(d2, h2) + w3 * dot(d3, h3);
-    const T gz = w0 * dot(h0, h0) + w1 * dot(h1, h1) + w2 * dot(h2, h2) + w3 * dot(h3, h3);
+    const T gx = weighted4(w0, w1, w2, w3, dot(d0, d0), dot(d1, d1), dot(d2, d2), dot(d3, d3));
+    const T gy = weighted4(w0, w1, w2, w3, dot(d0, h0), dot(d1, h1), dot(d2, h2), dot(d3, h3));
+    const T gz = weighted4(w0, w1, w2, w3, dot(h0, h0), dot(h1, h1), dot(h2, h2), dot(h3, h3));
     const V3<T> x0 = p[i0] - prev[i0];
     const V3<T> x1 = p[i1] - prev[i1];
     const V3<T> x2 = p[i2] - prev[i2];
@@ -494,10 +520,10 @@ inline void projectTet(V3<T>* p, const V3<T>* prev, const T* w, const uint32_t t
     const T ry = dot(h0, x0) + dot(h1, x1) + dot(h2, x2) + dot(h3, x3);
     T lx, ly;
     xpbdCouple(cDev, cHyd, alphaDev, alphaHyd, relax, rx, ry, gx, gy, gz, lx, ly);
-    p[i0] = p[i0] + (d0 * lx + h0 * ly) * w0;
-    p[i1] = p[i1] + (d1 * lx + h1 * ly) * w1;
-    p[i2] = p[i2] + (d2 * lx + h2 * ly) * w2;
-    p[i3] = p[i3] + (d3 * lx + h3 * ly) * w3;
+    p[i0] = moved(p[i0], d0, h0, lx, ly, w0);
+    p[i1] = moved(p[i1], d1, h1, lx, ly, w1);
+    p[i2] = moved(p[i2], d2, h2, lx, ly, w2);
+    p[i3] = moved(p[i3], d3, h3, lx, ly, w3);
 }
 
 template <class T>

@@ -61,13 +61,14 @@ __global__ void __launch_bounds__(256) splatDeformKernel(const float4* __restric
     const V a0 = mul(F, r0) * sb.x;
     const V a1 = mul(F, r1) * sb.y;
     const V a2 = mul(F, r2) * sb.z;
-    // (A A^T)(row, col) = a0[row] a0[col] + a1[row] a1[col] + a2[row] a2[col].
-    const float xx = a0.x * a0.x + a1.x * a1.x + a2.x * a2.x;
-    const float xy = a0.y * a0.x + a1.y * a1.x + a2.y * a2.x;
-    const float xz = a0.z * a0.x + a1.z * a1.x + a2.z * a2.x;
-    const float yy = a0.y * a0.y + a1.y * a1.y + a2.y * a2.y;
-    const float yz = a0.z * a0.y + a1.z * a1.y + a2.z * a2.y;
-    const float zz = a0.z * a0.z + a1.z * a1.z + a2.z * a2.z;
+    // (A A^T)(row, col) = a0[row] a0[col] + a1[row] a1[col] + a2[row] a2[col],
+    // column col of A times row col of A^T, fused as M * v is.
+    const float xx = fmaf(a2.x, a2.x, fmaf(a1.x, a1.x, a0.x * a0.x));
+    const float xy = fmaf(a2.y, a2.x, fmaf(a1.y, a1.x, a0.y * a0.x));
+    const float xz = fmaf(a2.z, a2.x, fmaf(a1.z, a1.x, a0.z * a0.x));
+    const float yy = fmaf(a2.y, a2.y, fmaf(a1.y, a1.y, a0.y * a0.y));
+    const float yz = fmaf(a2.z, a2.y, fmaf(a1.z, a1.y, a0.z * a0.y));
+    const float zz = fmaf(a2.z, a2.z, fmaf(a1.z, a1.z, a0.z * a0.z));
     const float depth = position.x * vx + position.y * vy + position.z * vz;
     meanDepth[i] = make_float4(position.x, position.y, position.z, depth);
     cov[3 * i] = make_float2(xx, xy);

@@ -52,10 +52,10 @@ void kuhnTable(float out[54]) {
 }
 
 // a0 k0 s + a1 k1 s + a2 k2 s for constant k in {-1, 0, 1}, summed left to
-// right with the zero terms left out. The reference multiplies by the full
-// matrix B = K s; a product with an exact zero is a signed zero and adding it
-// changes nothing but the sign of an exact-zero sum, so this is the same
-// value with a third of the arithmetic.
+// right as M * v is (the first product rounded, the next ones fused in),
+// with the zero terms left out. A product with an exact zero is a signed
+// zero, and fusing it in changes nothing but the sign of an exact-zero sum,
+// so this is the full product's value with a third of the arithmetic.
 template <int K>
 __device__ __forceinline__ float kscale(float s, float ns) {
     return K > 0 ? s : ns;
@@ -65,12 +65,12 @@ template <int K0, int K1, int K2>
 __device__ __forceinline__ V sparse3(V a0, V a1, V a2, float s, float ns) {
     if constexpr (K0 != 0) {
         V acc = a0 * kscale<K0>(s, ns);
-        if constexpr (K1 != 0) acc = acc + a1 * kscale<K1>(s, ns);
-        if constexpr (K2 != 0) acc = acc + a2 * kscale<K2>(s, ns);
+        if constexpr (K1 != 0) acc = fma3(a1, kscale<K1>(s, ns), acc);
+        if constexpr (K2 != 0) acc = fma3(a2, kscale<K2>(s, ns), acc);
         return acc;
     } else if constexpr (K1 != 0) {
         V acc = a1 * kscale<K1>(s, ns);
-        if constexpr (K2 != 0) acc = acc + a2 * kscale<K2>(s, ns);
+        if constexpr (K2 != 0) acc = fma3(a2, kscale<K2>(s, ns), acc);
         return acc;
     } else {
         return a2 * kscale<K2>(s, ns);
@@ -97,19 +97,30 @@ __device__ __forceinline__ M timesBt(const M& A, float s, float ns) {
 __device__ __forceinline__ void couple(float cx, float cy, float ax, float ay, float relax, float rx, float ry, float gx,
                                        float gy, float gz, float& lx, float& ly) {
     const float stiffened = 1.0f + relax;
-    const float a00 = gx * stiffened + ax;
+    const float a00 = fmaf(gx, stiffened, ax);
     const float a01 = gy * stiffened;
-    const float a11 = gz * stiffened + ay;
-    const float det = a00 * a11 - a01 * a01;
+    const float a11 = fmaf(gz, stiffened, ay);
+    const float det = fmaf(a00, a11, -(a01 * a01));
     if (det < 1e-20f) {
         lx = 0.0f;
         ly = 0.0f;
         return;
     }
-    const float bx = -(cx + rx * relax);
-    const float by = -(cy + ry * relax);
-    lx = (a11 * bx - a01 * by) / det;
-    ly = (a00 * by - a01 * bx) / det;
+    const float bx = -fmaf(rx, relax, cx);
+    const float by = -fmaf(ry, relax, cy);
+    lx = fmaf(a11, bx, -(a01 * by)) / det;
+    ly = fmaf(a00, by, -(a01 * bx)) / det;
+}
+
+// sum_i w_i e_i over a tetrahedron's four nodes, fused.
+__device__ __forceinline__ float weighted4(float w0, float w1, float w2, float w3, float e0, float e1, float e2,
+                                           float e3) {
+    return fmaf(w3, e3, fmaf(w2, e2, fmaf(w1, e1, w0 * e0)));
+}
+
+// p + (d lx + h ly) w, fused.
+__device__ __forceinline__ V moved(V p, V d, V h, float lx, float ly, float w) {
+    return fma3(fma3(h, ly, d * lx), w, p);
 }
 
 // project.wgsl:75-153, tetrahedron t of the cell held in registers.
@@ -130,9 +141,9 @@ __device__ __forceinline__ void projectTet(V (&p)[8], const V (&prev)[8], const 
     const V d0 = -(d1 + d2 + d3);
     const V h1 = mHyd.c[0], h2 = mHyd.c[1], h3 = mHyd.c[2];
     const V h0 = -(h1 + h2 + h3);
-    const float gx = w0 * dot(d0, d0) + w1 * dot(d1, d1) + w2 * dot(d2, d2) + w3 * dot(d3, d3);
-    const float gy = w0 * dot(d0, h0) + w1 * dot(d1, h1) + w2 * dot(d2, h2) + w3 * dot(d3, h3);
-    const float gz = w0 * dot(h0, h0) + w1 * dot(h1, h1) + w2 * dot(h2, h2) + w3 * dot(h3, h3);
+    const float gx = weighted4(w0, w1, w2, w3, dot(d0, d0), dot(d1, d1), dot(d2, d2), dot(d3, d3));
+    const float gy = weighted4(w0, w1, w2, w3, dot(d0, h0), dot(d1, h1), dot(d2, h2), dot(d3, h3));
+    const float gz = weighted4(w0, w1, w2, w3, dot(h0, h0), dot(h1, h1), dot(h2, h2), dot(h3, h3));
     const V x0 = p[i0] - prev[i0];
     const V x1 = p[i1] - prev[i1];
     const V x2 = p[i2] - prev[i2];
@@ -141,10 +152,10 @@ __device__ __forceinline__ void projectTet(V (&p)[8], const V (&prev)[8], const 
     const float ry = dot(h0, x0) + dot(h1, x1) + dot(h2, x2) + dot(h3, x3);
     float lx, ly;
     couple(cDev, cHyd, alphaDev, alphaHyd, relax, rx, ry, gx, gy, gz, lx, ly);
-    p[i0] = p[i0] + (d0 * lx + h0 * ly) * w0;
-    p[i1] = p[i1] + (d1 * lx + h1 * ly) * w1;
-    p[i2] = p[i2] + (d2 * lx + h2 * ly) * w2;
-    p[i3] = p[i3] + (d3 * lx + h3 * ly) * w3;
+    p[i0] = moved(p[i0], d0, h0, lx, ly, w0);
+    p[i1] = moved(p[i1], d1, h1, lx, ly, w1);
+    p[i2] = moved(p[i2], d2, h2, lx, ly, w2);
+    p[i3] = moved(p[i3], d3, h3, lx, ly, w3);
 }
 
 // ------------------------------------------------------------- kernels --

@@ -1,10 +1,13 @@
 // Device vector arithmetic in the reference's evaluation order (WGSL: left
 // to right, `dot` as (x + y) + z, `M * v` as c0 v.x + c1 v.y + c2 v.z).
 //
-// Every translation unit that includes this is compiled with -fmad=false,
-// so each multiply and each add rounds separately, exactly as the CPU
-// restatement of the reference does; together with IEEE division and square
-// root (nvcc's defaults) that makes the kernels' results equal to it.
+// Rounding is fixed, not left to the compiler: every translation unit that
+// includes this is compiled with -fmad=false, so a multiply and an add fuse
+// only where fmaf is written -- in dot, cross, M * v and the determinant
+// here, and at the named places of the solver kernels -- and everything else
+// rounds once per operation. The CPU restatement of the solver fuses at the
+// same places (std::fma); together with IEEE division and square root
+// (nvcc's defaults) the kernels' results equal it bit for bit.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -25,10 +28,15 @@ __device__ __forceinline__ V operator-(V a) { return V{-a.x, -a.y, -a.z}; }
 __device__ __forceinline__ V operator*(V a, float s) { return V{a.x * s, a.y * s, a.z * s}; }
 __device__ __forceinline__ V operator*(float s, V a) { return V{s * a.x, s * a.y, s * a.z}; }
 __device__ __forceinline__ V operator/(V a, float s) { return V{a.x / s, a.y / s, a.z / s}; }
-__device__ __forceinline__ float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// a * s + acc per component, one rounding each.
+__device__ __forceinline__ V fma3(V a, float s, V acc) {
+    return V{fmaf(a.x, s, acc.x), fmaf(a.y, s, acc.y), fmaf(a.z, s, acc.z)};
+}
+// x first, then y and z fused in.
+__device__ __forceinline__ float dot(V a, V b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
 __device__ __forceinline__ float length(V a) { return sqrtf(dot(a, a)); }
 __device__ __forceinline__ V cross(V a, V b) {
-    return V{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return V{fmaf(a.y, b.z, -(a.z * b.y)), fmaf(a.z, b.x, -(a.x * b.z)), fmaf(a.x, b.y, -(a.y * b.x))};
 }
 
 // Column-major 3x3: c[k] is column k.
@@ -37,13 +45,16 @@ struct M {
 };
 
 __device__ __forceinline__ M operator*(const M& m, float s) { return M{{m.c[0] * s, m.c[1] * s, m.c[2] * s}}; }
-__device__ __forceinline__ V mul(const M& m, V v) { return m.c[0] * v.x + m.c[1] * v.y + m.c[2] * v.z; }
+__device__ __forceinline__ V mul(const M& m, V v) { return fma3(m.c[2], v.z, fma3(m.c[1], v.y, m.c[0] * v.x)); }
 // Expansion order of the reference's mat3Determinant (mat3.js:25-31).
 __device__ __forceinline__ float determinant(const M& m) {
     const float m0 = m.c[0].x, m1 = m.c[0].y, m2 = m.c[0].z;
     const float m3 = m.c[1].x, m4 = m.c[1].y, m5 = m.c[1].z;
     const float m6 = m.c[2].x, m7 = m.c[2].y, m8 = m.c[2].z;
-    return m0 * (m4 * m8 - m7 * m5) - m3 * (m1 * m8 - m7 * m2) + m6 * (m1 * m5 - m4 * m2);
+    const float t1 = fmaf(m4, m8, -(m7 * m5));
+    const float t2 = fmaf(m1, m8, -(m7 * m2));
+    const float t3 = fmaf(m1, m5, -(m4 * m2));
+    return fmaf(m6, t3, fmaf(m0, t1, -(m3 * t2)));
 }
 
 __device__ __forceinline__ float4 withW(V p, float w) { return make_float4(p.x, p.y, p.z, w); }

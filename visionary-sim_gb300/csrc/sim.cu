@@ -189,6 +189,7 @@ void buildDensePlan(vsim_sim* s) {
     p.nodes = denseSpan(s->activeCount, 256);
     for (int c = 0; c < 8; c++) p.colour[c] = elasticSpan(s->colorStart[c + 1] - s->colorStart[c], s->block, s->sms);
     p.records = denseSpan(s->surfaceCount, 256);
+    p.recordCount = s->surfaceCount;
 }
 
 void useDensePlan(vsim_sim* s) { s->plan = s->dense; }
@@ -211,6 +212,7 @@ int planBodies(vsim_sim* s, const std::vector<uint32_t>& bodies) {
     bool ok = emit(s->nodeBodyStart, p.nodes);
     for (int c = 0; c < 8 && ok; c++) ok = emit(s->colourBodyStart[c], p.colour[c]);
     ok = ok && emit(s->recordBodyStart, p.records);
+    for (uint32_t b : bodies) p.recordCount += s->recordBodyStart[b + 1] - s->recordBodyStart[b];
     if (!ok) return fail(VSIM_ERR_CAPACITY, "chunk table too small");
     CK(cudaMemcpyAsync(s->chunkDev, s->chunkPinned, at * sizeof(uint2), cudaMemcpyHostToDevice, s->stream),
        "upload work chunks");
@@ -301,7 +303,7 @@ cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMod
                 }
         if (contact && plan.records.grid) {
             begin(VSIM_KIND_CONTACT, kContactKernels);
-            if ((e = launchContact(c, s->d, plan.records, mode, nullptr, 0, nullptr))) return e;
+            if ((e = launchContact(c, s->d, plan.records, plan.recordCount, mode, nullptr, 0, nullptr))) return e;
             end();
         }
         begin(VSIM_KIND_FINALIZE, 1);
@@ -1081,7 +1083,7 @@ int vsim_contact_pairs(vsim_sim* s, uint32_t* pairs, size_t capacity, size_t* co
     if (rc) return rc;
     CK(cudaMemsetAsync(s->pairCount, 0, sizeof(unsigned long long), s->stream), "count pairs");
     const LaunchCtx c{s->stream, false, s->sms};
-    CK(launchContact(c, s->d, s->dense.records, ContactMode::Pairs, s->pairs, uint32_t(capacity), s->pairCount),
+    CK(launchContact(c, s->d, s->dense.records, s->dense.recordCount, ContactMode::Pairs, s->pairs, uint32_t(capacity), s->pairCount),
        "list pairs");
     unsigned long long total = 0;
     CK(cudaMemcpyAsync(&total, s->pairCount, sizeof total, cudaMemcpyDeviceToHost, s->stream), "count pairs");

@@ -51,6 +51,7 @@ struct FramePlan {
     Span nodes{};
     Span colour[8]{};
     Span records{};
+    uint32_t recordCount = 0;  // surface records the spans cover
 };
 
 }  // namespace vsim

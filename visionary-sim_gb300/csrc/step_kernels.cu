@@ -531,90 +531,99 @@ __device__ __forceinline__ bool admitted(uint4 a, uint4 b, uint32_t selfContact)
 // the contiguous run canonKernel laid out. With EMIT, every counted hit
 // (r, other) is also appended to `pairs` (capacity-checked), for the
 // pair-set checks.
+//
+// Threads take the records in bucket order (`entries`, the counting sort's
+// output, `*cursor` entries long) rather than in record order: the records
+// of one bucket sit in neighbouring lanes and scan the same 27 neighbour
+// runs, so a warp's candidate loads coincide and its lanes run loops of the
+// same length. Each record's hits are still summed in the reference's
+// order (neighbour buckets dz, dy, dx; entries in bucket order), so the
+// result does not depend on which thread computes it.
 template <bool EMIT>
-__global__ void collideKernel(const FrameParams* __restrict__ fp, Work work, const uint4* __restrict__ surf,
-                              const DevBody* __restrict__ bodies, const uint32_t* __restrict__ bodyActive,
-                              const float4* __restrict__ pos,
-                              const float4* __restrict__ prevState, const uint32_t* __restrict__ start,
-                              const uint32_t* __restrict__ count, const uint4* __restrict__ sMeta,
-                              const float4* __restrict__ sPos, const uint32_t* __restrict__ sRec,
-                              float4* __restrict__ delta, uint32_t* __restrict__ pairs, uint32_t capacity,
-                              unsigned long long* __restrict__ pairCount) {
+__global__ void __launch_bounds__(256) collideKernel(
+    const FrameParams* __restrict__ fp, uint32_t items, const uint32_t* __restrict__ entries,
+    const uint32_t* __restrict__ cursor, const uint4* __restrict__ surf, const DevBody* __restrict__ bodies,
+    const float4* __restrict__ pos, const float4* __restrict__ prevState, const uint32_t* __restrict__ start,
+    const uint32_t* __restrict__ count, const uint4* __restrict__ sMeta, const float4* __restrict__ sPos,
+    const uint32_t* __restrict__ sRec, float4* __restrict__ delta, uint32_t* __restrict__ pairs, uint32_t capacity,
+    unsigned long long* __restrict__ pairCount) {
     pdlWait();
     pdlLaunchNext();
-    uint32_t r;
-    if (!workItem(work, r)) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= items || i >= *cursor) return;
+    const uint32_t r = entries[i];
     const uint4 me = surf[r];
     const DevBody* grid = bodies + me.y;
-    if (!bodyActive[me.y]) return;
     const uint32_t node = me.x;
     const float radius = __uint_as_float(me.w);
     const float4 P = pos[node];
     const float wi = P.w;
     const V pi = xyz(P);
     const V movedI = pi - xyz(prevState[node]);
-    const float frictionI = bodies[me.y].friction;
+    const float frictionI = grid->friction;
     const uint32_t selfContact = fp->selfContact;
-    V sum = mk(0.0f, 0.0f, 0.0f);
-    float hits = 0.0f;
     int centre[3];
     bucketOf(grid, pi, centre);
     const int dims[3] = {int(grid->gridDims[0]), int(grid->gridDims[1]), int(grid->gridDims[2])};
     const uint32_t base = grid->gridBase;
-    // All 27 bucket counts first (independent loads), then the runs in
-    // the reference's dz, dy, dx order.
-    uint32_t cnt[27], bkt[27];
-#pragma unroll
-    for (int q = 0; q < 27; q++) {
+    auto bucketAt = [&](int q, bool& inside) {
         const int x = centre[0] + q % 3 - 1, y = centre[1] + (q / 3) % 3 - 1, z = centre[2] + q / 9 - 1;
-        const bool inside = x >= 0 && x < dims[0] && y >= 0 && y < dims[1] && z >= 0 && z < dims[2];
-        bkt[q] = inside ? base + uint32_t(x) + uint32_t(dims[0]) * (uint32_t(y) + uint32_t(dims[1]) * uint32_t(z)) : 0u;
-        cnt[q] = inside ? count[bkt[q]] : 0u;
-    }
+        inside = x >= 0 && x < dims[0] && y >= 0 && y < dims[1] && z >= 0 && z < dims[2];
+        return base + uint32_t(x) + uint32_t(dims[0]) * (uint32_t(y) + uint32_t(dims[1]) * uint32_t(z));
+    };
+    // Which of the 27 neighbour buckets hold entries: 27 independent loads.
+    uint32_t live = 0;
 #pragma unroll
     for (int q = 0; q < 27; q++) {
-        {
-            const uint32_t n = cnt[q];
-            if (n == 0) continue;
-            const uint32_t held = n < kBucketSlots ? n : kBucketSlots;
-            const uint32_t at = start[bkt[q]];
-            for (uint32_t k = 0; k < held; k++) {
-                {
-                    const uint4 them = sMeta[at + k];
-                    if (!admitted(me, them, selfContact)) continue;
-                    const uint32_t mate = them.x;
-                    const float4 Q = sPos[at + k];
-                    const V pj = xyz(Q);
-                    const V d = pi - pj;
-                    const float dist2 = dot(d, d);
-                    const float reach = radius + __uint_as_float(them.w);
-                    if (dist2 >= reach * reach) continue;
-                    const float wj = Q.w;
-                    const float total = wi + wj;
-                    if (total <= 0.0f) continue;
-                    const float share = wi / total;
-                    const float dist = sqrtf(dist2);
-                    V normal = mk(0.0f, node < mate ? 1.0f : -1.0f, 0.0f);
-                    if (dist > 1e-9f) normal = d / dist;
-                    const float depth = reach - dist;
-                    V correction = normal * (depth * share);
-                    const V sliding = movedI - (pj - xyz(prevState[mate]));
-                    const V tangent = sliding - normal * dot(sliding, normal);
-                    const float slid = length(tangent);
-                    if (slid > 1e-9f) {
-                        const float mu = fminf(frictionI, bodies[them.y].friction);
-                        correction = correction - tangent * (share * fminf(1.0f, mu * depth / slid));
-                    }
-                    sum = sum + correction;
-                    hits = hits + 1.0f;
-                    if (EMIT) {
-                        const uint32_t other = sRec[at + k];
-                        const unsigned long long slot = atomicAdd(pairCount, 1ull);
-                        if (slot < capacity) {
-                            pairs[2 * slot] = r;
-                            pairs[2 * slot + 1] = other;
-                        }
-                    }
+        bool inside;
+        const uint32_t b = bucketAt(q, inside);
+        if (inside && count[b] != 0) live |= 1u << q;
+    }
+    V sum = mk(0.0f, 0.0f, 0.0f);
+    float hits = 0.0f;
+    // The runs in the reference's dz, dy, dx order (ascending q).
+    while (live) {
+        const int q = __ffs(live) - 1;
+        live &= live - 1;
+        bool inside;
+        const uint32_t b = bucketAt(q, inside);
+        const uint32_t n = count[b];
+        const uint32_t held = n < kBucketSlots ? n : kBucketSlots;
+        const uint32_t at = start[b];
+        for (uint32_t k = 0; k < held; k++) {
+            const uint4 them = sMeta[at + k];
+            const float4 Q = sPos[at + k];
+            if (!admitted(me, them, selfContact)) continue;
+            const uint32_t mate = them.x;
+            const V pj = xyz(Q);
+            const V d = pi - pj;
+            const float dist2 = dot(d, d);
+            const float reach = radius + __uint_as_float(them.w);
+            if (dist2 >= reach * reach) continue;
+            const float wj = Q.w;
+            const float total = wi + wj;
+            if (total <= 0.0f) continue;
+            const float share = wi / total;
+            const float dist = sqrtf(dist2);
+            V normal = mk(0.0f, node < mate ? 1.0f : -1.0f, 0.0f);
+            if (dist > 1e-9f) normal = d / dist;
+            const float depth = reach - dist;
+            V correction = normal * (depth * share);
+            const V sliding = movedI - (pj - xyz(prevState[mate]));
+            const V tangent = sliding - normal * dot(sliding, normal);
+            const float slid = length(tangent);
+            if (slid > 1e-9f) {
+                const float mu = fminf(frictionI, bodies[them.y].friction);
+                correction = correction - tangent * (share * fminf(1.0f, mu * depth / slid));
+            }
+            sum = sum + correction;
+            hits = hits + 1.0f;
+            if (EMIT) {
+                const uint32_t other = sRec[at + k];
+                const unsigned long long slot = atomicAdd(pairCount, 1ull);
+                if (slot < capacity) {
+                    pairs[2 * slot] = r;
+                    pairs[2 * slot + 1] = other;
                 }
             }
         }
@@ -739,8 +748,8 @@ cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span&
 // Solve mode leaves the corrections in `delta` for the closing pass, which
 // applies them and empties the grid; Pairs mode lists the hits and empties
 // the grid itself.
-cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& r, ContactMode mode,
-                          uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount) {
+cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& r, uint32_t recordItems,
+                          ContactMode mode, uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount) {
     const uint32_t g = r.grid, b = r.block;
     const Work w = r.work;
     cudaError_t e;
@@ -757,19 +766,20 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& 
                     (const uint32_t*)s.start, (const uint32_t*)s.count, s.entries, (const uint4*)s.surf,
                     (const float4*)s.pos, s.sMeta, s.sPos, s.sRec)))
         return e;
+    // The gather runs over the bucket-ordered entries, one thread each.
+    const uint32_t cg = blocks(recordItems, 256);
+    auto collide = [&](auto kernel, uint32_t* out, uint32_t cap, unsigned long long* n) {
+        return launch(c, kernel, cg, 256u, s.fp, recordItems, (const uint32_t*)s.entries, (const uint32_t*)s.cursor,
+                      (const uint4*)s.surf, (const DevBody*)s.bodies, (const float4*)s.pos, (const float4*)s.prev,
+                      (const uint32_t*)s.start, (const uint32_t*)s.count, (const uint4*)s.sMeta,
+                      (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, out, cap, n);
+    };
     if (mode == ContactMode::Pairs) {
-        if ((e = launch(c, collideKernel<true>, g, b, s.fp, w, s.surf, s.bodies, (const uint32_t*)s.bodyActive,
-                        (const float4*)s.pos, (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count,
-                        (const uint4*)s.sMeta, (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, pairs,
-                        capacity, pairCount)))
-            return e;
+        if ((e = collide(collideKernel<true>, pairs, capacity, pairCount))) return e;
         return launch(c, settleKernel, g, b, s.fp, w, s.surf, (const uint32_t*)s.key, (const float4*)s.delta, s.pos,
                       s.count, s.cursor, 0);
     }
-    return launch(c, collideKernel<false>, g, b, s.fp, w, s.surf, s.bodies, (const uint32_t*)s.bodyActive,
-                  (const float4*)s.pos, (const float4*)s.prev, (const uint32_t*)s.start, (const uint32_t*)s.count,
-                  (const uint4*)s.sMeta, (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, (uint32_t*)nullptr,
-                  0u, (unsigned long long*)nullptr);
+    return collide(collideKernel<false>, (uint32_t*)nullptr, 0u, (unsigned long long*)nullptr);
 }
 
 cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos) {

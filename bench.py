@@ -370,13 +370,16 @@ def drift(frames: int = 300):
             "final_max_abs_m": float(np.max(np.abs(g - r)))}
 
 
-def serving_sweep(quick: bool, seconds_per_point: float = 3.0):
+def serving_sweep(quick: bool, seconds_per_point: float = 3.0, settle_frames: int = 30):
     """Continuous batching under load: a pool of sessions resident on the
     GPU; requests advance a session k ~ U{1..4} frames, half of them dragging
-    a random surface node along a seeded Bezier curve at 0.5 m/s. Saturation
-    is measured closed-loop (every session always has a request), then
-    Poisson arrivals at fractions of it. Frame latency of a request =
-    (completion - arrival) / k."""
+    a random surface node along a seeded Bezier curve at 0.5 m/s. Every
+    session first runs `settle_frames` frames (all at once), so that the
+    bodies have landed and flattened -- the state they spend their life in,
+    with far more self contact than at rest -- before anything is measured.
+    Saturation is then measured closed-loop (every session always has a
+    request), then Poisson arrivals at fractions of it. Frame latency of a
+    request = (completion - arrival) / k."""
     import vsim.scenes as sc
     from vsim.server import Server
 
@@ -398,6 +401,14 @@ def serving_sweep(quick: bool, seconds_per_point: float = 3.0):
             node, control, speed = drags[session]
             drag = (node, control, speed)
         return frames, drag
+
+    t0 = time.perf_counter()
+    for s in range(admitted):
+        server.submit(s, settle_frames)
+    while server.stats()["pending"]:
+        server.tick()
+        server.poll()
+    settle_s = time.perf_counter() - t0
 
     # Saturation: keep every session busy.
     arrival = {}
@@ -468,7 +479,8 @@ def serving_sweep(quick: bool, seconds_per_point: float = 3.0):
             "saturation": {"requests_per_s": round(sat_rate, 1),
                            "session_frames_per_s": round(frames_done / sat_elapsed, 1),
                            "ticks": ticks, "cell_updates_per_s": round(stats0["cell_updates"] / sat_elapsed)},
-            "sweep": points, "pool_generation_s": round(gen_s, 1)}
+            "sweep": points, "settle": {"frames": settle_frames, "seconds": round(settle_s, 1)},
+            "pool_generation_s": round(gen_s, 1)}
 
 
 def main():

@@ -45,23 +45,53 @@ struct LaunchCtx {
     uint32_t sms;  // multiprocessors of the device
 };
 
-// The items one launch covers: all of [0, count) (one thread each), or, with
-// `chunks`, one block per (first item, item count) entry -- the ranges of
-// the bodies a frame steps, so idle bodies cost no threads at all.
+// The items one launch covers. Dense (`table` null): [0, count), one thread
+// each. Chunked: `table[span]` = (first chunk, chunk count) of this launch,
+// and `table[kSpans + first + c]` = (first item, item count <= kChunk) --
+// the ranges of the bodies a frame steps, so idle bodies cost no threads.
+// Blocks of kChunk threads take the chunks in turn, so a fixed grid covers
+// any set of bodies and the launch can be captured once in a graph.
 struct Work {
-    const uint2* chunks;
+    const uint2* table;
+    uint32_t span;
     uint32_t count;
 };
 
-__device__ __forceinline__ bool workItem(const Work& w, uint32_t& item) {
-    if (w.chunks) {
-        const uint2 c = w.chunks[blockIdx.x];
-        if (threadIdx.x >= c.y) return false;
-        item = c.x + threadIdx.x;
-        return true;
+// Spans of a frame: the active nodes, the eight colours' cells, the surface
+// records.
+constexpr uint32_t kSpans = 10;
+constexpr uint32_t kNodeSpan = 0, kRecordSpan = 9;
+constexpr uint32_t colourSpan(int c) { return 1 + uint32_t(c); }
+
+// Calls f(item) for each item of `w` this thread owns.
+template <class F>
+__device__ __forceinline__ void forEachItem(const Work& w, F&& f) {
+    if (!w.table) {
+        const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < w.count) f(i);
+        return;
     }
-    item = blockIdx.x * blockDim.x + threadIdx.x;
-    return item < w.count;
+    const uint2 d = w.table[w.span];
+    for (uint32_t c = blockIdx.x; c < d.y; c += gridDim.x) {
+        const uint2 chunk = w.table[kSpans + d.x + c];
+        if (threadIdx.x < chunk.y) f(chunk.x + threadIdx.x);
+    }
+}
+
+// As forEachItem, but every thread of the block calls f(has, item) the same
+// number of times (for block-wide scans); `has` says whether `item` is real.
+template <class F>
+__device__ __forceinline__ void forEachItemUniform(const Work& w, F&& f) {
+    if (!w.table) {
+        const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+        f(i < w.count, i);
+        return;
+    }
+    const uint2 d = w.table[w.span];
+    for (uint32_t c = blockIdx.x; c < d.y; c += gridDim.x) {
+        const uint2 chunk = w.table[kSpans + d.x + c];
+        f(threadIdx.x < chunk.y, chunk.x + threadIdx.x);
+    }
 }
 
 // One launch: its work, grid and block.
@@ -99,8 +129,8 @@ cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4*
 // next substep's prediction.
 cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span& nodes, bool contact,
                            bool predictNext);
-// `records` covers the surface records of the stepped bodies, `recordItems`
-// of them in all (the gather's thread count).
+// `records` covers the surface records of the stepped bodies; at most
+// `recordItems` of them are binned.
 cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& records, uint32_t recordItems,
                           ContactMode mode, uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount);
 cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos);

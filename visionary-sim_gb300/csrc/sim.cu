@@ -189,34 +189,37 @@ void buildDensePlan(vsim_sim* s) {
     p.nodes = denseSpan(s->activeCount, 256);
     for (int c = 0; c < 8; c++) p.colour[c] = elasticSpan(s->colorStart[c + 1] - s->colorStart[c], s->block, s->sms);
     p.records = denseSpan(s->surfaceCount, 256);
-    p.recordCount = s->surfaceCount;
 }
 
 void useDensePlan(vsim_sim* s) { s->plan = s->dense; }
 
-// One (first, count) chunk per block over the given bodies' ranges.
+// Chunks of at most kChunk items over the listed bodies' ranges, one table
+// for the whole frame: kSpans descriptors, then the chunks. The spans' grids
+// and the table's address never change, so one captured graph serves every
+// set of bodies; only the table is uploaded per frame.
 int planBodies(vsim_sim* s, const std::vector<uint32_t>& bodies) {
+    uint2* table = s->chunkPinned;
+    uint2* chunks = table + kSpans;
     size_t at = 0;
-    auto emit = [&](const std::vector<uint32_t>& start, Span& span) {
+    auto emit = [&](uint32_t span, const std::vector<uint32_t>& start) {
         const size_t first = at;
         for (uint32_t b : bodies)
             for (uint32_t i = start[b]; i < start[b + 1]; i += kChunk) {
                 if (at == s->chunkCapacity) return false;
-                s->chunkPinned[at++] = make_uint2(i, std::min(kChunk, start[b + 1] - i));
+                chunks[at++] = make_uint2(i, std::min(kChunk, start[b + 1] - i));
             }
-        span = Span{Work{s->chunkDev + first, 0}, uint32_t(at - first), kChunk};
+        table[span] = make_uint2(uint32_t(first), uint32_t(at - first));
         return true;
     };
-    FramePlan p;
-    p.chunked = true;
-    bool ok = emit(s->nodeBodyStart, p.nodes);
-    for (int c = 0; c < 8 && ok; c++) ok = emit(s->colourBodyStart[c], p.colour[c]);
-    ok = ok && emit(s->recordBodyStart, p.records);
-    for (uint32_t b : bodies) p.recordCount += s->recordBodyStart[b + 1] - s->recordBodyStart[b];
-    if (!ok) return fail(VSIM_ERR_CAPACITY, "chunk table too small");
-    CK(cudaMemcpyAsync(s->chunkDev, s->chunkPinned, at * sizeof(uint2), cudaMemcpyHostToDevice, s->stream),
+    // The staging may still feed the previous frame's upload.
+    CK(cudaStreamSynchronize(s->stream), "upload work chunks");
+    bool ok = emit(kNodeSpan, s->nodeBodyStart);
+    for (int c = 0; c < 8 && ok; c++) ok = emit(colourSpan(c), s->colourBodyStart[c]);
+    ok = ok && emit(kRecordSpan, s->recordBodyStart);
+    if (!ok) return fail(VSIM_ERR_CAPACITY, "chunk table too small (a body listed twice?)");
+    CK(cudaMemcpyAsync(s->chunkDev, table, (kSpans + at) * sizeof(uint2), cudaMemcpyHostToDevice, s->stream),
        "upload work chunks");
-    s->plan = p;
+    s->plan = s->chunked;
     return VSIM_OK;
 }
 
@@ -303,7 +306,7 @@ cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMod
                 }
         if (contact && plan.records.grid) {
             begin(VSIM_KIND_CONTACT, kContactKernels);
-            if ((e = launchContact(c, s->d, plan.records, plan.recordCount, mode, nullptr, 0, nullptr))) return e;
+            if ((e = launchContact(c, s->d, plan.records, s->surfaceCount, mode, nullptr, 0, nullptr))) return e;
             end();
         }
         begin(VSIM_KIND_FINALIZE, 1);
@@ -322,6 +325,7 @@ uint64_t graphKey(const vsim_sim* s, uint32_t steps) {
     k = k * 31 + (anyStretch(s) ? 1 : 0);
     k = k * 1031 + s->block;
     k = k * 31 + (s->pdl ? 1 : 0);
+    k = k * 31 + (s->plan.chunked ? 1 : 0);
     return k;
 }
 
@@ -333,9 +337,7 @@ void dropGraphs(vsim_sim* s) {
 int runFrame(vsim_sim* s, uint32_t steps) {
     int rc = syncParams(s);
     if (rc) return rc;
-    // A chunked plan changes every frame: launch it directly (with
-    // programmatic dependent launch) rather than capture it.
-    if (!s->useGraph || s->plan.chunked) {
+    if (!s->useGraph) {
         CK(encodeFrame(s, s->stream, steps), "launch substep");
         return VSIM_OK;
     }
@@ -574,17 +576,28 @@ int createSim(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, v
     buildDensePlan(s);
     useDensePlan(s);
     if (isolated) {
-        // Room for a chunk table over every body at once.
+        // Room for a chunk table over every body at once, and the spans
+        // over it: blocks of kChunk threads, as many as fill the device
+        // (the elastic pass holds 4 such blocks per SM at its registers).
         size_t chunks = 0;
-        auto count = [&](const std::vector<uint32_t>& start) {
-            for (uint32_t b = 0; b < n; b++) chunks += (start[b + 1] - start[b] + kChunk - 1) / kChunk;
+        auto span = [&](uint32_t index, const std::vector<uint32_t>& start, uint32_t perSm) {
+            size_t most = 0;
+            for (uint32_t b = 0; b < n; b++) most += (start[b + 1] - start[b] + kChunk - 1) / kChunk;
+            chunks += most;
+            const uint32_t grid = uint32_t(std::min<size_t>(most, size_t(perSm) * s->sms));
+            return Span{Work{nullptr, index, 0}, grid, kChunk};
         };
-        count(s->nodeBodyStart);
-        for (int c = 0; c < 8; c++) count(s->colourBodyStart[c]);
-        count(s->recordBodyStart);
+        FramePlan& p = s->chunked;
+        p.chunked = true;
+        p.nodes = span(kNodeSpan, s->nodeBodyStart, 16);
+        for (int c = 0; c < 8; c++) p.colour[c] = span(colourSpan(c), s->colourBodyStart[c], 4);
+        p.records = span(kRecordSpan, s->recordBodyStart, 16);
         s->chunkCapacity = chunks;
-        CK(allocN(&s->chunkDev, chunks), "allocate work chunks");
-        CK(cudaMallocHost(&s->chunkPinned, std::max<size_t>(chunks, 1) * sizeof(uint2)), "allocate staging");
+        CK(allocN(&s->chunkDev, kSpans + chunks), "allocate work chunks");
+        CK(cudaMallocHost(&s->chunkPinned, (kSpans + chunks) * sizeof(uint2)), "allocate staging");
+        p.nodes.work.table = s->chunkDev;
+        for (int c = 0; c < 8; c++) p.colour[c].work.table = s->chunkDev;
+        p.records.work.table = s->chunkDev;
     }
     std::vector<int32_t> nodeRecord(N, -1);
     for (uint32_t r = 0; r < s->surfaceCount; r++) nodeRecord[s->surfHost[r].x] = int32_t(r);
@@ -1083,7 +1096,8 @@ int vsim_contact_pairs(vsim_sim* s, uint32_t* pairs, size_t capacity, size_t* co
     if (rc) return rc;
     CK(cudaMemsetAsync(s->pairCount, 0, sizeof(unsigned long long), s->stream), "count pairs");
     const LaunchCtx c{s->stream, false, s->sms};
-    CK(launchContact(c, s->d, s->dense.records, s->dense.recordCount, ContactMode::Pairs, s->pairs, uint32_t(capacity), s->pairCount),
+    CK(launchContact(c, s->d, s->dense.records, s->surfaceCount, ContactMode::Pairs, s->pairs,
+                     uint32_t(capacity), s->pairCount),
        "list pairs");
     unsigned long long total = 0;
     CK(cudaMemcpyAsync(&total, s->pairCount, sizeof total, cudaMemcpyDeviceToHost, s->stream), "count pairs");

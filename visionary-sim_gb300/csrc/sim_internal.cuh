@@ -51,7 +51,6 @@ struct FramePlan {
     Span nodes{};
     Span colour[8]{};
     Span records{};
-    uint32_t recordCount = 0;  // surface records the spans cover
 };
 
 }  // namespace vsim
@@ -121,11 +120,12 @@ struct vsim_sim {
     // colour's cell range (relative to the colour's start) and in the
     // surface records; one past the last body closes each list.
     std::vector<uint32_t> nodeBodyStart, recordBodyStart, colourBodyStart[8];
-    vsim::FramePlan plan;    // the current frame's spans
-    vsim::FramePlan dense;   // every body
-    uint2* chunkDev = nullptr;
+    vsim::FramePlan plan;     // the current frame's spans
+    vsim::FramePlan dense;    // every body
+    vsim::FramePlan chunked;  // the bodies planBodies listed (fixed grids over the chunk table)
+    uint2* chunkDev = nullptr;     // span descriptors, then chunks (Work)
     uint2* chunkPinned = nullptr;  // host staging of the chunk table
-    size_t chunkCapacity = 0;
+    size_t chunkCapacity = 0;      // chunks, not counting the descriptors
     uint32_t* activePinned = nullptr;  // host staging of the activity and drive tables
     float4* grabsPinned = nullptr;
 };

@@ -166,18 +166,19 @@ __global__ void predictKernel(const FrameParams* __restrict__ fp, Work work, con
                               float4* __restrict__ pos, float4* __restrict__ prev, float4* __restrict__ vel) {
     pdlWait();
     pdlLaunchNext();
-    uint32_t i;
-    if (!workItem(work, i) || !bodyActive[activeBody[i]]) return;
-    const uint32_t n = active[i];
-    const float4 P = pos[n];
-    if (P.w == 0.0f) return;
-    const float dt = fp->dt;
-    const V g = mk(fp->gx, fp->gy, fp->gz);
-    const V v = xyz(vel[n]) + g * dt;
-    const V p = xyz(P);
-    prev[n] = withW(p, 0.0f);
-    pos[n] = withW(p + v * dt, P.w);
-    vel[n] = withW(v, 0.0f);
+    forEachItem(work, [&](uint32_t i) {
+        if (!bodyActive[activeBody[i]]) return;
+        const uint32_t n = active[i];
+        const float4 P = pos[n];
+        if (P.w == 0.0f) return;
+        const float dt = fp->dt;
+        const V g = mk(fp->gx, fp->gy, fp->gz);
+        const V v = xyz(vel[n]) + g * dt;
+        const V p = xyz(P);
+        prev[n] = withW(p, 0.0f);
+        pos[n] = withW(p + v * dt, P.w);
+        vel[n] = withW(v, 0.0f);
+    });
 }
 
 // driveHard.wgsl:15-35 and driveCompliant.wgsl:24-41.
@@ -231,61 +232,62 @@ __global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ c
                                                      const float4* __restrict__ prevState, StretchLengths lens) {
     pdlWait();
     pdlLaunchNext();
-    uint32_t slot;
-    if (!workItem(work, slot)) return;
-    const uint4 entry = cells[slot];
-    if (!bodyActive[entry.y]) return;
-    const DevBody* b = bodies + entry.y;
-    const float maxStretch = b->maxStretch;
-    if (LIMIT_ONLY && !(maxStretch > 1.0f)) return;
-    const uint32_t nx = entry.z, nxy = entry.w, n0 = entry.x;
-    const uint32_t ids[8] = {n0, n0 + 1, n0 + nx, n0 + nx + 1, n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
-    V p[8], prev[8];
-    float w[8];
+    forEachItem(work, [&](uint32_t slot) {
+        const uint4 entry = cells[slot];
+        if (!bodyActive[entry.y]) return;
+        const DevBody* b = bodies + entry.y;
+        const float maxStretch = b->maxStretch;
+        if (LIMIT_ONLY && !(maxStretch > 1.0f)) return;
+        const uint32_t nx = entry.z, nxy = entry.w, n0 = entry.x;
+        const uint32_t ids[8] = {n0,       n0 + 1,       n0 + nx,       n0 + nx + 1,
+                                 n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
+        V p[8], prev[8];
+        float w[8];
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-        const float4 P = pos[ids[c]];
-        p[c] = xyz(P);
-        w[c] = P.w;
-    }
+        for (int c = 0; c < 8; c++) {
+            const float4 P = pos[ids[c]];
+            p[c] = xyz(P);
+            w[c] = P.w;
+        }
 #pragma unroll
-    for (int c = 0; c < 8; c++) prev[c] = xyz(prevState[ids[c]]);
+        for (int c = 0; c < 8; c++) prev[c] = xyz(prevState[ids[c]]);
 
-    if (!LIMIT_ONLY) {
-        const float alphaDev = b->alphaDev, alphaHyd = b->alphaHyd, gamma = b->gamma, relax = b->relax;
-        const float s = b->restScale, ns = -s;
-        projectTet<0>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-        projectTet<1>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-        projectTet<2>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-        projectTet<3>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-        projectTet<4>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-        projectTet<5>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-    }
+        if (!LIMIT_ONLY) {
+            const float alphaDev = b->alphaDev, alphaHyd = b->alphaHyd, gamma = b->gamma, relax = b->relax;
+            const float s = b->restScale, ns = -s;
+            projectTet<0>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            projectTet<1>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            projectTet<2>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            projectTet<3>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            projectTet<4>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            projectTet<5>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+        }
 
-    // project.wgsl:162-179: unilateral length limit over all 28 corner pairs.
-    if (maxStretch > 1.0f) {
-        const float h = b->h;
-        for (int sweep = 0; sweep < 2; sweep++) {
+        // project.wgsl:162-179: unilateral length limit over all 28 corner pairs.
+        if (maxStretch > 1.0f) {
+            const float h = b->h;
+            for (int sweep = 0; sweep < 2; sweep++) {
 #pragma unroll
-            for (int a = 0; a < 8; a++) {
+                for (int a = 0; a < 8; a++) {
 #pragma unroll
-                for (int bb = a + 1; bb < 8; bb++) {
-                    const V delta = p[bb] - p[a];
-                    const float len = length(delta);
-                    const float maximum = lens.len[__popc(a ^ bb) - 1] * h * maxStretch;
-                    const float weight = w[a] + w[bb];
-                    if (len > maximum && weight > 0.0f) {
-                        const V correction = delta * ((len - maximum) / (len * weight));
-                        p[a] = p[a] + w[a] * correction;
-                        p[bb] = p[bb] - w[bb] * correction;
+                    for (int bb = a + 1; bb < 8; bb++) {
+                        const V delta = p[bb] - p[a];
+                        const float len = length(delta);
+                        const float maximum = lens.len[__popc(a ^ bb) - 1] * h * maxStretch;
+                        const float weight = w[a] + w[bb];
+                        if (len > maximum && weight > 0.0f) {
+                            const V correction = delta * ((len - maximum) / (len * weight));
+                            p[a] = p[a] + w[a] * correction;
+                            p[bb] = p[bb] - w[bb] * correction;
+                        }
                     }
                 }
             }
         }
-    }
 
 #pragma unroll
-    for (int c = 0; c < 8; c++) pos[ids[c]] = withW(p[c], w[c]);
+        for (int c = 0; c < 8; c++) pos[ids[c]] = withW(p[c], w[c]);
+    });
 }
 
 // finalize.wgsl:29-42.
@@ -318,49 +320,49 @@ __global__ void finalizeKernel(const FrameParams* __restrict__ fp, Work work, co
     pdlWait();
     pdlLaunchNext();
     if (CONTACT && blockIdx.x == 0 && threadIdx.x == 0) *cursor = 0;
-    uint32_t i;
-    if (!workItem(work, i)) return;
-    const uint32_t bodyIndex = activeBody[i];
-    if (!bodyActive[bodyIndex]) return;
-    const uint32_t n = active[i];
-    float4 P = pos[n];
-    if (CONTACT) {
-        const int32_t r = nodeRecord[n];
-        if (r >= 0) {
-            const float4 d = delta[r];
-            if (d.w > 0.0f) {
-                const V step = xyz(d) * (1.0f / d.w);
-                P = withW(xyz(P) + step, P.w);
-                if (P.w == 0.0f) pos[n] = P;
+    forEachItem(work, [&](uint32_t i) {
+        const uint32_t bodyIndex = activeBody[i];
+        if (!bodyActive[bodyIndex]) return;
+        const uint32_t n = active[i];
+        float4 P = pos[n];
+        if (CONTACT) {
+            const int32_t r = nodeRecord[n];
+            if (r >= 0) {
+                const float4 d = delta[r];
+                if (d.w > 0.0f) {
+                    const V step = xyz(d) * (1.0f / d.w);
+                    P = withW(xyz(P) + step, P.w);
+                    if (P.w == 0.0f) pos[n] = P;
+                }
+                count[key[r]] = 0;
             }
-            count[key[r]] = 0;
         }
-    }
-    if (P.w == 0.0f) return;
-    const DevBody* b = bodies + bodyIndex;
-    const V prev = xyz(prevState[n]);
-    const float fr = b->friction;
-    const V mn = mk(fp->tankMin[0], fp->tankMin[1], fp->tankMin[2]);
-    const V mx = mk(fp->tankMax[0], fp->tankMax[1], fp->tankMax[2]);
-    V p = xyz(P);
-    p = resolvePlane(p, prev, mk(0.0f, 1.0f, 0.0f), mn.y - p.y, fr);
-    p = resolvePlane(p, prev, mk(1.0f, 0.0f, 0.0f), mn.x - p.x, fr);
-    p = resolvePlane(p, prev, mk(-1.0f, 0.0f, 0.0f), p.x - mx.x, fr);
-    p = resolvePlane(p, prev, mk(0.0f, 0.0f, 1.0f), mn.z - p.z, fr);
-    p = resolvePlane(p, prev, mk(0.0f, 0.0f, -1.0f), p.z - mx.z, fr);
-    const float dt = fp->dt;
-    V v = (p - prev) / dt;
-    v = v * b->damp;
-    if (PREDICT) {
-        const V g = mk(fp->gx, fp->gy, fp->gz);
-        const V v2 = v + g * dt;
-        prevState[n] = withW(p, 0.0f);
-        pos[n] = withW(p + v2 * dt, P.w);
-        vel[n] = withW(v2, 0.0f);
-    } else {
-        pos[n] = withW(p, P.w);
-        vel[n] = withW(v, 0.0f);
-    }
+        if (P.w == 0.0f) return;
+        const DevBody* b = bodies + bodyIndex;
+        const V prev = xyz(prevState[n]);
+        const float fr = b->friction;
+        const V mn = mk(fp->tankMin[0], fp->tankMin[1], fp->tankMin[2]);
+        const V mx = mk(fp->tankMax[0], fp->tankMax[1], fp->tankMax[2]);
+        V p = xyz(P);
+        p = resolvePlane(p, prev, mk(0.0f, 1.0f, 0.0f), mn.y - p.y, fr);
+        p = resolvePlane(p, prev, mk(1.0f, 0.0f, 0.0f), mn.x - p.x, fr);
+        p = resolvePlane(p, prev, mk(-1.0f, 0.0f, 0.0f), p.x - mx.x, fr);
+        p = resolvePlane(p, prev, mk(0.0f, 0.0f, 1.0f), mn.z - p.z, fr);
+        p = resolvePlane(p, prev, mk(0.0f, 0.0f, -1.0f), p.z - mx.z, fr);
+        const float dt = fp->dt;
+        V v = (p - prev) / dt;
+        v = v * b->damp;
+        if (PREDICT) {
+            const V g = mk(fp->gx, fp->gy, fp->gz);
+            const V v2 = v + g * dt;
+            prevState[n] = withW(p, 0.0f);
+            pos[n] = withW(p + v2 * dt, P.w);
+            vel[n] = withW(v2, 0.0f);
+        } else {
+            pos[n] = withW(p, P.w);
+            vel[n] = withW(v, 0.0f);
+        }
+    });
 }
 
 // ------------------------------------------------------------- contact --
@@ -394,18 +396,18 @@ __global__ void binKernel(const FrameParams* __restrict__ fp, Work work, const u
                           uint32_t* __restrict__ count) {
     pdlWait();
     pdlLaunchNext();
-    uint32_t r;
-    if (!workItem(work, r)) return;
-    const uint4 rec = surf[r];
-    if (!bodyActive[rec.y]) {
-        key[r] = kIdle;
-        rank[r] = kIdle;
-        return;
-    }
-    int coord[3];
-    const uint32_t b = bucketOf(bodies + rec.y, xyz(pos[rec.x]), coord);
-    key[r] = b;
-    rank[r] = atomicAdd(&count[b], 1u);
+    forEachItem(work, [&](uint32_t r) {
+        const uint4 rec = surf[r];
+        if (!bodyActive[rec.y]) {
+            key[r] = kIdle;
+            rank[r] = kIdle;
+            return;
+        }
+        int coord[3];
+        const uint32_t b = bucketOf(bodies + rec.y, xyz(pos[rec.x]), coord);
+        key[r] = b;
+        rank[r] = atomicAdd(&count[b], 1u);
+    });
 }
 
 // Each bucket's first-arriving record reserves the bucket's segment; one
@@ -417,35 +419,36 @@ __global__ void allocKernel(const FrameParams* __restrict__ fp, Work work, const
     pdlLaunchNext();
     __shared__ uint32_t warpSum[32];
     __shared__ uint32_t blockBase;
-    uint32_t r = 0;
-    const bool has = workItem(work, r);
-    const bool first = has && rank[r] == 0;
-    const uint32_t b = first ? key[r] : 0;
-    const uint32_t need = first ? count[b] : 0;
-    // Block-wide exclusive prefix of `need`.
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t incl = need;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= uint32_t(d)) incl += v;
-    }
-    if (lane == 31) warpSum[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        const uint32_t nw = blockDim.x >> 5;
-        uint32_t v = lane < nw ? warpSum[lane] : 0;
-        uint32_t scan = v;
+    forEachItemUniform(work, [&](bool has, uint32_t r) {
+        const bool first = has && rank[r] == 0;
+        const uint32_t b = first ? key[r] : 0;
+        const uint32_t need = first ? count[b] : 0;
+        // Block-wide exclusive prefix of `need`.
+        const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint32_t incl = need;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t u = __shfl_up_sync(0xffffffffu, scan, d);
-            if (lane >= uint32_t(d)) scan += u;
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= uint32_t(d)) incl += v;
         }
-        if (lane < nw) warpSum[lane] = scan - v;
-        if (lane == nw - 1) blockBase = scan > 0 ? atomicAdd(cursor, scan) : 0;
-    }
-    __syncthreads();
-    if (first) start[b] = blockBase + warpSum[warp] + (incl - need);
+        if (lane == 31) warpSum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t nw = blockDim.x >> 5;
+            uint32_t v = lane < nw ? warpSum[lane] : 0;
+            uint32_t scan = v;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, scan, d);
+                if (lane >= uint32_t(d)) scan += u;
+            }
+            if (lane < nw) warpSum[lane] = scan - v;
+            if (lane == nw - 1) blockBase = scan > 0 ? atomicAdd(cursor, scan) : 0;
+        }
+        __syncthreads();
+        if (first) start[b] = blockBase + warpSum[warp] + (incl - need);
+        __syncthreads();  // warpSum and blockBase are rewritten by the next chunk
+    });
 }
 
 __global__ void scatterKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ key,
@@ -453,9 +456,10 @@ __global__ void scatterKernel(const FrameParams* __restrict__ fp, Work work, con
                               uint32_t* __restrict__ entries) {
     pdlWait();
     pdlLaunchNext();
-    uint32_t r;
-    if (!workItem(work, r) || key[r] == kIdle) return;
-    entries[start[key[r]] + rank[r]] = r;
+    forEachItem(work, [&](uint32_t r) {
+        if (key[r] == kIdle) return;
+        entries[start[key[r]] + rank[r]] = r;
+    });
 }
 
 // sort.wgsl:14-53: the bucket's visible entries -- its kBucketSlots lowest
@@ -469,48 +473,49 @@ __global__ void canonKernel(const FrameParams* __restrict__ fp, Work work, const
                             float4* __restrict__ sPos, uint32_t* __restrict__ sRec) {
     pdlWait();
     pdlLaunchNext();
-    uint32_t r;
-    if (!workItem(work, r) || rank[r] != 0) return;
-    const uint32_t b = key[r];
-    const uint32_t n = count[b];
-    const uint32_t base = start[b];
-    uint32_t* e = entries + base;
-    const uint32_t m = n < kBucketSlots ? n : kBucketSlots;
-    if (n < 2) {
-        const uint4 rec = surf[r];
-        sMeta[base] = rec;
-        sPos[base] = pos[rec.x];
-        sRec[base] = r;
-        return;
-    }
-    for (uint32_t i = 1; i < m; i++) {
-        const uint32_t v = e[i];
-        uint32_t at = i;
-        while (at > 0 && e[at - 1] > v) {
-            e[at] = e[at - 1];
-            at--;
+    forEachItem(work, [&](uint32_t r) {
+        if (rank[r] != 0) return;
+        const uint32_t b = key[r];
+        const uint32_t n = count[b];
+        const uint32_t base = start[b];
+        uint32_t* e = entries + base;
+        const uint32_t m = n < kBucketSlots ? n : kBucketSlots;
+        if (n < 2) {
+            const uint4 rec = surf[r];
+            sMeta[base] = rec;
+            sPos[base] = pos[rec.x];
+            sRec[base] = r;
+            return;
         }
-        e[at] = v;
-    }
-    // Past capacity, keep the lowest kBucketSlots in the visible prefix.
-    for (uint32_t i = m; i < n; i++) {
-        const uint32_t v = e[i];
-        if (v >= e[m - 1]) continue;
-        e[i] = e[m - 1];
-        uint32_t at = m - 1;
-        while (at > 0 && e[at - 1] > v) {
-            e[at] = e[at - 1];
-            at--;
+        for (uint32_t i = 1; i < m; i++) {
+            const uint32_t v = e[i];
+            uint32_t at = i;
+            while (at > 0 && e[at - 1] > v) {
+                e[at] = e[at - 1];
+                at--;
+            }
+            e[at] = v;
         }
-        e[at] = v;
-    }
-    for (uint32_t k = 0; k < m; k++) {
-        const uint32_t other = e[k];
-        const uint4 rec = surf[other];
-        sMeta[base + k] = rec;
-        sPos[base + k] = pos[rec.x];
-        sRec[base + k] = other;
-    }
+        // Past capacity, keep the lowest kBucketSlots in the visible prefix.
+        for (uint32_t i = m; i < n; i++) {
+            const uint32_t v = e[i];
+            if (v >= e[m - 1]) continue;
+            e[i] = e[m - 1];
+            uint32_t at = m - 1;
+            while (at > 0 && e[at - 1] > v) {
+                e[at] = e[at - 1];
+                at--;
+            }
+            e[at] = v;
+        }
+        for (uint32_t k = 0; k < m; k++) {
+            const uint32_t other = e[k];
+            const uint4 rec = surf[other];
+            sMeta[base + k] = rec;
+            sPos[base + k] = pos[rec.x];
+            sRec[base + k] = other;
+        }
+    });
 }
 
 // Whether records a and b may touch: the reference drops every same-body
@@ -549,86 +554,87 @@ __global__ void __launch_bounds__(256) collideKernel(
     unsigned long long* __restrict__ pairCount) {
     pdlWait();
     pdlLaunchNext();
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= items || i >= *cursor) return;
-    const uint32_t r = entries[i];
-    const uint4 me = surf[r];
-    const DevBody* grid = bodies + me.y;
-    const uint32_t node = me.x;
-    const float radius = __uint_as_float(me.w);
-    const float4 P = pos[node];
-    const float wi = P.w;
-    const V pi = xyz(P);
-    const V movedI = pi - xyz(prevState[node]);
-    const float frictionI = grid->friction;
-    const uint32_t selfContact = fp->selfContact;
-    int centre[3];
-    bucketOf(grid, pi, centre);
-    const int dims[3] = {int(grid->gridDims[0]), int(grid->gridDims[1]), int(grid->gridDims[2])};
-    const uint32_t base = grid->gridBase;
-    auto bucketAt = [&](int q, bool& inside) {
-        const int x = centre[0] + q % 3 - 1, y = centre[1] + (q / 3) % 3 - 1, z = centre[2] + q / 9 - 1;
-        inside = x >= 0 && x < dims[0] && y >= 0 && y < dims[1] && z >= 0 && z < dims[2];
-        return base + uint32_t(x) + uint32_t(dims[0]) * (uint32_t(y) + uint32_t(dims[1]) * uint32_t(z));
-    };
-    // Which of the 27 neighbour buckets hold entries: 27 independent loads.
-    uint32_t live = 0;
+    const uint32_t total = min(items, *cursor);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const uint32_t r = entries[i];
+        const uint4 me = surf[r];
+        const DevBody* grid = bodies + me.y;
+        const uint32_t node = me.x;
+        const float radius = __uint_as_float(me.w);
+        const float4 P = pos[node];
+        const float wi = P.w;
+        const V pi = xyz(P);
+        const V movedI = pi - xyz(prevState[node]);
+        const float frictionI = grid->friction;
+        const uint32_t selfContact = fp->selfContact;
+        int centre[3];
+        bucketOf(grid, pi, centre);
+        const int dims[3] = {int(grid->gridDims[0]), int(grid->gridDims[1]), int(grid->gridDims[2])};
+        const uint32_t base = grid->gridBase;
+        auto bucketAt = [&](int q, bool& inside) {
+            const int x = centre[0] + q % 3 - 1, y = centre[1] + (q / 3) % 3 - 1, z = centre[2] + q / 9 - 1;
+            inside = x >= 0 && x < dims[0] && y >= 0 && y < dims[1] && z >= 0 && z < dims[2];
+            return base + uint32_t(x) + uint32_t(dims[0]) * (uint32_t(y) + uint32_t(dims[1]) * uint32_t(z));
+        };
+        // Which of the 27 neighbour buckets hold entries: 27 independent loads.
+        uint32_t live = 0;
 #pragma unroll
-    for (int q = 0; q < 27; q++) {
-        bool inside;
-        const uint32_t b = bucketAt(q, inside);
-        if (inside && count[b] != 0) live |= 1u << q;
-    }
-    V sum = mk(0.0f, 0.0f, 0.0f);
-    float hits = 0.0f;
-    // The runs in the reference's dz, dy, dx order (ascending q).
-    while (live) {
-        const int q = __ffs(live) - 1;
-        live &= live - 1;
-        bool inside;
-        const uint32_t b = bucketAt(q, inside);
-        const uint32_t n = count[b];
-        const uint32_t held = n < kBucketSlots ? n : kBucketSlots;
-        const uint32_t at = start[b];
-        for (uint32_t k = 0; k < held; k++) {
-            const uint4 them = sMeta[at + k];
-            const float4 Q = sPos[at + k];
-            if (!admitted(me, them, selfContact)) continue;
-            const uint32_t mate = them.x;
-            const V pj = xyz(Q);
-            const V d = pi - pj;
-            const float dist2 = dot(d, d);
-            const float reach = radius + __uint_as_float(them.w);
-            if (dist2 >= reach * reach) continue;
-            const float wj = Q.w;
-            const float total = wi + wj;
-            if (total <= 0.0f) continue;
-            const float share = wi / total;
-            const float dist = sqrtf(dist2);
-            V normal = mk(0.0f, node < mate ? 1.0f : -1.0f, 0.0f);
-            if (dist > 1e-9f) normal = d / dist;
-            const float depth = reach - dist;
-            V correction = normal * (depth * share);
-            const V sliding = movedI - (pj - xyz(prevState[mate]));
-            const V tangent = sliding - normal * dot(sliding, normal);
-            const float slid = length(tangent);
-            if (slid > 1e-9f) {
-                const float mu = fminf(frictionI, bodies[them.y].friction);
-                correction = correction - tangent * (share * fminf(1.0f, mu * depth / slid));
-            }
-            sum = sum + correction;
-            hits = hits + 1.0f;
-            if (EMIT) {
-                const uint32_t other = sRec[at + k];
-                const unsigned long long slot = atomicAdd(pairCount, 1ull);
-                if (slot < capacity) {
-                    pairs[2 * slot] = r;
-                    pairs[2 * slot + 1] = other;
+        for (int q = 0; q < 27; q++) {
+            bool inside;
+            const uint32_t b = bucketAt(q, inside);
+            if (inside && count[b] != 0) live |= 1u << q;
+        }
+        V sum = mk(0.0f, 0.0f, 0.0f);
+        float hits = 0.0f;
+        // The runs in the reference's dz, dy, dx order (ascending q).
+        while (live) {
+            const int q = __ffs(live) - 1;
+            live &= live - 1;
+            bool inside;
+            const uint32_t b = bucketAt(q, inside);
+            const uint32_t n = count[b];
+            const uint32_t held = n < kBucketSlots ? n : kBucketSlots;
+            const uint32_t at = start[b];
+            for (uint32_t k = 0; k < held; k++) {
+                const uint4 them = sMeta[at + k];
+                const float4 Q = sPos[at + k];
+                if (!admitted(me, them, selfContact)) continue;
+                const uint32_t mate = them.x;
+                const V pj = xyz(Q);
+                const V d = pi - pj;
+                const float dist2 = dot(d, d);
+                const float reach = radius + __uint_as_float(them.w);
+                if (dist2 >= reach * reach) continue;
+                const float wj = Q.w;
+                const float total = wi + wj;
+                if (total <= 0.0f) continue;
+                const float share = wi / total;
+                const float dist = sqrtf(dist2);
+                V normal = mk(0.0f, node < mate ? 1.0f : -1.0f, 0.0f);
+                if (dist > 1e-9f) normal = d / dist;
+                const float depth = reach - dist;
+                V correction = normal * (depth * share);
+                const V sliding = movedI - (pj - xyz(prevState[mate]));
+                const V tangent = sliding - normal * dot(sliding, normal);
+                const float slid = length(tangent);
+                if (slid > 1e-9f) {
+                    const float mu = fminf(frictionI, bodies[them.y].friction);
+                    correction = correction - tangent * (share * fminf(1.0f, mu * depth / slid));
+                }
+                sum = sum + correction;
+                hits = hits + 1.0f;
+                if (EMIT) {
+                    const uint32_t other = sRec[at + k];
+                    const unsigned long long slot = atomicAdd(pairCount, 1ull);
+                    if (slot < capacity) {
+                        pairs[2 * slot] = r;
+                        pairs[2 * slot + 1] = other;
+                    }
                 }
             }
         }
+        if (!EMIT) delta[r] = withW(sum, hits);
     }
-    if (!EMIT) delta[r] = withW(sum, hits);
 }
 
 // settle.wgsl:20-36 (gain 1, bodyContact.js:48), then empties the buckets
@@ -639,20 +645,19 @@ __global__ void settleKernel(const FrameParams* __restrict__ fp, Work work, cons
                              int apply) {
     pdlWait();
     pdlLaunchNext();
-    uint32_t r;
-    const bool has = workItem(work, r);
     if (blockIdx.x == 0 && threadIdx.x == 0) *cursor = 0;
-    if (!has) return;
-    if (apply) {
-        const float4 d = delta[r];
-        if (d.w > 0.0f) {
-            const uint32_t node = surf[r].x;
-            const float4 P = pos[node];
-            const V step = xyz(d) * (1.0f / d.w);
-            pos[node] = withW(xyz(P) + step, P.w);
+    forEachItem(work, [&](uint32_t r) {
+        if (apply) {
+            const float4 d = delta[r];
+            if (d.w > 0.0f) {
+                const uint32_t node = surf[r].x;
+                const float4 P = pos[node];
+                const V step = xyz(d) * (1.0f / d.w);
+                pos[node] = withW(xyz(P) + step, P.w);
+            }
         }
-    }
-    if (key[r] != kIdle) count[key[r]] = 0;
+        if (key[r] != kIdle) count[key[r]] = 0;
+    });
 }
 
 // ------------------------------------------------------- node utilities --
@@ -707,7 +712,7 @@ cudaError_t launch(const LaunchCtx& ctx, void (*kernel)(KArgs...), uint32_t grid
 inline uint32_t blocks(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
 }  // namespace
 
-Span denseSpan(uint32_t count, uint32_t block) { return Span{Work{nullptr, count}, blocks(count, block), block}; }
+Span denseSpan(uint32_t count, uint32_t block) { return Span{Work{nullptr, 0, count}, blocks(count, block), block}; }
 
 // A colour pass of a small scene has too few cells to put a block of the
 // configured size on every SM; smaller blocks spread it over all of them.
@@ -766,8 +771,9 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& 
                     (const uint32_t*)s.start, (const uint32_t*)s.count, s.entries, (const uint4*)s.surf,
                     (const float4*)s.pos, s.sMeta, s.sPos, s.sRec)))
         return e;
-    // The gather runs over the bucket-ordered entries, one thread each.
-    const uint32_t cg = blocks(recordItems, 256);
+    // The gather runs over the bucket-ordered entries (at most recordItems),
+    // a thread each in turn.
+    const uint32_t cg = std::min(blocks(recordItems, 256), 16 * c.sms);
     auto collide = [&](auto kernel, uint32_t* out, uint32_t cap, unsigned long long* n) {
         return launch(c, kernel, cg, 256u, s.fp, recordItems, (const uint32_t*)s.entries, (const uint32_t*)s.cursor,
                       (const uint4*)s.surf, (const DevBody*)s.bodies, (const float4*)s.pos, (const float4*)s.prev,

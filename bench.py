@@ -442,7 +442,8 @@ def serving_sweep(quick: bool, seconds_per_point: float = 3.0, settle_frames: in
         next_arrival = t + rng.exponential(1 / lam)
         end = t + seconds_per_point
         stepped = []
-        c_before = server.stats()["cell_updates"]
+        st_before = server.stats()
+        c_before = st_before["cell_updates"]
         t_begin = t
         while True:
             now = server.clock()
@@ -462,6 +463,10 @@ def serving_sweep(quick: bool, seconds_per_point: float = 3.0, settle_frames: in
                 req_lat.append(total)
                 lat.append(total / c["frames"])
         elapsed = server.clock() - t_begin
+        st_after = server.stats()
+        ticks_run = max(1, st_after["ticks"] - st_before["ticks"])
+        tick_ms = {k: round(1e3 * (st_after[f"{k}_seconds"] - st_before[f"{k}_seconds"]) / ticks_run, 3)
+                   for k in ("tick", "prepare", "frame")}
         points.append({"load": frac, "offered_req_per_s": round(lam, 1),
                        "frame_latency_ms": {"p50": round(1e3 * float(np.percentile(lat, 50)), 3),
                                             "p99": round(1e3 * float(np.percentile(lat, 99)), 3)},
@@ -469,6 +474,7 @@ def serving_sweep(quick: bool, seconds_per_point: float = 3.0, settle_frames: in
                                               "p99": round(1e3 * float(np.percentile(req_lat, 99)), 3)},
                        "requests": len(lat),
                        "sessions_per_tick": round(float(np.mean(stepped)), 1) if stepped else 0,
+                       "mean_tick_ms": tick_ms,
                        "cell_updates_per_s": round((server.stats()["cell_updates"] - c_before) / elapsed)})
     st = server.stats()
     server.destroy()

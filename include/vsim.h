@@ -405,6 +405,9 @@ typedef struct vsim_server_stats {
     uint64_t session_frames;  /* frames run, summed over sessions */
     uint64_t cell_updates;    /* occupied cells x substeps, summed over frames run */
     uint32_t pending;         /* requests queued or running */
+    double tick_seconds;      /* wall time inside vsim_server_tick, summed */
+    double prepare_seconds;   /* of which host work before the frame's launch */
+    double frame_seconds;     /* device time of the frames (CUDA events), summed */
 } vsim_server_stats;
 
 int vsim_server_create(const vsim_body_desc* sessions, uint32_t count, const vsim_tank* tank,

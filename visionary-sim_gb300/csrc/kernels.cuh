@@ -78,6 +78,45 @@ __device__ __forceinline__ void forEachItem(const Work& w, F&& f) {
     }
 }
 
+// As forEachItem, with the kernel's programmatic-launch wait inside. pre(item)
+// may read only what no kernel of the frame writes -- the cell and record
+// tables, body constants, activity flags, the chunk table, all uploaded by
+// copies before the frame's first kernel -- and runs before the wait for the
+// thread's first item, so those loads overlap the previous kernel's tail;
+// body(item, pre(item)) runs after it.
+template <class Pre, class Body>
+__device__ __forceinline__ void forEachItemAfterWait(const Work& w, Pre&& pre, Body&& body) {
+    using P = decltype(pre(0u));
+    if (!w.table) {
+        const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+        const bool has = i < w.count;
+        P first{};
+        if (has) first = pre(i);
+        pdlWait();
+        pdlLaunchNext();
+        if (has) body(i, first);
+        return;
+    }
+    const uint2 d = w.table[w.span];
+    uint32_t c = blockIdx.x;
+    bool has = false;
+    uint32_t item = 0;
+    P first{};
+    if (c < d.y) {
+        const uint2 chunk = w.table[kSpans + d.x + c];
+        has = threadIdx.x < chunk.y;
+        item = chunk.x + threadIdx.x;
+        if (has) first = pre(item);
+    }
+    pdlWait();
+    pdlLaunchNext();
+    if (has) body(item, first);
+    for (c += gridDim.x; c < d.y; c += gridDim.x) {
+        const uint2 chunk = w.table[kSpans + d.x + c];
+        if (threadIdx.x < chunk.y) body(chunk.x + threadIdx.x, pre(chunk.x + threadIdx.x));
+    }
+}
+
 // As forEachItem, but every thread of the block calls f(has, item) the same
 // number of times (for block-wide scans); `has` says whether `item` is real.
 template <class F>

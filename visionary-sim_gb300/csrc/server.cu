@@ -62,8 +62,9 @@ struct vsim_server {
     std::vector<vsim_completion> completed;
     uint64_t ticks = 0, nextId = 1, sessionFrames = 0, cellUpdates = 0;
     uint32_t pending = 0;
+    double tickSeconds = 0, prepareSeconds = 0, frameSeconds = 0;
     std::chrono::steady_clock::time_point origin = std::chrono::steady_clock::now();
-    cudaEvent_t frameDone = nullptr;
+    cudaEvent_t frameStart = nullptr, frameDone = nullptr;
 };
 
 namespace {
@@ -86,6 +87,7 @@ int destroyServer(vsim_server* s) {
     if (s->sim) {
         DeviceGuard guard(s->sim->device);
         cudaStreamSynchronize(s->sim->stream);
+        if (s->frameStart) cudaEventDestroy(s->frameStart);
         if (s->frameDone) cudaEventDestroy(s->frameDone);
         freeSim(s->sim);
         delete s->sim;
@@ -162,7 +164,7 @@ int vsim_server_create(const vsim_body_desc* sessions, uint32_t count, const vsi
     s->queue.resize(s->admitted);
     s->held.assign(s->admitted, -1);
     s->prevTarget.assign(3 * size_t(s->admitted), 0.0);
-    if (cudaEventCreateWithFlags(&s->frameDone, cudaEventDisableTiming) != cudaSuccess) {
+    if (cudaEventCreate(&s->frameStart) != cudaSuccess || cudaEventCreate(&s->frameDone) != cudaSuccess) {
         destroyServer(s);
         return fail(VSIM_ERR_CUDA, "create event");
     }
@@ -212,6 +214,7 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
     vsim_sim* sim = s->sim;
     DeviceGuard guard(sim->device);
     const double frameDt = s->substeps * s->stepDuration;
+    const double entered = seconds(s);
 
     // The sessions this frame runs, and the nodes their drags hold.
     bool holdChanged = false;
@@ -272,10 +275,16 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
         if (sim->activeHost[i]) activeBodies.push_back(i);
     int rc = planBodies(sim, activeBodies);
     if (rc) return rc;
+    rc = syncParams(sim);
+    if (rc) return rc;
+    s->prepareSeconds += seconds(s) - entered;
+    CK(cudaEventRecord(s->frameStart, sim->stream), "serve frame");
     rc = runFrame(sim, s->substeps);
     if (rc) return rc;
     CK(cudaEventRecord(s->frameDone, sim->stream), "serve frame");
     CK(cudaEventSynchronize(s->frameDone), "serve frame");
+    float frameMs = 0;
+    if (cudaEventElapsedTime(&frameMs, s->frameStart, s->frameDone) == cudaSuccess) s->frameSeconds += 1e-3 * frameMs;
     const double now = seconds(s);
     for (uint32_t i = 0; i < s->admitted; i++) {
         if (!sim->activeHost[i]) continue;
@@ -291,6 +300,7 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
         }
     }
     s->ticks++;
+    s->tickSeconds += seconds(s) - entered;
     if (stepped) *stepped = active;
     return VSIM_OK;
 }
@@ -314,6 +324,9 @@ int vsim_server_get_stats(const vsim_server* s, vsim_server_stats* out) {
     out->session_frames = s->sessionFrames;
     out->cell_updates = s->cellUpdates;
     out->pending = s->pending;
+    out->tick_seconds = s->tickSeconds;
+    out->prepare_seconds = s->prepareSeconds;
+    out->frame_seconds = s->frameSeconds;
     return VSIM_OK;
 }
 

@@ -164,11 +164,13 @@ __device__ __forceinline__ void projectTet(V (&p)[8], const V (&prev)[8], const 
 __global__ void predictKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ active,
                               const uint32_t* __restrict__ activeBody, const uint32_t* __restrict__ bodyActive,
                               float4* __restrict__ pos, float4* __restrict__ prev, float4* __restrict__ vel) {
-    pdlWait();
-    pdlLaunchNext();
-    forEachItem(work, [&](uint32_t i) {
-        if (!bodyActive[activeBody[i]]) return;
-        const uint32_t n = active[i];
+    struct Pre {
+        uint32_t n, live;
+    };
+    auto pre = [&](uint32_t i) { return Pre{active[i], bodyActive[activeBody[i]]}; };
+    forEachItemAfterWait(work, pre, [&](uint32_t i, Pre q) {
+        if (!q.live) return;
+        const uint32_t n = q.n;
         const float4 P = pos[n];
         if (P.w == 0.0f) return;
         const float dt = fp->dt;
@@ -230,13 +232,21 @@ __global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ c
                                                      const DevBody* __restrict__ bodies,
                                                      const uint32_t* __restrict__ bodyActive, float4* __restrict__ pos,
                                                      const float4* __restrict__ prevState, StretchLengths lens) {
-    pdlWait();
-    pdlLaunchNext();
-    forEachItem(work, [&](uint32_t slot) {
+    struct Pre {
+        uint4 entry;
+        uint32_t live;
+        float maxStretch, alphaDev, alphaHyd, gamma, relax, restScale, h;
+    };
+    auto pre = [&](uint32_t slot) {
         const uint4 entry = cells[slot];
-        if (!bodyActive[entry.y]) return;
         const DevBody* b = bodies + entry.y;
-        const float maxStretch = b->maxStretch;
+        return Pre{entry, bodyActive[entry.y], b->maxStretch, b->alphaDev, b->alphaHyd, b->gamma, b->relax,
+                   b->restScale, b->h};
+    };
+    forEachItemAfterWait(work, pre, [&](uint32_t, const Pre& q) {
+        if (!q.live) return;
+        const uint4 entry = q.entry;
+        const float maxStretch = q.maxStretch;
         if (LIMIT_ONLY && !(maxStretch > 1.0f)) return;
         const uint32_t nx = entry.z, nxy = entry.w, n0 = entry.x;
         const uint32_t ids[8] = {n0,       n0 + 1,       n0 + nx,       n0 + nx + 1,
@@ -253,8 +263,8 @@ __global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ c
         for (int c = 0; c < 8; c++) prev[c] = xyz(prevState[ids[c]]);
 
         if (!LIMIT_ONLY) {
-            const float alphaDev = b->alphaDev, alphaHyd = b->alphaHyd, gamma = b->gamma, relax = b->relax;
-            const float s = b->restScale, ns = -s;
+            const float alphaDev = q.alphaDev, alphaHyd = q.alphaHyd, gamma = q.gamma, relax = q.relax;
+            const float s = q.restScale, ns = -s;
             projectTet<0>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
             projectTet<1>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
             projectTet<2>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
@@ -265,7 +275,7 @@ __global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ c
 
         // project.wgsl:162-179: unilateral length limit over all 28 corner pairs.
         if (maxStretch > 1.0f) {
-            const float h = b->h;
+            const float h = q.h;
             for (int sweep = 0; sweep < 2; sweep++) {
 #pragma unroll
                 for (int a = 0; a < 8; a++) {
@@ -317,16 +327,22 @@ __global__ void finalizeKernel(const FrameParams* __restrict__ fp, Work work, co
                                const int32_t* __restrict__ nodeRecord, const float4* __restrict__ delta,
                                const uint32_t* __restrict__ key, uint32_t* __restrict__ count,
                                uint32_t* __restrict__ cursor, const uint32_t* __restrict__ bodyActive) {
-    pdlWait();
-    pdlLaunchNext();
-    if (CONTACT && blockIdx.x == 0 && threadIdx.x == 0) *cursor = 0;
-    forEachItem(work, [&](uint32_t i) {
-        const uint32_t bodyIndex = activeBody[i];
-        if (!bodyActive[bodyIndex]) return;
+    struct Pre {
+        uint32_t n, live;
+        int32_t record;
+        float friction, damp;
+    };
+    auto pre = [&](uint32_t i) {
+        const uint32_t body = activeBody[i];
         const uint32_t n = active[i];
+        return Pre{n, bodyActive[body], CONTACT ? nodeRecord[n] : -1, bodies[body].friction, bodies[body].damp};
+    };
+    forEachItemAfterWait(work, pre, [&](uint32_t, const Pre& q) {
+        if (!q.live) return;
+        const uint32_t n = q.n;
         float4 P = pos[n];
         if (CONTACT) {
-            const int32_t r = nodeRecord[n];
+            const int32_t r = q.record;
             if (r >= 0) {
                 const float4 d = delta[r];
                 if (d.w > 0.0f) {
@@ -338,9 +354,8 @@ __global__ void finalizeKernel(const FrameParams* __restrict__ fp, Work work, co
             }
         }
         if (P.w == 0.0f) return;
-        const DevBody* b = bodies + bodyIndex;
         const V prev = xyz(prevState[n]);
-        const float fr = b->friction;
+        const float fr = q.friction;
         const V mn = mk(fp->tankMin[0], fp->tankMin[1], fp->tankMin[2]);
         const V mx = mk(fp->tankMax[0], fp->tankMax[1], fp->tankMax[2]);
         V p = xyz(P);
@@ -351,7 +366,7 @@ __global__ void finalizeKernel(const FrameParams* __restrict__ fp, Work work, co
         p = resolvePlane(p, prev, mk(0.0f, 0.0f, -1.0f), p.z - mx.z, fr);
         const float dt = fp->dt;
         V v = (p - prev) / dt;
-        v = v * b->damp;
+        v = v * q.damp;
         if (PREDICT) {
             const V g = mk(fp->gx, fp->gy, fp->gz);
             const V v2 = v + g * dt;
@@ -363,6 +378,8 @@ __global__ void finalizeKernel(const FrameParams* __restrict__ fp, Work work, co
             vel[n] = withW(v, 0.0f);
         }
     });
+    // After the wait (inside the loop above): the gather has read it.
+    if (CONTACT && blockIdx.x == 0 && threadIdx.x == 0) *cursor = 0;
 }
 
 // ------------------------------------------------------------- contact --
@@ -394,11 +411,17 @@ __global__ void binKernel(const FrameParams* __restrict__ fp, Work work, const u
                           const DevBody* __restrict__ bodies, const uint32_t* __restrict__ bodyActive,
                           const float4* __restrict__ pos, uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
                           uint32_t* __restrict__ count) {
-    pdlWait();
-    pdlLaunchNext();
-    forEachItem(work, [&](uint32_t r) {
+    struct Pre {
+        uint4 rec;
+        uint32_t live;
+    };
+    auto pre = [&](uint32_t r) {
         const uint4 rec = surf[r];
-        if (!bodyActive[rec.y]) {
+        return Pre{rec, bodyActive[rec.y]};
+    };
+    forEachItemAfterWait(work, pre, [&](uint32_t r, const Pre& q) {
+        const uint4 rec = q.rec;
+        if (!q.live) {
             key[r] = kIdle;
             rank[r] = kIdle;
             return;

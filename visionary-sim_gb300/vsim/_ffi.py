@@ -127,7 +127,8 @@ class Completion(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("sessions", C.c_uint32), ("rejected", C.c_uint32), ("resident_bytes", C.c_double),
                 ("ticks", C.c_uint64), ("session_frames", C.c_uint64), ("cell_updates", C.c_uint64),
-                ("pending", C.c_uint32)]
+                ("pending", C.c_uint32), ("tick_seconds", C.c_double), ("prepare_seconds", C.c_double),
+                ("frame_seconds", C.c_double)]
 
 
 VSIM_CREATE_ISOLATED = 1

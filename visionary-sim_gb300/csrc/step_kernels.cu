@@ -560,13 +560,16 @@ __device__ __forceinline__ bool admitted(uint4 a, uint4 b, uint32_t selfContact)
 // (r, other) is also appended to `pairs` (capacity-checked), for the
 // pair-set checks.
 //
-// Threads take the records in bucket order (`entries`, the counting sort's
-// output, `*cursor` entries long) rather than in record order: the records
-// of one bucket sit in neighbouring lanes and scan the same 27 neighbour
-// runs, so a warp's candidate loads coincide and its lanes run loops of the
-// same length. Each record's hits are still summed in the reference's
-// order (neighbour buckets dz, dy, dx; entries in bucket order), so the
-// result does not depend on which thread computes it.
+// One warp per record. The record's candidates -- the visible entries of
+// its 27 neighbour buckets, concatenated in the reference's order (buckets
+// dz, dy, dx; entries in bucket order) -- are dealt to the lanes 32 at a
+// time: lane q < 27 first sizes neighbour bucket q, a warp scan turns the
+// sizes into offsets, and each lane finds its candidate's bucket by binary
+// search over them. Every lane tests its candidate and does the hit
+// arithmetic for it; the hits are then added to the record's sum one by one
+// in lane order, which is candidate order, so the sum is the sequential
+// one. Warps take the records in bucket order (`entries`, the counting
+// sort's output, `*cursor` long), so neighbouring warps read the same runs.
 template <bool EMIT>
 __global__ void __launch_bounds__(256) collideKernel(
     const FrameParams* __restrict__ fp, uint32_t items, const uint32_t* __restrict__ entries,
@@ -577,8 +580,12 @@ __global__ void __launch_bounds__(256) collideKernel(
     unsigned long long* __restrict__ pairCount) {
     pdlWait();
     pdlLaunchNext();
+    constexpr unsigned kAll = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t total = min(items, *cursor);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const uint32_t selfContact = fp->selfContact;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < total; i += warps) {
         const uint32_t r = entries[i];
         const uint4 me = surf[r];
         const DevBody* grid = bodies + me.y;
@@ -589,74 +596,95 @@ __global__ void __launch_bounds__(256) collideKernel(
         const V pi = xyz(P);
         const V movedI = pi - xyz(prevState[node]);
         const float frictionI = grid->friction;
-        const uint32_t selfContact = fp->selfContact;
         int centre[3];
         bucketOf(grid, pi, centre);
-        const int dims[3] = {int(grid->gridDims[0]), int(grid->gridDims[1]), int(grid->gridDims[2])};
-        const uint32_t base = grid->gridBase;
-        auto bucketAt = [&](int q, bool& inside) {
-            const int x = centre[0] + q % 3 - 1, y = centre[1] + (q / 3) % 3 - 1, z = centre[2] + q / 9 - 1;
-            inside = x >= 0 && x < dims[0] && y >= 0 && y < dims[1] && z >= 0 && z < dims[2];
-            return base + uint32_t(x) + uint32_t(dims[0]) * (uint32_t(y) + uint32_t(dims[1]) * uint32_t(z));
-        };
-        // Which of the 27 neighbour buckets hold entries: 27 independent loads.
-        uint32_t live = 0;
-#pragma unroll
-        for (int q = 0; q < 27; q++) {
-            bool inside;
-            const uint32_t b = bucketAt(q, inside);
-            if (inside && count[b] != 0) live |= 1u << q;
+        // Lane q sizes neighbour bucket q (q = dx + 3 dy + 9 dz, offsets + 1).
+        uint32_t held = 0, first = 0;
+        if (lane < 27) {
+            const int x = centre[0] + int(lane % 3) - 1, y = centre[1] + int((lane / 3) % 3) - 1,
+                      z = centre[2] + int(lane / 9) - 1;
+            const int dims[3] = {int(grid->gridDims[0]), int(grid->gridDims[1]), int(grid->gridDims[2])};
+            if (x >= 0 && x < dims[0] && y >= 0 && y < dims[1] && z >= 0 && z < dims[2]) {
+                const uint32_t b =
+                    grid->gridBase + uint32_t(x) + uint32_t(dims[0]) * (uint32_t(y) + uint32_t(dims[1]) * uint32_t(z));
+                const uint32_t n = count[b];
+                held = n < kBucketSlots ? n : kBucketSlots;
+                if (held) first = start[b];
+            }
         }
+        // Inclusive prefix of the run lengths: lane q's run is [end - held, end).
+        uint32_t end = held;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(kAll, end, d);
+            if (lane >= uint32_t(d)) end += v;
+        }
+        const uint32_t candidates = __shfl_sync(kAll, end, 31);
         V sum = mk(0.0f, 0.0f, 0.0f);
         float hits = 0.0f;
-        // The runs in the reference's dz, dy, dx order (ascending q).
-        while (live) {
-            const int q = __ffs(live) - 1;
-            live &= live - 1;
-            bool inside;
-            const uint32_t b = bucketAt(q, inside);
-            const uint32_t n = count[b];
-            const uint32_t held = n < kBucketSlots ? n : kBucketSlots;
-            const uint32_t at = start[b];
-            for (uint32_t k = 0; k < held; k++) {
-                const uint4 them = sMeta[at + k];
-                const float4 Q = sPos[at + k];
-                if (!admitted(me, them, selfContact)) continue;
-                const uint32_t mate = them.x;
+        for (uint32_t round = 0; round < candidates; round += 32) {
+            const uint32_t c = round + lane;
+            // The run holding candidate c: the first lane whose end exceeds c.
+            uint32_t lo = 0, hi = 26;
+#pragma unroll
+            for (int step = 0; step < 5; step++) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (__shfl_sync(kAll, end, mid) > c) hi = mid;
+                else lo = mid + 1;
+            }
+            const uint32_t runEnd = __shfl_sync(kAll, end, lo);
+            const uint32_t runHeld = __shfl_sync(kAll, held, lo);
+            const uint32_t runFirst = __shfl_sync(kAll, first, lo);
+            const uint32_t at = runFirst + (c - (runEnd - runHeld));
+            bool hit = false;
+            V correction = mk(0.0f, 0.0f, 0.0f);
+            if (c < candidates) {
+                const uint4 them = sMeta[at];
+                const float4 Q = sPos[at];
                 const V pj = xyz(Q);
                 const V d = pi - pj;
                 const float dist2 = dot(d, d);
                 const float reach = radius + __uint_as_float(them.w);
-                if (dist2 >= reach * reach) continue;
                 const float wj = Q.w;
-                const float total = wi + wj;
-                if (total <= 0.0f) continue;
-                const float share = wi / total;
-                const float dist = sqrtf(dist2);
-                V normal = mk(0.0f, node < mate ? 1.0f : -1.0f, 0.0f);
-                if (dist > 1e-9f) normal = d / dist;
-                const float depth = reach - dist;
-                V correction = normal * (depth * share);
-                const V sliding = movedI - (pj - xyz(prevState[mate]));
-                const V tangent = sliding - normal * dot(sliding, normal);
-                const float slid = length(tangent);
-                if (slid > 1e-9f) {
-                    const float mu = fminf(frictionI, bodies[them.y].friction);
-                    correction = correction - tangent * (share * fminf(1.0f, mu * depth / slid));
-                }
-                sum = sum + correction;
-                hits = hits + 1.0f;
-                if (EMIT) {
-                    const uint32_t other = sRec[at + k];
-                    const unsigned long long slot = atomicAdd(pairCount, 1ull);
-                    if (slot < capacity) {
-                        pairs[2 * slot] = r;
-                        pairs[2 * slot + 1] = other;
+                const float sumW = wi + wj;
+                // The reference's three skips, as written (a NaN distance is not skipped).
+                if (admitted(me, them, selfContact) && !(dist2 >= reach * reach) && !(sumW <= 0.0f)) {
+                    hit = true;
+                    const uint32_t mate = them.x;
+                    const float share = wi / sumW;
+                    const float dist = sqrtf(dist2);
+                    V normal = mk(0.0f, node < mate ? 1.0f : -1.0f, 0.0f);
+                    if (dist > 1e-9f) normal = d / dist;
+                    const float depth = reach - dist;
+                    correction = normal * (depth * share);
+                    const V sliding = movedI - (pj - xyz(prevState[mate]));
+                    const V tangent = sliding - normal * dot(sliding, normal);
+                    const float slid = length(tangent);
+                    if (slid > 1e-9f) {
+                        const float mu = fminf(frictionI, bodies[them.y].friction);
+                        correction = correction - tangent * (share * fminf(1.0f, mu * depth / slid));
+                    }
+                    if (EMIT) {
+                        const unsigned long long slot = atomicAdd(pairCount, 1ull);
+                        if (slot < capacity) {
+                            pairs[2 * slot] = r;
+                            pairs[2 * slot + 1] = sRec[at];
+                        }
                     }
                 }
             }
+            // Candidate order = lane order.
+            uint32_t mask = __ballot_sync(kAll, hit);
+            while (mask) {
+                const int l = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const V add = mk(__shfl_sync(kAll, correction.x, l), __shfl_sync(kAll, correction.y, l),
+                                 __shfl_sync(kAll, correction.z, l));
+                sum = sum + add;
+                hits = hits + 1.0f;
+            }
         }
-        if (!EMIT) delta[r] = withW(sum, hits);
+        if (!EMIT && lane == 0) delta[r] = withW(sum, hits);
     }
 }
 
@@ -795,8 +823,8 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& 
                     (const float4*)s.pos, s.sMeta, s.sPos, s.sRec)))
         return e;
     // The gather runs over the bucket-ordered entries (at most recordItems),
-    // a thread each in turn.
-    const uint32_t cg = std::min(blocks(recordItems, 256), 16 * c.sms);
+    // a warp each in turn.
+    const uint32_t cg = std::min(blocks(recordItems, 8), 64 * c.sms);
     auto collide = [&](auto kernel, uint32_t* out, uint32_t cap, unsigned long long* n) {
         return launch(c, kernel, cg, 256u, s.fp, recordItems, (const uint32_t*)s.entries, (const uint32_t*)s.cursor,
                       (const uint4*)s.surf, (const DevBody*)s.bodies, (const float4*)s.pos, (const float4*)s.prev,

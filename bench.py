@@ -501,6 +501,11 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
     ap.add_argument("--stress-only", action="store_true", help="only the stress workload's frames (for captures)")
+    ap.add_argument("--capture-after", type=int, default=None, metavar="N",
+                    help="profiler capture mode: run N frames of the bench workload, then bracket one more frame "
+                         "(or --capture-substeps substeps) with cudaProfilerStart/Stop for "
+                         "`ncu --profile-from-start off`, and exit")
+    ap.add_argument("--capture-substeps", type=int, default=None)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -539,6 +544,20 @@ def main():
     torch.cuda.set_device(local)
     if args.stress_only:
         print(json.dumps({"stress": stress(args.quick, peaks()[0], frames=args.steps)}))
+        return
+    if args.capture_after is not None:
+        sim = Simulator(scene)
+        for _ in range(args.capture_after):
+            run_frame(sim, scene)
+        sim.synchronize()
+        torch.cuda.profiler.start()
+        if args.capture_substeps:
+            sim.dispatch(args.capture_substeps)
+        else:
+            run_frame(sim, scene)
+        sim.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"captured_after_frames": args.capture_after, "substeps": args.capture_substeps}))
         return
     if world > 1:
         import torch.distributed as dist

@@ -485,6 +485,24 @@ __global__ void scatterKernel(const FrameParams* __restrict__ fp, Work work, con
     });
 }
 
+// Buckets of at most this many entries are ordered in registers.
+constexpr uint32_t kSmallBucket = 8;
+
+// Ascending sort of eight keys: a 19-comparator network.
+__device__ __forceinline__ void sortSmall(uint32_t (&v)[kSmallBucket]) {
+    auto cx = [&](int a, int b) {
+        const uint32_t lo = min(v[a], v[b]), hi = max(v[a], v[b]);
+        v[a] = lo;
+        v[b] = hi;
+    };
+    cx(0, 2), cx(1, 3), cx(4, 6), cx(5, 7);
+    cx(0, 4), cx(1, 5), cx(2, 6), cx(3, 7);
+    cx(0, 1), cx(2, 3), cx(4, 5), cx(6, 7);
+    cx(2, 4), cx(3, 5);
+    cx(1, 4), cx(3, 6);
+    cx(1, 2), cx(3, 4), cx(5, 6);
+}
+
 // sort.wgsl:14-53: the bucket's visible entries -- its kBucketSlots lowest
 // record indices -- in ascending order at the front of its segment; then
 // their records and positions copied out in that order, so the gather reads
@@ -497,17 +515,30 @@ __global__ void canonKernel(const FrameParams* __restrict__ fp, Work work, const
     pdlWait();
     pdlLaunchNext();
     forEachItem(work, [&](uint32_t r) {
-        if (rank[r] != 0) return;
-        const uint32_t b = key[r];
+        const uint32_t first = rank[r], b = key[r];
+        if (first != 0) return;
         const uint32_t n = count[b];
         const uint32_t base = start[b];
         uint32_t* e = entries + base;
         const uint32_t m = n < kBucketSlots ? n : kBucketSlots;
-        if (n < 2) {
-            const uint4 rec = surf[r];
-            sMeta[base] = rec;
-            sPos[base] = pos[rec.x];
-            sRec[base] = r;
+        if (n <= kSmallBucket) {
+            // In registers: all loads of a step issued together.
+            uint32_t v[kSmallBucket];
+#pragma unroll
+            for (uint32_t k = 0; k < kSmallBucket; k++) v[k] = k < n ? e[k] : 0xffffffffu;
+            sortSmall(v);
+            uint4 rec[kSmallBucket];
+#pragma unroll
+            for (uint32_t k = 0; k < kSmallBucket; k++)
+                if (k < n) rec[k] = surf[v[k]];
+#pragma unroll
+            for (uint32_t k = 0; k < kSmallBucket; k++)
+                if (k < n) {
+                    e[k] = v[k];
+                    sMeta[base + k] = rec[k];
+                    sPos[base + k] = pos[rec[k].x];
+                    sRec[base + k] = v[k];
+                }
             return;
         }
         for (uint32_t i = 1; i < m; i++) {

@@ -252,6 +252,16 @@ int vsim_tune(vsim_sim* sim, uint32_t frames, uint32_t* block, uint32_t* brick);
    on): the next kernel's launch overlaps the tail of the one before it. */
 int vsim_set_pdl(vsim_sim* sim, int enabled);
 
+/* How the contact gather maps surface records to GPU threads: AUTO (default)
+   gives each record a warp while the substep has fewer than 2048 records
+   per SM and a thread otherwise; WARP and THREAD force one mapping. All three
+   give the same results (each record's hits are summed in the reference's
+   order); the setting exists for tests and sweeps. No reference counterpart. */
+#define VSIM_GATHER_AUTO 0
+#define VSIM_GATHER_WARP 1
+#define VSIM_GATHER_THREAD 2
+int vsim_set_gather_mapping(vsim_sim* sim, int mapping);
+
 /* ---- readout ---------------------------------------------------------- */
 
 /* The six Kuhn rest shape inverses of the unit cube the kernels use,

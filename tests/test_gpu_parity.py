@@ -97,6 +97,26 @@ def test_blob_contact_self_contact(lib):
     assert sim.read_positions()[:, 1].min() > -0.01  # the ground held
 
 
+@pytest.mark.parametrize("mapping", ["warp", "thread"])
+def test_gather_mappings_agree(lib, mapping):
+    """Both record-to-thread mappings of the contact gather give the oracle's
+    result, on a state squeezed into heavy self contact."""
+    import vsim.scenes as sc
+
+    scene = sc.noise_blob(n=20, seed=5, splats=0)
+    sim, orc = make(scene)
+    sim.set_gather_mapping(mapping)
+    pos, prev, vel = orc.state()
+    squashed = squeeze(pos, scene, 0.5)
+    sim.write_state(squashed, pos, vel)
+    orc.set_state(squashed, pos, vel)
+    assert np.array_equal(sim.contact_pairs(), orc.contact_pairs())
+    for frame in range(3):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"{mapping} frame {frame}")
+
+
 def squeeze(pos, scene, factor=0.6):
     """A shared state with overlapping surfaces: every body squashed toward
     its own bottom plane."""

@@ -169,9 +169,10 @@ cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4*
 cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span& nodes, bool contact,
                            bool predictNext);
 // `records` covers the surface records of the stepped bodies; at most
-// `recordItems` of them are binned.
+// `recordItems` of them are binned. `mapping` is a VSIM_GATHER_* value.
 cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& records, uint32_t recordItems,
-                          ContactMode mode, uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount);
+                          int mapping, ContactMode mode, uint32_t* pairs, uint32_t capacity,
+                          unsigned long long* pairCount);
 cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos);
 cudaError_t launchZeroW(cudaStream_t st, const uint32_t* nodes, uint32_t n, float4* pos);
 cudaError_t launchRefreshW(cudaStream_t st, uint32_t first, uint32_t n, const float* base, float4* pos);

@@ -307,7 +307,7 @@ cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMod
                 }
         if (contact && plan.records.grid) {
             begin(VSIM_KIND_CONTACT, kContactKernels);
-            if ((e = launchContact(c, s->d, plan.records, s->surfaceCount, mode, nullptr, 0, nullptr))) return e;
+            if ((e = launchContact(c, s->d, plan.records, s->surfaceCount, s->gatherMapping, mode, nullptr, 0, nullptr))) return e;
             end();
         }
         begin(VSIM_KIND_FINALIZE, 1);
@@ -327,6 +327,7 @@ uint64_t graphKey(const vsim_sim* s, uint32_t steps) {
     k = k * 1031 + s->block;
     k = k * 31 + (s->pdl ? 1 : 0);
     k = k * 31 + (s->plan.chunked ? 1 : 0);
+    k = k * 31 + uint64_t(s->gatherMapping);
     return k;
 }
 
@@ -1098,7 +1099,7 @@ int vsim_contact_pairs(vsim_sim* s, uint32_t* pairs, size_t capacity, size_t* co
     if (rc) return rc;
     CK(cudaMemsetAsync(s->pairCount, 0, sizeof(unsigned long long), s->stream), "count pairs");
     const LaunchCtx c{s->stream, false, s->sms};
-    CK(launchContact(c, s->d, s->dense.records, s->surfaceCount, ContactMode::Pairs, s->pairs,
+    CK(launchContact(c, s->d, s->dense.records, s->surfaceCount, s->gatherMapping, ContactMode::Pairs, s->pairs,
                      uint32_t(capacity), s->pairCount),
        "list pairs");
     unsigned long long total = 0;
@@ -1131,6 +1132,14 @@ int vsim_kuhn_rest_inverse(float out[54]) {
 int vsim_set_pdl(vsim_sim* s, int enabled) {
     SIM_GUARD(s);
     s->pdl = enabled != 0;
+    return VSIM_OK;
+}
+
+int vsim_set_gather_mapping(vsim_sim* s, int mapping) {
+    SIM_GUARD(s);
+    if (mapping != VSIM_GATHER_AUTO && mapping != VSIM_GATHER_WARP && mapping != VSIM_GATHER_THREAD)
+        return fail(VSIM_ERR_RANGE, "gather mapping must be VSIM_GATHER_AUTO, _WARP or _THREAD");
+    s->gatherMapping = mapping;
     return VSIM_OK;
 }
 

@@ -88,6 +88,7 @@ struct vsim_sim {
     bool contact = true, selfContact = false;
     uint32_t iterations = 1;
     bool useGraph = true, pdl = true;
+    int gatherMapping = VSIM_GATHER_AUTO;
     uint32_t block = 256, brick = 0;
     vsim::Clock clock;
     bool stepOverridden = false;

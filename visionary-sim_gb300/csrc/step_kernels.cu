@@ -591,19 +591,68 @@ __device__ __forceinline__ bool admitted(uint4 a, uint4 b, uint32_t selfContact)
 // (r, other) is also appended to `pairs` (capacity-checked), for the
 // pair-set checks.
 //
-// One warp per record. The record's candidates -- the visible entries of
-// its 27 neighbour buckets, concatenated in the reference's order (buckets
-// dz, dy, dx; entries in bucket order) -- are dealt to the lanes 32 at a
-// time: lane q < 27 first sizes neighbour bucket q, a warp scan turns the
-// sizes into offsets, and each lane finds its candidate's bucket by binary
-// search over them. Every lane tests its candidate and does the hit
-// arithmetic for it; the hits are then added to the record's sum one by one
-// in lane order, which is candidate order, so the sum is the sequential
-// one. Warps take the records in bucket order (`entries`, the counting
-// sort's output, `*cursor` long), so neighbouring warps read the same runs.
+// Records are taken in bucket order (`entries`, the counting sort's output,
+// `*cursor` long), so neighbouring records read the same runs. Two mappings
+// of records to threads, chosen per launch from the number of records:
+//
+// - few records (below `warpModeBelow`): one warp per record. The record's
+//   candidates -- the visible entries of its 27 neighbour buckets,
+//   concatenated in the reference's order (buckets dz, dy, dx; entries in
+//   bucket order) -- are dealt to the lanes 32 at a time: lane q < 27 sizes
+//   neighbour bucket q, a warp scan turns the sizes into offsets, and each
+//   lane finds its candidate's run by binary search. The record's chain of
+//   dependent candidate loads is spread over 32 lanes, which is what a
+//   launch too small to fill the GPU needs;
+// - many records: one thread per record, scanning the runs itself, which
+//   costs fewer instructions per record once the GPU is full anyway.
+//
+// Either way each record's hits are added to its sum one at a time in
+// candidate order, so both give the sequential result.
+
+struct Contactor {
+    uint4 me;
+    V pi, movedI;
+    float radius, wi, frictionI;
+    uint32_t node;
+};
+
+// The per-hit arithmetic of collide.wgsl:70-118 for a candidate that passed
+// the three skips; returns the correction to add.
+__device__ __forceinline__ V contactCorrection(const Contactor& c, uint4 them, float4 Q, float dist2,
+                                               const float4* __restrict__ prevState,
+                                               const DevBody* __restrict__ bodies) {
+    const uint32_t mate = them.x;
+    const V pj = xyz(Q);
+    const V d = c.pi - pj;
+    const float reach = c.radius + __uint_as_float(them.w);
+    const float share = c.wi / (c.wi + Q.w);
+    const float dist = sqrtf(dist2);
+    V normal = mk(0.0f, c.node < mate ? 1.0f : -1.0f, 0.0f);
+    if (dist > 1e-9f) normal = d / dist;
+    const float depth = reach - dist;
+    V correction = normal * (depth * share);
+    const V sliding = c.movedI - (pj - xyz(prevState[mate]));
+    const V tangent = sliding - normal * dot(sliding, normal);
+    const float slid = length(tangent);
+    if (slid > 1e-9f) {
+        const float mu = fminf(c.frictionI, bodies[them.y].friction);
+        correction = correction - tangent * (share * fminf(1.0f, mu * depth / slid));
+    }
+    return correction;
+}
+
+// The reference's three skips, as written (a NaN distance is not skipped).
+__device__ __forceinline__ bool contactHit(const Contactor& c, uint4 them, float4 Q, uint32_t selfContact,
+                                           float& dist2) {
+    const V d = c.pi - xyz(Q);
+    dist2 = dot(d, d);
+    const float reach = c.radius + __uint_as_float(them.w);
+    return admitted(c.me, them, selfContact) && !(dist2 >= reach * reach) && !(c.wi + Q.w <= 0.0f);
+}
+
 template <bool EMIT>
 __global__ void __launch_bounds__(256) collideKernel(
-    const FrameParams* __restrict__ fp, uint32_t items, const uint32_t* __restrict__ entries,
+    const FrameParams* __restrict__ fp, uint32_t items, uint32_t warpModeBelow, const uint32_t* __restrict__ entries,
     const uint32_t* __restrict__ cursor, const uint4* __restrict__ surf, const DevBody* __restrict__ bodies,
     const float4* __restrict__ pos, const float4* __restrict__ prevState, const uint32_t* __restrict__ start,
     const uint32_t* __restrict__ count, const uint4* __restrict__ sMeta, const float4* __restrict__ sPos,
@@ -612,32 +661,87 @@ __global__ void __launch_bounds__(256) collideKernel(
     pdlWait();
     pdlLaunchNext();
     constexpr unsigned kAll = 0xffffffffu;
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t total = min(items, *cursor);
     const uint32_t selfContact = fp->selfContact;
-    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < total; i += warps) {
+    const uint32_t thread = blockIdx.x * blockDim.x + threadIdx.x;
+    auto setup = [&](uint32_t r, int centre[3]) {
+        Contactor c;
+        c.me = surf[r];
+        c.node = c.me.x;
+        c.radius = __uint_as_float(c.me.w);
+        const float4 P = pos[c.node];
+        c.wi = P.w;
+        c.pi = xyz(P);
+        c.movedI = c.pi - xyz(prevState[c.node]);
+        c.frictionI = bodies[c.me.y].friction;
+        bucketOf(bodies + c.me.y, c.pi, centre);
+        return c;
+    };
+    // Neighbour bucket q of the record's bucket (q = dx + 3 dy + 9 dz, offsets + 1).
+    auto neighbour = [&](const DevBody* grid, const int centre[3], int q, bool& inside) {
+        const int x = centre[0] + q % 3 - 1, y = centre[1] + (q / 3) % 3 - 1, z = centre[2] + q / 9 - 1;
+        const int dims[3] = {int(grid->gridDims[0]), int(grid->gridDims[1]), int(grid->gridDims[2])};
+        inside = x >= 0 && x < dims[0] && y >= 0 && y < dims[1] && z >= 0 && z < dims[2];
+        return grid->gridBase + uint32_t(x) + uint32_t(dims[0]) * (uint32_t(y) + uint32_t(dims[1]) * uint32_t(z));
+    };
+    auto emit = [&](uint32_t r, uint32_t at) {
+        const unsigned long long slot = atomicAdd(pairCount, 1ull);
+        if (slot < capacity) {
+            pairs[2 * slot] = r;
+            pairs[2 * slot + 1] = sRec[at];
+        }
+    };
+
+    if (total >= warpModeBelow) {
+        for (uint32_t i = thread; i < total; i += gridDim.x * blockDim.x) {
+            const uint32_t r = entries[i];
+            int centre[3];
+            const Contactor c = setup(r, centre);
+            const DevBody* grid = bodies + c.me.y;
+            uint32_t live = 0;  // which neighbour buckets hold entries: 27 independent loads
+#pragma unroll
+            for (int q = 0; q < 27; q++) {
+                bool inside;
+                const uint32_t b = neighbour(grid, centre, q, inside);
+                if (inside && count[b] != 0) live |= 1u << q;
+            }
+            V sum = mk(0.0f, 0.0f, 0.0f);
+            float hits = 0.0f;
+            while (live) {
+                const int q = __ffs(live) - 1;
+                live &= live - 1;
+                bool inside;
+                const uint32_t b = neighbour(grid, centre, q, inside);
+                const uint32_t n = count[b];
+                const uint32_t held = n < kBucketSlots ? n : kBucketSlots;
+                const uint32_t at = start[b];
+                for (uint32_t k = 0; k < held; k++) {
+                    const uint4 them = sMeta[at + k];
+                    const float4 Q = sPos[at + k];
+                    float dist2;
+                    if (!contactHit(c, them, Q, selfContact, dist2)) continue;
+                    sum = sum + contactCorrection(c, them, Q, dist2, prevState, bodies);
+                    hits = hits + 1.0f;
+                    if (EMIT) emit(r, at + k);
+                }
+            }
+            if (!EMIT) delta[r] = withW(sum, hits);
+        }
+        return;
+    }
+
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = thread >> 5; i < total; i += warps) {
         const uint32_t r = entries[i];
-        const uint4 me = surf[r];
-        const DevBody* grid = bodies + me.y;
-        const uint32_t node = me.x;
-        const float radius = __uint_as_float(me.w);
-        const float4 P = pos[node];
-        const float wi = P.w;
-        const V pi = xyz(P);
-        const V movedI = pi - xyz(prevState[node]);
-        const float frictionI = grid->friction;
         int centre[3];
-        bucketOf(grid, pi, centre);
-        // Lane q sizes neighbour bucket q (q = dx + 3 dy + 9 dz, offsets + 1).
+        const Contactor c = setup(r, centre);
+        const DevBody* grid = bodies + c.me.y;
         uint32_t held = 0, first = 0;
         if (lane < 27) {
-            const int x = centre[0] + int(lane % 3) - 1, y = centre[1] + int((lane / 3) % 3) - 1,
-                      z = centre[2] + int(lane / 9) - 1;
-            const int dims[3] = {int(grid->gridDims[0]), int(grid->gridDims[1]), int(grid->gridDims[2])};
-            if (x >= 0 && x < dims[0] && y >= 0 && y < dims[1] && z >= 0 && z < dims[2]) {
-                const uint32_t b =
-                    grid->gridBase + uint32_t(x) + uint32_t(dims[0]) * (uint32_t(y) + uint32_t(dims[1]) * uint32_t(z));
+            bool inside;
+            const uint32_t b = neighbour(grid, centre, int(lane), inside);
+            if (inside) {
                 const uint32_t n = count[b];
                 held = n < kBucketSlots ? n : kBucketSlots;
                 if (held) first = start[b];
@@ -654,54 +758,29 @@ __global__ void __launch_bounds__(256) collideKernel(
         V sum = mk(0.0f, 0.0f, 0.0f);
         float hits = 0.0f;
         for (uint32_t round = 0; round < candidates; round += 32) {
-            const uint32_t c = round + lane;
-            // The run holding candidate c: the first lane whose end exceeds c.
+            const uint32_t cand = round + lane;
+            // The run holding the candidate: the first lane whose end exceeds it.
             uint32_t lo = 0, hi = 26;
 #pragma unroll
             for (int step = 0; step < 5; step++) {
                 const uint32_t mid = (lo + hi) >> 1;
-                if (__shfl_sync(kAll, end, mid) > c) hi = mid;
+                if (__shfl_sync(kAll, end, mid) > cand) hi = mid;
                 else lo = mid + 1;
             }
             const uint32_t runEnd = __shfl_sync(kAll, end, lo);
             const uint32_t runHeld = __shfl_sync(kAll, held, lo);
             const uint32_t runFirst = __shfl_sync(kAll, first, lo);
-            const uint32_t at = runFirst + (c - (runEnd - runHeld));
+            const uint32_t at = runFirst + (cand - (runEnd - runHeld));
             bool hit = false;
             V correction = mk(0.0f, 0.0f, 0.0f);
-            if (c < candidates) {
+            if (cand < candidates) {
                 const uint4 them = sMeta[at];
                 const float4 Q = sPos[at];
-                const V pj = xyz(Q);
-                const V d = pi - pj;
-                const float dist2 = dot(d, d);
-                const float reach = radius + __uint_as_float(them.w);
-                const float wj = Q.w;
-                const float sumW = wi + wj;
-                // The reference's three skips, as written (a NaN distance is not skipped).
-                if (admitted(me, them, selfContact) && !(dist2 >= reach * reach) && !(sumW <= 0.0f)) {
+                float dist2;
+                if (contactHit(c, them, Q, selfContact, dist2)) {
                     hit = true;
-                    const uint32_t mate = them.x;
-                    const float share = wi / sumW;
-                    const float dist = sqrtf(dist2);
-                    V normal = mk(0.0f, node < mate ? 1.0f : -1.0f, 0.0f);
-                    if (dist > 1e-9f) normal = d / dist;
-                    const float depth = reach - dist;
-                    correction = normal * (depth * share);
-                    const V sliding = movedI - (pj - xyz(prevState[mate]));
-                    const V tangent = sliding - normal * dot(sliding, normal);
-                    const float slid = length(tangent);
-                    if (slid > 1e-9f) {
-                        const float mu = fminf(frictionI, bodies[them.y].friction);
-                        correction = correction - tangent * (share * fminf(1.0f, mu * depth / slid));
-                    }
-                    if (EMIT) {
-                        const unsigned long long slot = atomicAdd(pairCount, 1ull);
-                        if (slot < capacity) {
-                            pairs[2 * slot] = r;
-                            pairs[2 * slot + 1] = sRec[at];
-                        }
-                    }
+                    correction = contactCorrection(c, them, Q, dist2, prevState, bodies);
+                    if (EMIT) emit(r, at);
                 }
             }
             // Candidate order = lane order.
@@ -836,7 +915,8 @@ cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span&
 // applies them and empties the grid; Pairs mode lists the hits and empties
 // the grid itself.
 cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& r, uint32_t recordItems,
-                          ContactMode mode, uint32_t* pairs, uint32_t capacity, unsigned long long* pairCount) {
+                          int mapping, ContactMode mode, uint32_t* pairs, uint32_t capacity,
+                          unsigned long long* pairCount) {
     const uint32_t g = r.grid, b = r.block;
     const Work w = r.work;
     cudaError_t e;
@@ -854,10 +934,14 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& 
                     (const float4*)s.pos, s.sMeta, s.sPos, s.sRec)))
         return e;
     // The gather runs over the bucket-ordered entries (at most recordItems),
-    // a warp each in turn.
+    // a warp each while fewer than 2048 per SM, else a thread each.
     const uint32_t cg = std::min(blocks(recordItems, 8), 64 * c.sms);
+    const uint32_t warpModeBelow = mapping == VSIM_GATHER_WARP     ? 0xffffffffu
+                                   : mapping == VSIM_GATHER_THREAD ? 0u
+                                                                   : 2048 * c.sms;
     auto collide = [&](auto kernel, uint32_t* out, uint32_t cap, unsigned long long* n) {
-        return launch(c, kernel, cg, 256u, s.fp, recordItems, (const uint32_t*)s.entries, (const uint32_t*)s.cursor,
+        return launch(c, kernel, cg, 256u, s.fp, recordItems, warpModeBelow, (const uint32_t*)s.entries,
+                      (const uint32_t*)s.cursor,
                       (const uint4*)s.surf, (const DevBody*)s.bodies, (const float4*)s.pos, (const float4*)s.prev,
                       (const uint32_t*)s.start, (const uint32_t*)s.count, (const uint4*)s.sMeta,
                       (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, out, cap, n);

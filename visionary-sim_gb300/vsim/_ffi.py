@@ -185,6 +185,7 @@ SIGNATURES = {
     "vsim_set_launch_shape": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "vsim_tune": (C.c_int, [_P, C.c_uint32, _U, _U]),
     "vsim_set_pdl": (C.c_int, [_P, C.c_int]),
+    "vsim_set_gather_mapping": (C.c_int, [_P, C.c_int]),
     "vsim_kuhn_rest_inverse": (C.c_int, [_F]),
     "vsim_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "vsim_cfl_number": (C.c_int, [_P, _D]),

@@ -261,6 +261,11 @@ class Simulator:
     def set_pdl(self, enabled: bool):
         check(lib().vsim_set_pdl(self._h, int(bool(enabled))))
 
+    def set_gather_mapping(self, mapping: str):
+        """'auto', 'warp' or 'thread' (vsim_set_gather_mapping)."""
+        code = {"auto": 0, "warp": 1, "thread": 2}[mapping]
+        check(lib().vsim_set_gather_mapping(self._h, code))
+
     def set_launch_shape(self, block: int, brick: int):
         check(lib().vsim_set_launch_shape(self._h, int(block), int(brick)))
 

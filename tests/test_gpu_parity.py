@@ -97,6 +97,25 @@ def test_blob_contact_self_contact(lib):
     assert sim.read_positions()[:, 1].min() > -0.01  # the ground held
 
 
+def test_large_colour_passes_stream_bit_exact(lib):
+    """A body whose colour passes exceed 155,648 cells (two cells per resident
+    thread on 152 SMs), so the streaming colour pass runs; one frame with
+    ground contact, compared node for node."""
+    import vsim.scenes as sc
+
+    nx, ny, nz = 128, 80, 128  # 1,310,720 cells, 163,840 per colour
+    mat = dict(sc.DEFAULT_MATERIAL, youngs_modulus=2e5, poisson_ratio=0.45, density=1000.0)
+    body = sc.Body((nx, ny, nz), (0.0, 2 * sc.H, 0.0), sc.H, np.ones(nx * ny * nz, np.uint8), mat)
+    ext = (nx * sc.H, (ny + 4) * sc.H, nz * sc.H)
+    scene = sc.Scene([body], ((-0.1, 0.0, -0.1), (ext[0] + 0.1, ext[1] + 0.1, ext[2] + 0.1)),
+                     step_duration=1 / 600, substeps=10)
+    sim, orc = make(scene)
+    assert min(sim.color_counts()) >= 155_648
+    sim.dispatch(scene.substeps)
+    orc.dispatch(scene.substeps)
+    assert_same(sim, orc, scene, "streamed frame")
+
+
 @pytest.mark.parametrize("mapping", ["warp", "thread"])
 def test_gather_mappings_agree(lib, mapping):
     """Both record-to-thread mappings of the contact gather give the oracle's

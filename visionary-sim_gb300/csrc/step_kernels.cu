@@ -300,6 +300,111 @@ __global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ c
     });
 }
 
+// The colour pass for passes much larger than the GPU: each thread solves
+// cells in turn (grid-stride) and copies the next cell's eight positions and
+// eight previous positions into its slots of shared memory (cp.async) while
+// it solves the current one, so the gathers' latency hides behind the
+// arithmetic instead of stalling the warp. Cells of one colour share no
+// node, so reading ahead is safe. Same arithmetic as elasticKernel.
+constexpr uint32_t kStreamBlock = 128;
+
+__device__ __forceinline__ void copyAsync16(float4* dst, const float4* src) {
+    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+
+__global__ void __launch_bounds__(kStreamBlock) elasticStreamKernel(const uint4* __restrict__ cells, uint32_t count,
+                                                                    const DevBody* __restrict__ bodies,
+                                                                    const uint32_t* __restrict__ bodyActive,
+                                                                    float4* __restrict__ pos,
+                                                                    const float4* __restrict__ prevState,
+                                                                    StretchLengths lens) {
+    __shared__ float4 stage[16][kStreamBlock];  // [corner] pos, [8 + corner] prev
+    const uint32_t t = threadIdx.x;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t slot = blockIdx.x * blockDim.x + t;
+    uint4 entry = slot < count ? cells[slot] : make_uint4(0, 0, 0, 0);  // frame constants: before the wait
+    pdlWait();
+    pdlLaunchNext();
+    if (slot >= count) return;
+    // Copies cell `e`'s nodes into the stage; `after` (zero, computed from the
+    // values just read out of the stage) orders the copies after those reads.
+    auto fetch = [&](uint4 e, uint32_t after) {
+        const uint32_t nx = e.z, nxy = e.w, n0 = e.x + after;
+        const uint32_t ids[8] = {n0,       n0 + 1,       n0 + nx,       n0 + nx + 1,
+                                 n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            copyAsync16(&stage[c][t], pos + ids[c]);
+            copyAsync16(&stage[8 + c][t], prevState + ids[c]);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    fetch(entry, 0);
+    while (true) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        V p[8], prev[8];
+        float w[8];
+        uint32_t bits = 0;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const float4 P = stage[c][t];
+            const float4 Q = stage[8 + c][t];
+            p[c] = xyz(P);
+            w[c] = P.w;
+            prev[c] = xyz(Q);
+            bits ^= __float_as_uint(P.x) ^ __float_as_uint(P.y) ^ __float_as_uint(P.z) ^ __float_as_uint(P.w) ^
+                    __float_as_uint(Q.x) ^ __float_as_uint(Q.y) ^ __float_as_uint(Q.z);
+        }
+        uint32_t zero;
+        asm volatile("and.b32 %0, %1, 0;" : "=r"(zero) : "r"(bits));
+        const uint4 cur = entry;
+        const uint32_t next = slot + stride;
+        if (next < count) {
+            entry = cells[next];
+            fetch(entry, zero);
+        }
+        if (bodyActive[cur.y]) {
+            const DevBody* b = bodies + cur.y;
+            const float alphaDev = b->alphaDev, alphaHyd = b->alphaHyd, gamma = b->gamma, relax = b->relax;
+            const float s = b->restScale, ns = -s, maxStretch = b->maxStretch;
+            projectTet<0>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            projectTet<1>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            projectTet<2>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            projectTet<3>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            projectTet<4>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            projectTet<5>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
+            if (maxStretch > 1.0f) {
+                const float h = b->h;
+                for (int sweep = 0; sweep < 2; sweep++) {
+#pragma unroll
+                    for (int a = 0; a < 8; a++) {
+#pragma unroll
+                        for (int bb = a + 1; bb < 8; bb++) {
+                            const V delta = p[bb] - p[a];
+                            const float len = length(delta);
+                            const float maximum = lens.len[__popc(a ^ bb) - 1] * h * maxStretch;
+                            const float weight = w[a] + w[bb];
+                            if (len > maximum && weight > 0.0f) {
+                                const V correction = delta * ((len - maximum) / (len * weight));
+                                p[a] = p[a] + w[a] * correction;
+                                p[bb] = p[bb] - w[bb] * correction;
+                            }
+                        }
+                    }
+                }
+            }
+            const uint32_t nx = cur.z, nxy = cur.w, n0 = cur.x;
+            const uint32_t ids[8] = {n0,       n0 + 1,       n0 + nx,       n0 + nx + 1,
+                                     n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
+#pragma unroll
+            for (int c = 0; c < 8; c++) pos[ids[c]] = withW(p[c], w[c]);
+        }
+        if (next >= count) break;
+        slot = next;
+    }
+}
+
 // finalize.wgsl:29-42.
 __device__ __forceinline__ V resolvePlane(V p, V prev, V normal, float depth, float friction) {
     if (depth <= 0.0f) return p;
@@ -894,6 +999,12 @@ cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drive
 
 cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, const Span& sp,
                           bool limitOnly, const StretchLengths& lens) {
+    // A dense pass of at least two cells per resident thread streams.
+    const uint32_t resident = 4 * c.sms * kStreamBlock;
+    if (!limitOnly && !sp.work.table && sp.work.count >= 2 * resident)
+        return launch(c, elasticStreamKernel, std::min(blocks(sp.work.count, kStreamBlock), 4 * c.sms), kStreamBlock,
+                      cells, sp.work.count, s.bodies, (const uint32_t*)s.bodyActive, s.pos, (const float4*)s.prev,
+                      lens);
     if (limitOnly)
         return launch(c, elasticKernel<true>, sp.grid, sp.block, cells, sp.work, s.bodies,
                       (const uint32_t*)s.bodyActive, s.pos, (const float4*)s.prev, lens);

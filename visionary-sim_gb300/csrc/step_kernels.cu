@@ -353,8 +353,9 @@ __global__ void __launch_bounds__(kStreamBlock) elasticStreamKernel(const uint4*
             p[c] = xyz(P);
             w[c] = P.w;
             prev[c] = xyz(Q);
-            bits ^= __float_as_uint(P.x) ^ __float_as_uint(P.y) ^ __float_as_uint(P.z) ^ __float_as_uint(P.w) ^
-                    __float_as_uint(Q.x) ^ __float_as_uint(Q.y) ^ __float_as_uint(Q.z);
+            // One word of each 16-byte read is enough: a read's registers
+            // are written together.
+            bits ^= __float_as_uint(P.w) ^ __float_as_uint(Q.x);
         }
         uint32_t zero;
         asm volatile("and.b32 %0, %1, 0;" : "=r"(zero) : "r"(bits));

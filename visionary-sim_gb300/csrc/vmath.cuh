@@ -22,6 +22,11 @@ struct V {
 
 __device__ __forceinline__ V mk(float x, float y, float z) { return V{x, y, z}; }
 __device__ __forceinline__ V xyz(float4 a) { return V{a.x, a.y, a.z}; }
+
+// fma3 issues x and y as one packed FP32x2 fused multiply-add (sm_100 and
+// later), which rounds each lane to nearest exactly as fmaf does.
+__device__ __forceinline__ float2 xyOf(V a) { return make_float2(a.x, a.y); }
+__device__ __forceinline__ V withXy(float2 xy, float z) { return V{xy.x, xy.y, z}; }
 __device__ __forceinline__ V operator+(V a, V b) { return V{a.x + b.x, a.y + b.y, a.z + b.z}; }
 __device__ __forceinline__ V operator-(V a, V b) { return V{a.x - b.x, a.y - b.y, a.z - b.z}; }
 __device__ __forceinline__ V operator-(V a) { return V{-a.x, -a.y, -a.z}; }
@@ -30,7 +35,7 @@ __device__ __forceinline__ V operator*(float s, V a) { return V{s * a.x, s * a.y
 __device__ __forceinline__ V operator/(V a, float s) { return V{a.x / s, a.y / s, a.z / s}; }
 // a * s + acc per component, one rounding each.
 __device__ __forceinline__ V fma3(V a, float s, V acc) {
-    return V{fmaf(a.x, s, acc.x), fmaf(a.y, s, acc.y), fmaf(a.z, s, acc.z)};
+    return withXy(__ffma2_rn(xyOf(a), make_float2(s, s), xyOf(acc)), fmaf(a.z, s, acc.z));
 }
 // x first, then y and z fused in.
 __device__ __forceinline__ float dot(V a, V b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }

@@ -99,11 +99,11 @@ def test_blob_contact_self_contact(lib):
 
 def test_large_colour_passes_stream_bit_exact(lib):
     """A body whose colour passes exceed 155,648 cells (two cells per resident
-    thread on 152 SMs), so the streaming colour pass runs; one frame with
-    ground contact, compared node for node."""
+    thread: 4 blocks of 128 on each of 152 SMs), so the streaming colour pass
+    runs; one frame with ground contact, compared node for node."""
     import vsim.scenes as sc
 
-    nx, ny, nz = 128, 80, 128  # 1,310,720 cells, 163,840 per colour
+    nx, ny, nz = 128, 96, 128  # 1,572,864 cells, 196,608 per colour
     mat = dict(sc.DEFAULT_MATERIAL, youngs_modulus=2e5, poisson_ratio=0.45, density=1000.0)
     body = sc.Body((nx, ny, nz), (0.0, 2 * sc.H, 0.0), sc.H, np.ones(nx * ny * nz, np.uint8), mat)
     ext = (nx * sc.H, (ny + 4) * sc.H, nz * sc.H)

@@ -307,6 +307,7 @@ __global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ c
 // arithmetic instead of stalling the warp. Cells of one colour share no
 // node, so reading ahead is safe. Same arithmetic as elasticKernel.
 constexpr uint32_t kStreamBlock = 128;
+constexpr uint32_t kStreamBlocksPerSm = 4;  // what the ~127 registers of a cell allow
 
 __device__ __forceinline__ void copyAsync16(float4* dst, const float4* src) {
     const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
@@ -1001,9 +1002,10 @@ cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drive
 cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, const Span& sp,
                           bool limitOnly, const StretchLengths& lens) {
     // A dense pass of at least two cells per resident thread streams.
-    const uint32_t resident = 4 * c.sms * kStreamBlock;
+    const uint32_t resident = kStreamBlocksPerSm * c.sms * kStreamBlock;
     if (!limitOnly && !sp.work.table && sp.work.count >= 2 * resident)
-        return launch(c, elasticStreamKernel, std::min(blocks(sp.work.count, kStreamBlock), 4 * c.sms), kStreamBlock,
+        return launch(c, elasticStreamKernel, std::min(blocks(sp.work.count, kStreamBlock), kStreamBlocksPerSm * c.sms),
+                      kStreamBlock,
                       cells, sp.work.count, s.bodies, (const uint32_t*)s.bodyActive, s.pos, (const float4*)s.prev,
                       lens);
     if (limitOnly)

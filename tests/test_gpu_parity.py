@@ -1,9 +1,10 @@
 """GPU parity: libvsim's kernels against the float CPU oracle, through the C
 ABI, frame by frame from one shared state.
 
-The kernels evaluate every operation in the oracle's order with separately
-rounded multiplies and adds, so the expected agreement is exact equality
-(`==`: -0 and +0 compare equal). The configured tolerance -- 1e-5 relative,
+The kernels evaluate every operation in the oracle's order, fusing a
+multiply and an add exactly where the oracle does and rounding everything
+else once, so the expected agreement is exact equality (`==`: -0 and +0
+compare equal). The configured tolerance -- 1e-5 relative,
 max_i |x_gpu - x_oracle| / max(|x_oracle|, L_body) -- is asserted as well, so
 a failure reports both how far apart and whether the bar itself is met.
 """

@@ -86,6 +86,8 @@ void bodyParams(const vsim_sim* s, std::vector<DevBody>& out) {
         }
         d.bucket = float(s->grids[g].bucket);
         d.gridBase = s->gridBase[g];
+        d.divX = reciprocal64(d.gridDims[0]);
+        d.divXY = reciprocal64(d.gridDims[0] * d.gridDims[1]);
     }
 }
 

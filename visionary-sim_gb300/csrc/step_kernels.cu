@@ -757,10 +757,16 @@ __device__ __forceinline__ bool contactHit(const Contactor& c, uint4 them, float
     return admitted(c.me, them, selfContact) && !(dist2 >= reach * reach) && !(c.wi + Q.w <= 0.0f);
 }
 
+// n / d with m = reciprocal64(d).
+__device__ __forceinline__ uint32_t divBy(uint32_t n, uint64_t m) { return m ? uint32_t(__umul64hi(m, uint64_t(n))) : n; }
+
+constexpr uint32_t kCollideBlock = 256;
+
 template <bool EMIT>
-__global__ void __launch_bounds__(256) collideKernel(
+__global__ void __launch_bounds__(kCollideBlock) collideKernel(
     const FrameParams* __restrict__ fp, uint32_t items, uint32_t warpModeBelow, const uint32_t* __restrict__ entries,
-    const uint32_t* __restrict__ cursor, const uint4* __restrict__ surf, const DevBody* __restrict__ bodies,
+    const uint32_t* __restrict__ key, const uint32_t* __restrict__ cursor, const uint4* __restrict__ surf,
+    const DevBody* __restrict__ bodies,
     const float4* __restrict__ pos, const float4* __restrict__ prevState, const uint32_t* __restrict__ start,
     const uint32_t* __restrict__ count, const uint4* __restrict__ sMeta, const float4* __restrict__ sPos,
     const uint32_t* __restrict__ sRec, float4* __restrict__ delta, uint32_t* __restrict__ pairs, uint32_t capacity,
@@ -780,8 +786,18 @@ __global__ void __launch_bounds__(256) collideKernel(
         c.wi = P.w;
         c.pi = xyz(P);
         c.movedI = c.pi - xyz(prevState[c.node]);
-        c.frictionI = bodies[c.me.y].friction;
-        bucketOf(bodies + c.me.y, c.pi, centre);
+        const DevBody* grid = bodies + c.me.y;
+        c.frictionI = grid->friction;
+        // The record's bucket coordinates, from the bucket binKernel gave it
+        // (positions have not moved since): integer division by the grid's
+        // dimensions rather than bucketOf's three float divides.
+        const uint32_t linear = key[r] - grid->gridBase;
+        const uint32_t z = divBy(linear, grid->divXY);
+        const uint32_t rest = linear - z * (grid->gridDims[0] * grid->gridDims[1]);
+        const uint32_t y = divBy(rest, grid->divX);
+        centre[0] = int(rest - y * grid->gridDims[0]);
+        centre[1] = int(y);
+        centre[2] = int(z);
         return c;
     };
     // Neighbour bucket q of the record's bucket (q = dx + 3 dy + 9 dz, offsets + 1).
@@ -837,7 +853,11 @@ __global__ void __launch_bounds__(256) collideKernel(
         return;
     }
 
+    // Per warp: the neighbour bucket (lane) whose run starts at each candidate
+    // position of the current round.
+    __shared__ uint32_t runAt[kCollideBlock / 32][32];
     const uint32_t lane = threadIdx.x & 31;
+    uint32_t* starting = runAt[threadIdx.x >> 5];
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t i = thread >> 5; i < total; i += warps) {
         const uint32_t r = entries[i];
@@ -864,16 +884,23 @@ __global__ void __launch_bounds__(256) collideKernel(
         const uint32_t candidates = __shfl_sync(kAll, end, 31);
         V sum = mk(0.0f, 0.0f, 0.0f);
         float hits = 0.0f;
+        uint32_t carry = 0;  // the run holding the round's first candidate, if it began earlier
         for (uint32_t round = 0; round < candidates; round += 32) {
             const uint32_t cand = round + lane;
-            // The run holding the candidate: the first lane whose end exceeds it.
-            uint32_t lo = 0, hi = 26;
-#pragma unroll
-            for (int step = 0; step < 5; step++) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (__shfl_sync(kAll, end, mid) > cand) hi = mid;
-                else lo = mid + 1;
+            // The run holding the candidate: the last run to start at or
+            // before it. Runs that start in this round mark their positions.
+            const uint32_t begin = end - held;
+            uint32_t bit = 0;
+            if (held && begin >= round && begin < round + 32) {
+                bit = 1u << (begin - round);
+                starting[begin - round] = lane;
             }
+            const uint32_t starts = __reduce_or_sync(kAll, bit);
+            __syncwarp();
+            const uint32_t below = starts & (0xffffffffu >> (31 - lane));
+            const uint32_t lo = below ? starting[31 - __clz(below)] : carry;
+            carry = __shfl_sync(kAll, lo, 31);
+            __syncwarp();  // the next round rewrites `starting`
             const uint32_t runEnd = __shfl_sync(kAll, end, lo);
             const uint32_t runHeld = __shfl_sync(kAll, held, lo);
             const uint32_t runFirst = __shfl_sync(kAll, first, lo);
@@ -1054,8 +1081,8 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& 
                                    : mapping == VSIM_GATHER_THREAD ? 0u
                                                                    : 2048 * c.sms;
     auto collide = [&](auto kernel, uint32_t* out, uint32_t cap, unsigned long long* n) {
-        return launch(c, kernel, cg, 256u, s.fp, recordItems, warpModeBelow, (const uint32_t*)s.entries,
-                      (const uint32_t*)s.cursor,
+        return launch(c, kernel, cg, kCollideBlock, s.fp, recordItems, warpModeBelow, (const uint32_t*)s.entries,
+                      (const uint32_t*)s.key, (const uint32_t*)s.cursor,
                       (const uint4*)s.surf, (const DevBody*)s.bodies, (const float4*)s.pos, (const float4*)s.prev,
                       (const uint32_t*)s.start, (const uint32_t*)s.count, (const uint4*)s.sMeta,
                       (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, out, cap, n);

@@ -107,8 +107,17 @@ struct DevBody {
     float bucket;
     uint32_t gridDims[3];
     uint32_t gridBase;  // index of the grid's first bucket in the bucket arrays
+    // Reciprocals for dividing a bucket's linear index by dims[0] and by
+    // dims[0] * dims[1]: floor(2^64 / d) + 1, exact for 32-bit numerators
+    // (0 stands for d = 1).
+    uint64_t divX, divXY;
 };
-static_assert(sizeof(DevBody) == 96, "DevBody is one 96-byte record");
+static_assert(sizeof(DevBody) == 112, "DevBody is one 112-byte record");
+
+// floor(2^64 / d) + 1 for a 32-bit divisor d > 1, 0 for d = 1: with it,
+// n / d = high 64 bits of n * m for every 32-bit n (Lemire, Kaser and
+// Kurz, "Faster remainder by direct computation", 2019).
+inline uint64_t reciprocal64(uint32_t d) { return d > 1 ? ~uint64_t(0) / d + 1 : 0; }
 
 // Scalars every substep kernel reads, refreshed by one small copy per frame.
 struct FrameParams {

@@ -312,6 +312,13 @@ typedef struct vsim_profile {
    kernel group. The frame advances the simulation like vsim_dispatch. */
 int vsim_profile_frame(vsim_sim* sim, uint32_t steps, int with_splats, const float view_dir[3],
                        vsim_profile* out);
+/* Time `sweeps` Gauss-Seidel sweeps of the elastic colour passes (8 passes
+   each, the frame's launch shapes) run back to back as one captured graph,
+   with events only at its two ends; *ms receives the total. The positions
+   the passes move are saved first and restored after, so the state is
+   unchanged. For roofline measurement: the bracketed launches in
+   vsim_profile_frame cannot overlap one another. No reference counterpart. */
+int vsim_time_colour_passes(vsim_sim* sim, uint32_t sweeps, float* ms);
 /* Occupied cells per colour over all bodies (a colour pass's work). */
 int vsim_color_counts(const vsim_sim* sim, uint32_t out[8]);
 /* Kernels a frame of `steps` substeps launches (splats excluded). */

@@ -288,6 +288,26 @@ def test_material_change_midrun(lib):
         assert_same(sim, orc, scene, f"after change {frame}")
 
 
+def test_timing_colour_passes_leaves_state(lib):
+    """vsim_time_colour_passes restores what the timed passes moved: the
+    next frame still equals the oracle's."""
+    import vsim.scenes as sc
+
+    scene = sc.noise_blob(n=16, seed=3, splats=0)
+    sim, orc = make(scene)
+    for _ in range(2):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+    before = sim.read_state()
+    assert sim.time_colour_passes(3) > 0
+    after = sim.read_state()
+    for a, b in zip(before, after):
+        assert np.array_equal(a, b)
+    sim.dispatch(scene.substeps)
+    orc.dispatch(scene.substeps)
+    assert_same(sim, orc, scene, "after timing")
+
+
 def test_run_twice_identical(lib):
     import vsim.scenes as sc
 

@@ -1167,6 +1167,59 @@ uint32_t vsim_splat_launches(const vsim_sim* s) {
     return 1 + 5 * 4;  // deformation, then four 8-bit passes of five kernels
 }
 
+int vsim_time_colour_passes(vsim_sim* s, uint32_t sweeps, float* ms) {
+    SIM_GUARD(s);
+    if (!ms) return fail(VSIM_ERR_INVALID, "ms is NULL");
+    *ms = 0;
+    if (sweeps < 1) return VSIM_OK;
+    int rc = syncParams(s);
+    if (rc) return rc;
+    const size_t bytes = size_t(s->nodeCount) * 16;
+    float4* saved = nullptr;
+    CK(cudaMalloc(&saved, bytes), "save positions");
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool savedOk = false;
+    auto body = [&]() -> cudaError_t {
+        cudaError_t e;
+        if ((e = cudaMemcpyAsync(saved, s->d.pos, bytes, cudaMemcpyDeviceToDevice, s->stream))) return e;
+        savedOk = true;
+        const LaunchCtx c{s->capture, s->pdl, s->sms};
+        const StretchLengths lens = stretchLengths();
+        if ((e = cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal))) return e;
+        cudaError_t enc = cudaSuccess;
+        for (uint32_t sweep = 0; sweep < sweeps && enc == cudaSuccess; sweep++)
+            for (int col = 0; col < 8 && enc == cudaSuccess; col++)
+                if (s->plan.colour[col].grid)
+                    enc = launchElastic(c, s->d, s->d.cells + s->colorStart[col], s->plan.colour[col], false, lens);
+        const cudaError_t end = cudaStreamEndCapture(s->capture, &graph);
+        if (enc) return enc;
+        if (end) return end;
+        if ((e = cudaGraphInstantiate(&exec, graph, 0))) return e;
+        if ((e = cudaEventCreate(&e0)) || (e = cudaEventCreate(&e1))) return e;
+        if ((e = cudaGraphLaunch(exec, s->stream))) return e;  // warm-up
+        if ((e = cudaEventRecord(e0, s->stream))) return e;
+        if ((e = cudaGraphLaunch(exec, s->stream))) return e;
+        if ((e = cudaEventRecord(e1, s->stream))) return e;
+        if ((e = cudaEventSynchronize(e1))) return e;
+        return cudaEventElapsedTime(ms, e0, e1);
+    };
+    cudaError_t e = body();
+    if (savedOk) {  // put back what the passes moved
+        const cudaError_t back = cudaMemcpyAsync(s->d.pos, saved, bytes, cudaMemcpyDeviceToDevice, s->stream);
+        if (e == cudaSuccess) e = back;
+    }
+    cudaStreamSynchronize(s->stream);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(saved);
+    CK(e, "time colour passes");
+    return VSIM_OK;
+}
+
 int vsim_profile_frame(vsim_sim* s, uint32_t steps, int with_splats, const float view_dir[3], vsim_profile* out) {
     SIM_GUARD(s);
     if (!out) return fail(VSIM_ERR_INVALID, "out is NULL");

@@ -314,6 +314,13 @@ class Simulator:
         check(lib().vsim_profile_frame(self._h, int(steps), int(bool(splats)), fptr(v), C.byref(prof)))
         return {k: (prof.ms[i], prof.launches[i]) for i, k in enumerate(_ffi.KINDS) if prof.launches[i]}
 
+    def time_colour_passes(self, sweeps: int) -> float:
+        """Milliseconds for `sweeps` x 8 colour passes run back to back
+        (vsim_time_colour_passes); the state is left unchanged."""
+        ms = C.c_float()
+        check(lib().vsim_time_colour_passes(self._h, int(sweeps), C.byref(ms)))
+        return float(ms.value)
+
     def color_counts(self) -> np.ndarray:
         out = np.zeros(8, np.uint32)
         check(lib().vsim_color_counts(self._h, uptr(out)))

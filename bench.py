@@ -155,6 +155,24 @@ def time_frames(sim, scene, stream, frames: int, flush) -> list:
     return times
 
 
+def replica_throughput(local_seconds: float, units_per_rank: int, device):
+    """Whole-job throughput of replicas: every rank processed
+    `units_per_rank` units, and the job took the slowest rank's time (a MAX
+    all-reduce of the timed interval, then a barrier). Returns (seconds,
+    units/s over all ranks)."""
+    import torch
+    import torch.distributed as dist
+
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    total = local_seconds
+    if world > 1:
+        t = torch.tensor([local_seconds], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+        dist.barrier()
+    return total, units_per_rank * world / total
+
+
 def colour_pass_rate(sim, sweeps: int = 10):
     """The elastic colour pass timed as the frame runs it: `sweeps` x 8
     passes back to back in one graph (programmatic dependent launch), events
@@ -591,14 +609,7 @@ def main():
     with ClockSampler(local) as clocks:
         times = time_frames(sim, scene, stream, args.steps, flush)
     torch.cuda.synchronize()
-    total = float(sum(times))
-    if world > 1:
-        t = torch.tensor([total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total = float(t.item())
-        dist.barrier()
-    units = units_per_frame(scene) * args.steps * world
-    value = units / total
+    total, value = replica_throughput(float(sum(times)), units_per_frame(scene) * args.steps, "cuda")
     launches = args.steps * (sim.frame_launches(scene.substeps) + sim.splat_launches())
 
     hbm, peak_kind = peaks()

@@ -307,3 +307,26 @@ def blob_and_sheet(n: int = 192, seed: int = 4, splats: int = 20_000_000) -> Sce
     if splats:
         scene.splats[0] = splats_in(blob, splats, seed + 1)
     return scene
+
+
+MATERIAL_KEYS = ("youngs_modulus", "poisson_ratio", "density", "friction", "damping", "relaxation", "max_stretch")
+
+
+def tank_scene(fixture) -> Scene:
+    """The reference's `tank` scene (apps/simulator/src/scene/tank.js:47-83):
+    two meshes (spot, suzanne) and three analytic shapes (torus, sphere,
+    cube) above a 0.6 x 0.5 x 0.4 m open-topped tank, each body's cells
+    as the reference's voxelisers produce them (vsim.voxelize), read from
+    `fixture` (an npz written by tests/golden/make_tank_fixture.py). The
+    step duration is left to the CFL rule, contact between bodies is on,
+    self contact off, as in the reference."""
+    z = np.load(fixture) if not isinstance(fixture, dict) else fixture
+    bodies = []
+    for b in range(len(z["names"])):
+        dims = tuple(int(v) for v in z[f"dims{b}"])
+        occupancy = np.unpackbits(z[f"occupancy{b}"])[: dims[0] * dims[1] * dims[2]].astype(np.uint8)
+        material = {k: float(v) for k, v in zip(MATERIAL_KEYS, z[f"material{b}"])}
+        bodies.append(Body(dims, tuple(float(v) for v in z[f"origin{b}"]), float(z[f"h{b}"]), occupancy, material))
+    tank = (tuple(float(v) for v in z["tank_min"]), tuple(float(v) for v in z["tank_max"]))
+    return Scene(bodies, tank, step_duration=None, substeps=24, contact=True, self_contact=False)
+

@@ -1,0 +1,311 @@
+"""Rest geometry to occupancy grid: the reference's asset preparation and
+voxelisers, restated on the host so that scenes built from meshes and
+analytic shapes get exactly the reference's cells.
+
+Follows, operation by operation in JavaScript's double arithmetic (mesh
+vertices stored as float32, as the reference's Float32Array does):
+
+- `apps/simulator/src/assets/objLoader.js:22-119` -- OBJ parsing, normalising
+  to a size, translating;
+- `packages/visionary-sim/src/body/restGeometry.js:31-43` -- mesh bounds;
+- `apps/simulator/src/assets/shapes.js:29-172` -- torus, sphere and box
+  signed distances, `translateShape`, `restOnGround` (the drawn surfaces are
+  not needed here);
+- `packages/visionary-sim/src/sim/discretize/lattice/voxelize.js:19-435` --
+  `gridForBounds`, `voxelizeSdf`, `voxelizeMesh` (three-axis ray parity with a
+  majority vote, edge marking, 6-neighbourhood close).
+
+The result feeds `vsim_create` as a body's cell grid (cell_dims, origin, h,
+occupancy).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+from typing import Callable
+
+import numpy as np
+
+
+@dataclass
+class Mesh:
+    positions: np.ndarray  # float32, (n, 3)
+    indices: np.ndarray    # uint32, (m, 3)
+
+
+@dataclass
+class Shape:
+    sdf: Callable[[float, float, float], float]
+    bounds: tuple           # (min xyz, max xyz), doubles
+
+
+@dataclass
+class OccupancyGrid:
+    dims: list
+    origin: list
+    h: float
+    occupancy: np.ndarray  # uint8, dims[0] * dims[1] * dims[2], x fastest
+
+
+# ---- objLoader.js -------------------------------------------------------------
+
+def parse_obj(text: str) -> Mesh:
+    """objLoader.js:22-67: positions and fan-triangulated faces."""
+    positions, indices = [], []
+    for raw in text.split("\n"):
+        line = raw.strip()
+        if not line or line[0] == "#":
+            continue
+        if line.startswith("v "):
+            parts = line.split()
+            positions.append((float(parts[1]), float(parts[2]), float(parts[3])))
+            continue
+        if not line.startswith("f "):
+            continue
+        face = []
+        count = len(positions)
+        for token in line.split()[1:]:
+            head = token.split("/")[0]
+            try:
+                index = int(head)
+            except ValueError:
+                continue
+            face.append(index - 1 if index > 0 else count + index)
+        for i in range(2, len(face)):
+            indices.append((face[0], face[i - 1], face[i]))
+    return Mesh(np.asarray(positions, np.float32).reshape(-1, 3), np.asarray(indices, np.uint32).reshape(-1, 3))
+
+
+def mesh_bounds(positions: np.ndarray):
+    """restGeometry.js:31-43."""
+    p = positions.astype(np.float64)
+    return [float(v) for v in p.min(axis=0)], [float(v) for v in p.max(axis=0)]
+
+
+def normalize_mesh(mesh: Mesh, target_size: float) -> Mesh:
+    """objLoader.js:86-103: the largest axis scaled to `target_size`, centred in
+    x and z, base at y = 0; each result rounded to float32."""
+    lo, hi = mesh_bounds(mesh.positions)
+    extent = [hi[a] - lo[a] for a in range(3)]
+    scale = target_size / max(extent)
+    centre_x = (lo[0] + hi[0]) * 0.5
+    centre_z = (lo[2] + hi[2]) * 0.5
+    p = mesh.positions.astype(np.float64)
+    out = np.empty_like(mesh.positions)
+    out[:, 0] = ((p[:, 0] - centre_x) * scale).astype(np.float32)
+    out[:, 1] = ((p[:, 1] - lo[1]) * scale).astype(np.float32)
+    out[:, 2] = ((p[:, 2] - centre_z) * scale).astype(np.float32)
+    return Mesh(out, mesh.indices)
+
+
+def translate_mesh(mesh: Mesh, offset) -> Mesh:
+    """objLoader.js:110-117."""
+    p = mesh.positions.astype(np.float64) + np.asarray(offset, np.float64)
+    return Mesh(p.astype(np.float32), mesh.indices)
+
+
+# ---- shapes.js ----------------------------------------------------------------
+
+def torus(major_radius: float, minor_radius: float) -> Shape:
+    """shapes.js:29-52 (a torus in the XZ plane)."""
+    outer = major_radius + minor_radius
+
+    def sdf(x, y, z):
+        radial = math.hypot(x, z) - major_radius
+        return math.hypot(radial, y) - minor_radius
+
+    return Shape(sdf, ([-outer, -minor_radius, -outer], [outer, minor_radius, outer]))
+
+
+def sphere(radius: float) -> Shape:
+    """shapes.js:59-80."""
+    return Shape(lambda x, y, z: math.hypot(x, y, z) - radius, ([-radius] * 3, [radius] * 3))
+
+
+def box(half_extents) -> Shape:
+    """shapes.js:87-115."""
+    hx, hy, hz = half_extents
+
+    def sdf(x, y, z):
+        dx = abs(x) - hx
+        dy = abs(y) - hy
+        dz = abs(z) - hz
+        outside = math.hypot(max(dx, 0), max(dy, 0), max(dz, 0))
+        inside = min(max(dx, dy, dz), 0)
+        return outside + inside
+
+    return Shape(sdf, ([-hx, -hy, -hz], [hx, hy, hz]))
+
+
+def translate_shape(shape: Shape, offset) -> Shape:
+    """shapes.js:147-161."""
+    dx, dy, dz = offset
+    lo, hi = shape.bounds
+    inner = shape.sdf
+    return Shape(lambda x, y, z: inner(x - dx, y - dy, z - dz),
+                 ([lo[0] + dx, lo[1] + dy, lo[2] + dz], [hi[0] + dx, hi[1] + dy, hi[2] + dz]))
+
+
+def rest_on_ground(shape: Shape) -> Shape:
+    """shapes.js:169-171: lowest point at y = 0."""
+    return translate_shape(shape, [0, -shape.bounds[0][1], 0])
+
+
+# ---- voxelize.js --------------------------------------------------------------
+
+DEFAULT_PADDING = 2
+
+
+def grid_for_bounds(bounds, element_size: float, padding: int = DEFAULT_PADDING) -> OccupancyGrid:
+    """voxelize.js:40-67."""
+    if not (element_size > 0 and math.isfinite(element_size)):
+        raise ValueError(f"element_size must be a positive length in metres, got {element_size}")
+    h = element_size
+    lo, hi = bounds
+    extent = [hi[a] - lo[a] for a in range(3)]
+    dims = [max(1, math.ceil(e / h - 1e-6)) + 2 * padding for e in extent]
+    origin = [v - h * padding for v in lo]
+    return OccupancyGrid(dims, origin, h, np.zeros(dims[0] * dims[1] * dims[2], np.uint8))
+
+
+def voxelize_sdf(shape: Shape, element_size: float, padding: int = DEFAULT_PADDING) -> OccupancyGrid:
+    """voxelize.js:124-143 with anyCornerInside (:153-165): a cell is material
+    when its centre is within half a cell of the surface or any corner is
+    inside; the grid is shifted half a cell so centres land on the bounds."""
+    grid = grid_for_bounds(shape.bounds, element_size, padding)
+    h = grid.h
+    origin = [v - h * 0.5 for v in grid.origin]
+    grid.origin = origin
+    threshold = h * 0.5
+    nx, ny, nz = grid.dims
+    sdf = shape.sdf
+    occ = grid.occupancy
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                x = origin[0] + i * h
+                y = origin[1] + j * h
+                z = origin[2] + k * h
+                if sdf(x + h * 0.5, y + h * 0.5, z + h * 0.5) < threshold or any(
+                        sdf(x + (h if c & 1 else 0), y + (h if c & 2 else 0), z + (h if c & 4 else 0)) < 0
+                        for c in range(8)):
+                    occ[i + nx * (j + ny * k)] = 1
+    return grid
+
+
+def voxelize_mesh(mesh: Mesh, bounds, element_size: float, padding: int = DEFAULT_PADDING,
+                  close: bool = True) -> OccupancyGrid:
+    """voxelize.js:178-200."""
+    grid = grid_for_bounds(bounds, element_size, padding)
+    n = grid.occupancy.size
+    votes = np.zeros(n, np.uint8)
+    surface = np.zeros(n, np.uint8)
+    for axis in range(3):
+        _accumulate_axis(mesh, grid, axis, votes, surface)
+    _mark_edge_cells(mesh, grid, surface)
+    grid.occupancy[:] = ((votes >= 2) | (surface == 1)).astype(np.uint8)
+    if close:
+        grid.occupancy[:] = _neighbourhood_pass(grid, _neighbourhood_pass(grid, grid.occupancy, True), False)
+    return grid
+
+
+def _cell(grid: OccupancyGrid, i: int, j: int, k: int) -> int:
+    return i + grid.dims[0] * (j + grid.dims[1] * k)
+
+
+def _mark_edge_cells(mesh: Mesh, grid: OccupancyGrid, surface: np.ndarray):
+    """voxelize.js:214-248: every cell a triangle edge passes through."""
+    dims, origin, h = grid.dims, grid.origin, grid.h
+    step = h * 0.4
+    pos = mesh.positions.astype(np.float64)
+    for tri in mesh.indices:
+        for e in range(3):
+            a = pos[int(tri[e])]
+            b = pos[int(tri[(e + 1) % 3])]
+            dx = float(b[0]) - float(a[0])
+            dy = float(b[1]) - float(a[1])
+            dz = float(b[2]) - float(a[2])
+            steps = max(1, math.ceil(math.hypot(dx, dy, dz) / step))
+            ax, ay, az = float(a[0]), float(a[1]), float(a[2])
+            for s in range(steps + 1):
+                f = s / steps
+                i = math.floor((ax + dx * f - origin[0]) / h)
+                j = math.floor((ay + dy * f - origin[1]) / h)
+                k = math.floor((az + dz * f - origin[2]) / h)
+                if 0 <= i < dims[0] and 0 <= j < dims[1] and 0 <= k < dims[2]:
+                    surface[_cell(grid, i, j, k)] = 1
+
+
+def _accumulate_axis(mesh: Mesh, grid: OccupancyGrid, axis: int, votes: np.ndarray, surface: np.ndarray):
+    """voxelize.js:265-360: one ray per cell column along `axis` (sampled a
+    fixed sub-cell jitter off the centre); cells past an odd number of
+    crossings vote interior, crossed cells hold surface."""
+    dims, origin, h = grid.dims, grid.origin, grid.h
+    u, v, w = (axis + 1) % 3, (axis + 2) % 3, axis
+    crossings = {}
+    jitter_u = h * 1.7e-4
+    jitter_v = h * 0.9e-4
+    pos = mesh.positions.astype(np.float64)
+    for tri in mesh.indices:
+        a, b, c = pos[int(tri[0])], pos[int(tri[1])], pos[int(tri[2])]
+        au, av, aw = float(a[u]), float(a[v]), float(a[w])
+        bu, bv, bw = float(b[u]), float(b[v]), float(b[w])
+        cu, cv, cw = float(c[u]), float(c[v]), float(c[w])
+        area2 = (bv - cv) * (au - cu) + (cu - bu) * (av - cv)
+        if abs(area2) < 1e-20:
+            continue
+        inv_area2 = 1 / area2
+        min_u, max_u = min(au, bu, cu), max(au, bu, cu)
+        min_v, max_v = min(av, bv, cv), max(av, bv, cv)
+        a0 = max(0, math.ceil((min_u - origin[u]) / h - 0.5))
+        a1 = min(dims[u] - 1, math.floor((max_u - origin[u]) / h - 0.5))
+        b0 = max(0, math.ceil((min_v - origin[v]) / h - 0.5))
+        b1 = min(dims[v] - 1, math.floor((max_v - origin[v]) / h - 0.5))
+        for cv2 in range(b0, b1 + 1):
+            pv = origin[v] + (cv2 + 0.5) * h + jitter_v
+            for cu2 in range(a0, a1 + 1):
+                pu = origin[u] + (cu2 + 0.5) * h + jitter_u
+                l0 = ((bv - cv) * (pu - cu) + (cu - bu) * (pv - cv)) * inv_area2
+                if l0 < 0:
+                    continue
+                l1 = ((cv - av) * (pu - cu) + (au - cu) * (pv - cv)) * inv_area2
+                if l1 < 0:
+                    continue
+                l2 = 1 - l0 - l1
+                if l2 < 0:
+                    continue
+                crossings.setdefault(cu2 + dims[u] * cv2, []).append(l0 * aw + l1 * bw + l2 * cw)
+    ijk = [0, 0, 0]
+    for column, hits in crossings.items():
+        hits.sort()
+        ijk[u] = column % dims[u]
+        ijk[v] = column // dims[u]
+        for hit in hits:
+            cw = math.floor((hit - origin[w]) / h)
+            if 0 <= cw < dims[w]:
+                ijk[w] = cw
+                surface[_cell(grid, *ijk)] = 1
+        nxt, inside = 0, False
+        for cw in range(dims[w]):
+            centre = origin[w] + (cw + 0.5) * h
+            while nxt < len(hits) and hits[nxt] <= centre:
+                inside = not inside
+                nxt += 1
+            if inside:
+                ijk[w] = cw
+                votes[_cell(grid, *ijk)] += 1
+
+
+def _neighbourhood_pass(grid: OccupancyGrid, source: np.ndarray, dilate: bool) -> np.ndarray:
+    """voxelize.js:402-435: 6-neighbourhood dilate or erode; outside the grid
+    counts as empty."""
+    nx, ny, nz = grid.dims
+    s = source.reshape(nz, ny, nx).astype(bool)
+    padded = np.pad(s, 1, constant_values=False)
+    neighbours = [padded[1:-1, 1:-1, 2:], padded[1:-1, 1:-1, :-2], padded[1:-1, 2:, 1:-1],
+                  padded[1:-1, :-2, 1:-1], padded[2:, 1:-1, 1:-1], padded[:-2, 1:-1, 1:-1]]
+    if dilate:
+        out = s | np.logical_or.reduce(neighbours)
+    else:
+        out = s & np.logical_and.reduce(neighbours)
+    return out.reshape(-1).astype(np.uint8)

@@ -342,6 +342,15 @@ uint32_t vsim_splats_count(const vsim_sim* sim);
    mean' = x(rest) and covariance' = (F R S)(F R S)^T, and compute its depth
    key along `view_dir` (larger depth sorts first: back to front). */
 int vsim_splats_deform(vsim_sim* sim, const float view_dir[3]);
+/* vsim_splats_deform, and each deformed covariance taken apart into the
+   ellipsoid's orientation and axis lengths in the same launch -- what a
+   renderer that stores rotation + scale wants (ellipsoid.wgsl:20-91, four
+   sweeps of cyclic Jacobi; apps/simulator/src/render/ellipsoid.js is its CPU
+   twin). */
+int vsim_splats_deform_axes(vsim_sim* sim, const float view_dir[3]);
+/* The axes of the last vsim_splats_deform_axes: unit quaternions xyzw and
+   axis lengths xyz, splats in bind order (either pointer may be NULL). */
+int vsim_splats_read_axes(vsim_sim* sim, float* rotation, float* scale, size_t count);
 /* Stable radix sort of the depth keys: the draw order, back to front. */
 int vsim_splats_sort(vsim_sim* sim);
 /* Copy results to the host (any pointer may be NULL): means xyz, covariance

@@ -81,6 +81,8 @@ def lib():
             "vo_resolve_plane_f64": (None, [_D, _D, _D, C.c_double, C.c_double, _D]),
             "vo_deformation_at_f64": (None, [_D, _U, _U, _D, C.c_double, _D, _D, _D]),
             "vo_deformed_covariance_f64": (None, [_D, _D, _D, _D]),
+            "vo_ellipsoid_axes_f64": (None, [_D, _D, _D]),
+            "vo_ellipsoid_axes_f32": (None, [_F, C.c_uint32, _F, _F]),
             "vo_stretch_edges": (None, [_D]),
             "vo_broadphase_grid": (None, [_D, _D, C.c_double, _D, _D, _U]),
             "vo_bucket_of": (C.c_uint32, [_D, C.c_double, _U, _D]),
@@ -229,6 +231,23 @@ class Oracle:
                               scales.ctypes.data_as(_F), n, view.ctypes.data_as(_F), out_m.ctypes.data_as(_F),
                               out_c.ctypes.data_as(_F), keys.ctypes.data_as(_U))
         return out_m, out_c, keys
+
+
+def ellipsoid_axes_f64(cov6) -> tuple:
+    """(rotation xyzw, scale xyz) of one covariance (xx, xy, xz, yy, yz, zz)."""
+    c = np.ascontiguousarray(cov6, np.float64)
+    rot, sc = np.zeros(4), np.zeros(3)
+    lib().vo_ellipsoid_axes_f64(c.ctypes.data_as(_D), rot.ctypes.data_as(_D), sc.ctypes.data_as(_D))
+    return rot, sc
+
+
+def ellipsoid_axes_f32(cov6: np.ndarray) -> tuple:
+    """Rotations (n, 4) and scales (n, 3) of n float covariances (n, 6)."""
+    c = np.ascontiguousarray(cov6, np.float32).reshape(-1, 6)
+    n = c.shape[0]
+    rot, sc = np.zeros((n, 4), np.float32), np.zeros((n, 3), np.float32)
+    lib().vo_ellipsoid_axes_f32(c.ctypes.data_as(_F), n, rot.ctypes.data_as(_F), sc.ctypes.data_as(_F))
+    return rot, sc
 
 
 def stable_sort(keys: np.ndarray, key_bits: int = 32) -> np.ndarray:

@@ -874,6 +874,63 @@ void deformedCovariance(const M3<T>& F, const T q[4], const T scale[3], T out6[6
     out6[5] = cov.c[2].z;
 }
 
+// ellipsoid.wgsl:20-91 (CPU twin apps/simulator/src/render/ellipsoid.js:40-149):
+// a covariance (xx, xy, xz, yy, yz, zz) taken apart into a unit quaternion
+// (xyzw) and three axis lengths by four sweeps of cyclic Jacobi. Evaluation
+// here and in the kernel: inverseSqrt as 1 / sqrt, normalize as q / sqrt(|q|^2)
+// with |q|^2 fused as dot is, everything else one rounding per operation.
+template <class T>
+inline T dot4(const T q[4]) {
+    return std::fma(q[3], q[3], std::fma(q[2], q[2], std::fma(q[1], q[1], q[0] * q[0])));
+}
+
+template <class T>
+void ellipsoidAxes(const T cov6[6], T rotation[4], T scale[3]) {
+    T a[9] = {cov6[0], cov6[1], cov6[2], cov6[1], cov6[3], cov6[4], cov6[2], cov6[4], cov6[5]};
+    T q[4] = {T(0), T(0), T(0), T(1)};
+    for (int sweep = 0; sweep < 4; sweep++) {
+        for (int p = 0; p < 3; p++) {
+            const int r = (p + 1) % 3, other = (p + 2) % 3;
+            const T apr = a[r * 3 + p];
+            if (apr == T(0)) continue;
+            const T app = a[p * 3 + p];
+            const T arr = a[r * 3 + r];
+            const T theta = (arr - app) / (T(2) * apr);
+            const T sign = theta >= T(0) ? T(1) : T(-1);
+            const T tangent = sign / (std::fabs(theta) + std::sqrt(theta * theta + T(1)));
+            const T cosine = T(1) / std::sqrt(tangent * tangent + T(1));
+            const T sine = tangent * cosine;
+            const T apo = a[other * 3 + p];
+            const T aro = a[other * 3 + r];
+            const T turnedP = cosine * apo - sine * aro;
+            const T turnedR = sine * apo + cosine * aro;
+            a[p * 3 + p] = app - tangent * apr;
+            a[r * 3 + r] = arr + tangent * apr;
+            a[r * 3 + p] = T(0);
+            a[p * 3 + r] = T(0);
+            a[other * 3 + p] = turnedP;
+            a[p * 3 + other] = turnedP;
+            a[other * 3 + r] = turnedR;
+            a[r * 3 + other] = turnedR;
+            // q * (half along +other, 1): ellipsoidQuaternionProduct with b
+            // having one imaginary part; the zero terms are exact.
+            const T half = -(sine / (T(1) + cosine));
+            T b[4] = {T(0), T(0), T(0), T(1)};
+            b[other] = half;
+            const T prod[4] = {q[3] * b[0] + q[0] * b[3] + q[1] * b[2] - q[2] * b[1],
+                               q[3] * b[1] - q[0] * b[2] + q[1] * b[3] + q[2] * b[0],
+                               q[3] * b[2] + q[0] * b[1] - q[1] * b[0] + q[2] * b[3],
+                               q[3] * b[3] - q[0] * b[0] - q[1] * b[1] - q[2] * b[2]};
+            const T length = std::sqrt(dot4(prod));
+            for (int c = 0; c < 4; c++) q[c] = prod[c] / length;
+        }
+    }
+    for (int c = 0; c < 4; c++) rotation[c] = q[c];
+    scale[0] = std::sqrt(std::max(a[0], T(0)));
+    scale[1] = std::sqrt(std::max(a[4], T(0)));
+    scale[2] = std::sqrt(std::max(a[8], T(0)));
+}
+
 // Back-to-front draw key: ascending key order is descending depth.
 inline uint32_t depthKey(float depth) {
     uint32_t bits;
@@ -1449,6 +1506,14 @@ void vo_deformed_covariance_f64(const double gradient[9], const double quat[4], 
     out[0] = c6[0], out[1] = c6[1], out[2] = c6[2];
     out[3] = c6[1], out[4] = c6[3], out[5] = c6[4];
     out[6] = c6[2], out[7] = c6[4], out[8] = c6[5];
+}
+
+void vo_ellipsoid_axes_f64(const double cov6[6], double rotation[4], double scale[3]) {
+    ellipsoidAxes(cov6, rotation, scale);
+}
+
+void vo_ellipsoid_axes_f32(const float* cov6, uint32_t n, float* rotation, float* scale) {
+    for (uint32_t i = 0; i < n; i++) ellipsoidAxes(cov6 + 6 * size_t(i), rotation + 4 * size_t(i), scale + 3 * size_t(i));
 }
 
 void vo_stretch_edges(double out[84]) {

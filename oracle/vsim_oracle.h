@@ -127,6 +127,11 @@ void vo_deformation_at_f64(const double* node_pos, const uint32_t node_dims[3],
 /* Sigma' = (F R S)(F R S)^T, column-major 3x3 out (covariance.wgsl:30-42). */
 void vo_deformed_covariance_f64(const double gradient[9], const double quat[4],
                                 const double scale[3], double out[9]);
+/* A covariance (xx, xy, xz, yy, yz, zz) as a unit quaternion xyzw and three
+   axis lengths (ellipsoid.wgsl:20-91), in double and, for n covariances, in
+   float as the GPU evaluates it. */
+void vo_ellipsoid_axes_f64(const double cov6[6], double rotation[4], double scale[3]);
+void vo_ellipsoid_axes_f32(const float* cov6, uint32_t n, float* rotation, float* scale);
 /* 28 stretch edges: corner a, corner b, unit rest length (stretch.js:5-7). */
 void vo_stretch_edges(double out[84]);
 /* Grid layout of broadphase.js:46-58 for a bucket size. */

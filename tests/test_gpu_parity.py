@@ -357,6 +357,32 @@ def test_splats_and_sort(lib):
     assert np.array_equal(order, pyoracle.stable_sort(keys))
 
 
+def test_splat_axes(lib):
+    """The fused ellipsoid decomposition equals the oracle's float evaluation
+    of the same covariances, and leaves means, covariances and keys as the
+    plain deformation writes them."""
+    import pyoracle
+    import vsim.scenes as sc
+
+    scene = sc.noise_blob(n=16, seed=2, splats=20000)
+    sim, orc = make(scene)
+    for frame in range(3):
+        sim.dispatch(scene.substeps)
+    view = (0.3, -0.2, -0.93)
+    sim.deform_splats(view)
+    sim.sort_splats()
+    means, cov, order = sim.read_splats()
+    sim.deform_splats_axes(view)
+    sim.sort_splats()
+    means2, cov2, order2 = sim.read_splats()
+    assert np.array_equal(means, means2) and np.array_equal(cov, cov2) and np.array_equal(order, order2)
+    rot, scale = sim.read_splat_axes()
+    orot, oscale = pyoracle.ellipsoid_axes_f32(cov)
+    assert np.array_equal(rot, orot)
+    assert np.array_equal(scale, oscale)
+    assert np.all(np.abs(np.linalg.norm(rot.astype(np.float64), axis=1) - 1) < 1e-6)
+
+
 @pytest.mark.parametrize("n,bits", [(1, 32), (4095, 32), (4097, 8), (1_000_003, 32), (300_000, 20)])
 def test_radix_sort_matches_stable_sort(lib, gpu, n, bits):
     import torch

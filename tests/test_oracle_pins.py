@@ -593,3 +593,112 @@ def test_lattice_colours_mass_surface(oracle):
     assert np.all(inv[surface] > 0) and np.all(np.diff(surface.astype(np.int64)) > 0)
     mid = (n // 2) + nd[0] * ((n // 2) + nd[1] * (n // 2))
     assert mid not in set(surface.tolist()) and 0 not in set(surface.tolist())
+
+
+# ---- ellipsoid.test.js (apps/simulator/test/unit/ellipsoid.test.js) ---------------
+
+def _stream(seed):
+    """ellipsoid.test.js:95-98, in JavaScript's double arithmetic."""
+    state = float(seed)
+
+    def nxt():
+        nonlocal state
+        state = math.fmod(state * 1103515245.0 + 12345.0, 2147483648.0)
+        return state / 2147483648.0
+
+    return nxt
+
+
+def _rotation(nxt):
+    q = np.array([nxt() * 2 - 1 for _ in range(4)])
+    return q / np.linalg.norm(q)
+
+
+def _ellipsoid_cov(rot, scale):
+    """R diag(s)^2 R^T (ellipsoid.test.js:55-64)."""
+    x, y, z, w = rot
+    r = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                  [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                  [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+    return r @ np.diag(np.asarray(scale) ** 2) @ r.T
+
+
+def _six(m):
+    return np.array([m[0, 0], m[1, 0], m[2, 0], m[1, 1], m[2, 1], m[2, 2]])
+
+
+def _axes(m):
+    import pyoracle
+
+    return pyoracle.ellipsoid_axes_f64(_six(m))
+
+
+def _close(actual, expected, tol):
+    return np.max(np.abs(actual - expected)) / np.max(np.abs(expected)) < tol
+
+
+def test_ellipsoid_identity(oracle):
+    # ellipsoid.test.js:126-135: an undeformed ellipsoid comes back unchanged
+    rest = _rotation(_stream(11))
+    scale = [0.02, 0.006, 0.0004]
+    rot, sc = _axes(_ellipsoid_cov(rest, scale))
+    assert _close(_ellipsoid_cov(rot, sc), _ellipsoid_cov(rest, scale), 1e-9)
+
+
+def test_ellipsoid_diagonal(oracle):
+    # ellipsoid.test.js:137-146
+    rot, sc = _axes(np.diag([0.0004, 0.0036, 0.0004]))
+    assert np.allclose(np.sort(sc), [0.02, 0.02, 0.06], atol=5e-10, rtol=0)
+
+
+def test_ellipsoid_reconstructs(oracle):
+    # ellipsoid.test.js:148-166: 2000 carried covariances, flat splats included
+    nxt = _stream(20260810)
+    for trial in range(2000):
+        amp = [0.05, 0.4, 1.5][trial % 3]
+        g = np.eye(3).T.ravel() + np.array([(nxt() * 2 - 1) * amp for _ in range(9)])
+        g = g.reshape(3, 3).T
+        rot = _rotation(nxt)
+        flat = trial % 4 == 0
+        scale = [v * (0.5 + nxt()) * 0.02 for v in (1, 0.3, 0.003 if flat else 0.1)]
+        expected = g @ _ellipsoid_cov(rot, scale) @ g.T
+        r, s = _axes(expected)
+        assert _close(_ellipsoid_cov(r, s), expected, 1e-9), f"trial {trial}"
+
+
+def test_ellipsoid_unit_quaternion(oracle):
+    # ellipsoid.test.js:168-181
+    nxt = _stream(7)
+    for trial in range(500):
+        g = (np.eye(3).T.ravel() + np.array([(nxt() * 2 - 1) * 0.8 for _ in range(9)])).reshape(3, 3).T
+        r, _ = _axes(g @ _ellipsoid_cov(_rotation(nxt), [0.02, 0.01, 0.0002]) @ g.T)
+        assert abs(math.hypot(*r) - 1) < 5e-10, f"trial {trial}"
+
+
+def test_ellipsoid_degenerate(oracle):
+    # ellipsoid.test.js:183-196: a flattened ellipsoid loses an axis, not the splat
+    flattening = np.array([[1, 0, 0], [0, 0, 0], [0, 0, 1]], float)
+    m = flattening @ _ellipsoid_cov(_rotation(_stream(3)), [0.02, 0.01, 0.005]) @ flattening.T
+    r, s = _axes(m)
+    assert np.all(np.isfinite(s)) and np.all(np.isfinite(r))
+    assert np.sort(s)[0] < 1e-9 and np.sort(s)[2] > 1e-3
+
+
+def test_ellipsoid_float_evaluation_reconstructs(oracle):
+    """The float evaluation (what the GPU computes) keeps f32-level accuracy
+    on the same carried covariances."""
+    import pyoracle
+
+    nxt = _stream(20260810)
+    covs, expected = [], []
+    for trial in range(500):
+        amp = [0.05, 0.4, 1.5][trial % 3]
+        g = (np.eye(3).T.ravel() + np.array([(nxt() * 2 - 1) * amp for _ in range(9)])).reshape(3, 3).T
+        rot = _rotation(nxt)
+        scale = [v * (0.5 + nxt()) * 0.02 for v in (1, 0.3, 0.1)]
+        e = g @ _ellipsoid_cov(rot, scale) @ g.T
+        covs.append(_six(e))
+        expected.append(e)
+    rots, scales = pyoracle.ellipsoid_axes_f32(np.array(covs))
+    for r, s, e in zip(rots.astype(np.float64), scales.astype(np.float64), expected):
+        assert _close(_ellipsoid_cov(r, s), e, 1e-4)

@@ -197,10 +197,14 @@ struct SplatState {
     uint32_t* order = nullptr;
     void* sortTemp = nullptr;
     size_t sortTempBytes = 0;
+    float4* axesRotation = nullptr;  // per splat: the deformed ellipsoid's unit quaternion xyzw
+    float4* axesScale = nullptr;     //   ... and its axis lengths xyz (allocated on first use)
 };
 
+// With `axes` the deformation also takes each covariance apart into a
+// rotation and axis lengths (s.axesRotation, s.axesScale).
 cudaError_t launchSplatDeform(cudaStream_t st, const SplatState& s, const float4* pos, uint32_t n, float vx, float vy,
-                              float vz);
+                              float vz, bool axes = false);
 
 // ---- radix sort -------------------------------------------------------------
 

@@ -1267,7 +1267,8 @@ namespace {
 
 int rebuildSplats(vsim_sim* s) {
     SplatState& sp = s->sp;
-    void* old[] = {sp.embed, sp.quat, sp.scaleBody, sp.bodies, sp.meanDepth, sp.cov, sp.keys, sp.order, sp.sortTemp};
+    void* old[] = {sp.embed,  sp.quat,  sp.scaleBody, sp.bodies,       sp.meanDepth, sp.cov,
+                   sp.keys,   sp.order, sp.sortTemp,  sp.axesRotation, sp.axesScale};
     CK(cudaStreamSynchronize(s->stream), "rebind splats");
     for (void* p : old)
         if (p) cudaFree(p);
@@ -1351,6 +1352,44 @@ int vsim_splats_deform(vsim_sim* s, const float view_dir[3]) {
     if (s->splatCount == 0) return VSIM_OK;
     CK(launchSplatDeform(s->stream, s->sp, s->d.pos, s->splatCount, view_dir[0], view_dir[1], view_dir[2]),
        "deform splats");
+    return VSIM_OK;
+}
+
+int vsim_splats_deform_axes(vsim_sim* s, const float view_dir[3]) {
+    SIM_GUARD(s);
+    if (!view_dir) return fail(VSIM_ERR_INVALID, "view_dir is NULL");
+    if (s->splatCount == 0) return VSIM_OK;
+    if (!s->sp.axesRotation) {
+        CK(allocN(&s->sp.axesRotation, s->splatCount), "allocate splat axes");
+        CK(allocN(&s->sp.axesScale, s->splatCount), "allocate splat axes");
+    }
+    CK(launchSplatDeform(s->stream, s->sp, s->d.pos, s->splatCount, view_dir[0], view_dir[1], view_dir[2], true),
+       "deform splats");
+    return VSIM_OK;
+}
+
+int vsim_splats_read_axes(vsim_sim* s, float* rotation, float* scale, size_t count) {
+    SIM_GUARD(s);
+    if (count != s->splatCount) return fail(VSIM_ERR_CAPACITY, "count does not match the bound splats");
+    if (count == 0) return VSIM_OK;
+    if (!s->sp.axesRotation) return fail(VSIM_ERR_INVALID, "no axes yet: call vsim_splats_deform_axes first");
+    std::vector<float4> rot(count), sc(count);
+    CK(cudaMemcpyAsync(rot.data(), s->sp.axesRotation, count * 16, cudaMemcpyDeviceToHost, s->stream), "read axes");
+    CK(cudaMemcpyAsync(sc.data(), s->sp.axesScale, count * 16, cudaMemcpyDeviceToHost, s->stream), "read axes");
+    CK(cudaStreamSynchronize(s->stream), "read axes");
+    for (size_t i = 0; i < count; i++) {
+        if (rotation) {
+            rotation[4 * i] = rot[i].x;
+            rotation[4 * i + 1] = rot[i].y;
+            rotation[4 * i + 2] = rot[i].z;
+            rotation[4 * i + 3] = rot[i].w;
+        }
+        if (scale) {
+            scale[3 * i] = sc[i].x;
+            scale[3 * i + 1] = sc[i].y;
+            scale[3 * i + 2] = sc[i].z;
+        }
+    }
     return VSIM_OK;
 }
 

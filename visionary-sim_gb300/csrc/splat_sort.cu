@@ -20,6 +20,58 @@ __device__ __forceinline__ uint32_t depthKey(float depth) {
 // eight live nodes, then Sigma' = (F R S)(F R S)^T, then the depth key. The
 // embedding (cell corner node, local coordinates) was computed at bind time
 // with sample.wgsl:45-51's arithmetic.
+// ellipsoid.wgsl:20-91: a covariance (xx, xy, xz, yy, yz, zz) as a unit
+// quaternion xyzw and three axis lengths, by four sweeps of cyclic Jacobi.
+// inverseSqrt is 1 / sqrt and normalize is q / sqrt(|q|^2) with |q|^2 fused
+// as dot is; every other operation rounds once -- the CPU restatement's
+// evaluation, so the two agree bit for bit.
+__device__ __forceinline__ void ellipsoidAxes(const float cov[6], float4& rotation, float4& scale) {
+    float a[9] = {cov[0], cov[1], cov[2], cov[1], cov[3], cov[4], cov[2], cov[4], cov[5]};
+    float q[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+#pragma unroll
+    for (int sweep = 0; sweep < 4; sweep++) {
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+            const int r = (p + 1) % 3, other = (p + 2) % 3;
+            const float apr = a[r * 3 + p];
+            if (apr == 0.0f) continue;
+            const float app = a[p * 3 + p];
+            const float arr = a[r * 3 + r];
+            const float theta = (arr - app) / (2.0f * apr);
+            const float sign = theta >= 0.0f ? 1.0f : -1.0f;
+            const float tangent = sign / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+            const float cosine = 1.0f / sqrtf(tangent * tangent + 1.0f);
+            const float sine = tangent * cosine;
+            const float apo = a[other * 3 + p];
+            const float aro = a[other * 3 + r];
+            const float turnedP = cosine * apo - sine * aro;
+            const float turnedR = sine * apo + cosine * aro;
+            a[p * 3 + p] = app - tangent * apr;
+            a[r * 3 + r] = arr + tangent * apr;
+            a[r * 3 + p] = 0.0f;
+            a[p * 3 + r] = 0.0f;
+            a[other * 3 + p] = turnedP;
+            a[p * 3 + other] = turnedP;
+            a[other * 3 + r] = turnedR;
+            a[r * 3 + other] = turnedR;
+            const float half = -(sine / (1.0f + cosine));
+            float b[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+            b[other] = half;
+            const float prod[4] = {q[3] * b[0] + q[0] * b[3] + q[1] * b[2] - q[2] * b[1],
+                                   q[3] * b[1] - q[0] * b[2] + q[1] * b[3] + q[2] * b[0],
+                                   q[3] * b[2] + q[0] * b[1] - q[1] * b[0] + q[2] * b[3],
+                                   q[3] * b[3] - q[0] * b[0] - q[1] * b[1] - q[2] * b[2]};
+            const float length =
+                sqrtf(fmaf(prod[3], prod[3], fmaf(prod[2], prod[2], fmaf(prod[1], prod[1], prod[0] * prod[0]))));
+#pragma unroll
+            for (int c = 0; c < 4; c++) q[c] = prod[c] / length;
+        }
+    }
+    rotation = make_float4(q[0], q[1], q[2], q[3]);
+    scale = make_float4(sqrtf(fmaxf(a[0], 0.0f)), sqrtf(fmaxf(a[4], 0.0f)), sqrtf(fmaxf(a[8], 0.0f)), 0.0f);
+}
+
+template <bool AXES>
 __global__ void __launch_bounds__(256) splatDeformKernel(const float4* __restrict__ embed,
                                                          const float4* __restrict__ quat,
                                                          const float4* __restrict__ scaleBody,
@@ -27,7 +79,9 @@ __global__ void __launch_bounds__(256) splatDeformKernel(const float4* __restric
                                                          const float4* __restrict__ pos, uint32_t n, float vx,
                                                          float vy, float vz, float4* __restrict__ meanDepth,
                                                          float2* __restrict__ cov, uint32_t* __restrict__ keys,
-                                                         uint32_t* __restrict__ order) {
+                                                         uint32_t* __restrict__ order,
+                                                         float4* __restrict__ axesRotation,
+                                                         float4* __restrict__ axesScale) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 e = embed[i];
@@ -76,13 +130,23 @@ __global__ void __launch_bounds__(256) splatDeformKernel(const float4* __restric
     cov[3 * i + 2] = make_float2(yz, zz);
     keys[i] = depthKey(depth);
     (void)order;
+    if (AXES) {
+        const float c6[6] = {xx, xy, xz, yy, yz, zz};
+        ellipsoidAxes(c6, axesRotation[i], axesScale[i]);
+    }
 }
 
 cudaError_t launchSplatDeform(cudaStream_t st, const SplatState& s, const float4* pos, uint32_t n, float vx, float vy,
-                              float vz) {
+                              float vz, bool axes) {
     if (n == 0) return cudaSuccess;
-    splatDeformKernel<<<(n + 255) / 256, 256, 0, st>>>(s.embed, s.quat, s.scaleBody, s.bodies, pos, n, vx, vy, vz,
-                                                       s.meanDepth, s.cov, s.keys, s.order);
+    if (axes)
+        splatDeformKernel<true><<<(n + 255) / 256, 256, 0, st>>>(s.embed, s.quat, s.scaleBody, s.bodies, pos, n, vx,
+                                                                 vy, vz, s.meanDepth, s.cov, s.keys, s.order,
+                                                                 s.axesRotation, s.axesScale);
+    else
+        splatDeformKernel<false><<<(n + 255) / 256, 256, 0, st>>>(s.embed, s.quat, s.scaleBody, s.bodies, pos, n, vx,
+                                                                  vy, vz, s.meanDepth, s.cov, s.keys, s.order,
+                                                                  nullptr, nullptr);
     return cudaGetLastError();
 }
 

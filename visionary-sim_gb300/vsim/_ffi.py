@@ -196,6 +196,8 @@ SIGNATURES = {
     "vsim_splats_count": (C.c_uint32, [_P]),
     "vsim_splats_deform": (C.c_int, [_P, _F]),
     "vsim_splats_sort": (C.c_int, [_P]),
+    "vsim_splats_deform_axes": (C.c_int, [_P, _F]),
+    "vsim_splats_read_axes": (C.c_int, [_P, _F, _F, _SZ]),
     "vsim_splats_read": (C.c_int, [_P, _F, _F, _U, _SZ]),
     "vsim_radix_sort_u32": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P, C.POINTER(_SZ), _P]),
     "vsim_radix_sort_u32_noalloc": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P]),

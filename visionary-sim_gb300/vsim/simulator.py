@@ -351,6 +351,19 @@ class Simulator:
     def sort_splats(self):
         check(lib().vsim_splats_sort(self._h))
 
+    def deform_splats_axes(self, view_dir=(0.0, 0.0, -1.0)):
+        """deform_splats, plus each ellipsoid's rotation and axis lengths."""
+        v = np.asarray(view_dir, np.float32)
+        check(lib().vsim_splats_deform_axes(self._h, fptr(v)))
+
+    def read_splat_axes(self):
+        """(rotations (n, 4) xyzw, axis lengths (n, 3)) of the last deform_splats_axes."""
+        n = self.splat_count
+        rot = np.zeros((n, 4), np.float32)
+        scale = np.zeros((n, 3), np.float32)
+        check(lib().vsim_splats_read_axes(self._h, fptr(rot), fptr(scale), n))
+        return rot, scale
+
     def read_splats(self, order: bool = True):
         n = self.splat_count
         means = np.zeros((n, 3), np.float32)

@@ -200,6 +200,28 @@ int vsim_move_grab(vsim_sim* sim, const double position[3]);
 int vsim_place_grab(vsim_sim* sim, const double position[3]);
 /* Simulator.releaseGrab() / KinematicDrive.release(). */
 int vsim_release(vsim_sim* sim);
+
+/* Simulator.grab(origin, direction) (simulator.js:383-425) without reading
+   the node positions back: the nearest grabbable node along the ray within
+   1.2 x the coarsest node spacing of it (pick.js:41-68), then the grip --
+   the anchor alone, or every grabbable node of the anchor's body within
+   `grip_radius` of it, nearest first, ties by index, at most
+   VSIM_MAX_DRIVEN (grip.js:58-136) -- is held and the grab target placed
+   on the anchor. Picking and gripping run on the device in double
+   precision, as the reference's JavaScript does; only the anchor and the
+   candidates within the radius come back. A ray that hits nothing holds
+   nothing: out->body = -1. */
+#define VSIM_GRIP_SINGLE_NODE 0
+#define VSIM_GRIP_WITHIN_RADIUS 1
+typedef struct vsim_grab_result {
+    int32_t body;        /* the anchor's body, -1 when the ray missed */
+    uint32_t anchor;     /* global node */
+    double position[3];  /* the anchor's position: the grab target */
+    uint32_t held;       /* nodes held */
+    uint32_t found;      /* grabbable nodes within the grip radius, anchor included */
+} vsim_grab_result;
+int vsim_grab(vsim_sim* sim, const double origin[3], const double direction[3], int grip, double grip_radius,
+              vsim_grab_result* out);
 /* Simulator.setDriveLaw(law). */
 int vsim_set_drive_law(vsim_sim* sim, int law);
 /* Simulator.setDriveResponseTime(seconds): finite and > 0, else RANGE. */

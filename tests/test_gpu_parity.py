@@ -249,6 +249,52 @@ def test_drive_laws(lib, law):
     assert_same(sim, orc, scene, f"{law} after release")
 
 
+@pytest.mark.parametrize("strategy", ["singleNode", "withinRadius"])
+def test_device_grab_matches_host_grab(lib, strategy):
+    """vsim_grab (pick and grip on the device) holds what pick.js / grip.js
+    pick and grip from read-back positions: same anchor, same held set and
+    offsets (the next frames equal the oracle holding the host's set), and a
+    ray that misses holds nothing."""
+    import vsim.scenes as sc
+    from vsim import simulator as vs
+
+    scene = sc.noise_blob(n=16, seed=3, splats=0)
+    sim, orc = make(scene)
+    for _ in range(3):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+    sim.set_grip(strategy)
+    sim.set_grip_radius(0.03)
+    nodes = sim.read_positions()
+    centre = nodes[np.asarray(sim.inv_mass) > 0, :3].mean(axis=0).astype(np.float64)
+    origin = centre + np.array([0.05, 0.6, 0.1])
+    direction = (centre - origin) / np.linalg.norm(centre - origin)
+
+    aim = max(b.h for b in scene.bodies) * 1.2
+    anchor = vs.nearest_node_to_ray(nodes, sim.inv_mass, origin, direction, aim, sim.static)
+    assert anchor >= 0
+    if strategy == "singleNode":
+        held, offs, found = vs.single_node(nodes, sim.inv_mass, anchor, sim.static)
+    else:
+        held, offs, found = vs.within_radius(nodes, sim.inv_mass, anchor, 0.03, sim.offsets, sim.static, 4096)
+    got = sim.grab(origin, direction)
+    assert got["anchor"] == anchor and got["held"] == len(held) and got["found"] == found
+    assert got["position"] == [float(v) for v in nodes[anchor, :3]]
+    assert orc.hold(np.asarray(held, np.uint32), np.asarray(offs, np.float32).reshape(-1, 3)) == 0
+    target = np.asarray(got["position"], np.float64)
+    previous = target.copy()
+    for frame in range(4):
+        target = target + np.array([0.0, 0.003, 0.001])
+        sim.move_grab(target)
+        orc.set_grab(target, grab_velocity(target, previous, scene.substeps, scene.step_duration))
+        previous = target.copy()
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"{strategy} frame {frame}")
+    sim.release_grab()
+    assert sim.grab(origin, -direction) is None
+
+
 def test_errors_map_to_reference_throws(lib):
     import vsim.scenes as sc
     from vsim import VsimError, VsimRangeError

@@ -124,6 +124,15 @@ class Completion(C.Structure):
                 ("last_tick", C.c_uint64)]
 
 
+class GrabResult(C.Structure):
+    _fields_ = [("body", C.c_int32), ("anchor", C.c_uint32), ("position", C.c_double * 3), ("held", C.c_uint32),
+                ("found", C.c_uint32)]
+
+
+VSIM_GRIP_SINGLE_NODE = 0
+VSIM_GRIP_WITHIN_RADIUS = 1
+
+
 class ServerStats(C.Structure):
     _fields_ = [("sessions", C.c_uint32), ("rejected", C.c_uint32), ("resident_bytes", C.c_double),
                 ("ticks", C.c_uint64), ("session_frames", C.c_uint64), ("cell_updates", C.c_uint64),
@@ -186,6 +195,7 @@ SIGNATURES = {
     "vsim_tune": (C.c_int, [_P, C.c_uint32, _U, _U]),
     "vsim_set_pdl": (C.c_int, [_P, C.c_int]),
     "vsim_set_gather_mapping": (C.c_int, [_P, C.c_int]),
+    "vsim_grab": (C.c_int, [_P, _D, _D, C.c_int, C.c_double, C.POINTER(GrabResult)]),
     "vsim_time_colour_passes": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_float)]),
     "vsim_kuhn_rest_inverse": (C.c_int, [_F]),
     "vsim_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),

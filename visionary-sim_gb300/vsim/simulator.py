@@ -157,7 +157,21 @@ class Simulator:
 
     # -- grab (simulator.js:383-492) ---------------------------------------------
     def grab(self, origin, direction):
-        """Hold what the ray hits: {'bodyIndex', 'position', 'held'} or None."""
+        """Simulator.grab (simulator.js:383-425), picked and gripped on the
+        device (vsim_grab): {'bodyIndex', 'position', 'held'} or None."""
+        res = _ffi.GrabResult()
+        o = np.asarray(origin, np.float64)
+        d = np.asarray(direction, np.float64)
+        grip = _ffi.VSIM_GRIP_SINGLE_NODE if self.grip["strategy"] == "singleNode" else _ffi.VSIM_GRIP_WITHIN_RADIUS
+        check(lib().vsim_grab(self._h, dptr(o), dptr(d), grip, float(self.grip["radius"]), C.byref(res)))
+        if res.body < 0:
+            return None
+        return {"bodyIndex": int(res.body), "position": [float(v) for v in res.position], "held": int(res.held),
+                "anchor": int(res.anchor), "found": int(res.found)}
+
+    def grab_on_host(self, origin, direction):
+        """The same grab with every node position read back and picked and
+        gripped in Python, as the reference does (pick.js, grip.js)."""
         nodes = self.read_positions()
         aim = max(b.h for b in self.scene.bodies) * 1.2
         anchor = nearest_node_to_ray(nodes, self.inv_mass, origin, direction, aim, self.static)

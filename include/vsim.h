@@ -477,6 +477,17 @@ int vsim_server_get_stats(const vsim_server* server, vsim_server_stats* out);
 uint32_t vsim_server_node_count(const vsim_server* server, uint32_t session);
 /* The session's node positions, xyzw, w = 0. */
 int vsim_server_read_positions(vsim_server* server, uint32_t session, float* xyzw, size_t node_count);
+/* Checkpoint and restore of one session (any pointer may be NULL): its
+   positions, previous positions and velocities, xyzw per node (w = 0 out,
+   ignored in). Writing or resetting needs the session idle (no request
+   queued or running, else VSIM_ERR_INVALID); a drag still held from its last
+   request is let go first. A session written back continues exactly as the
+   one read out would have. Reset returns it to its rest state. */
+int vsim_server_read_state(vsim_server* server, uint32_t session, float* pos, float* prev, float* vel,
+                           size_t node_count);
+int vsim_server_write_state(vsim_server* server, uint32_t session, const float* pos, const float* prev,
+                            const float* vel, size_t node_count);
+int vsim_server_reset_session(vsim_server* server, uint32_t session);
 
 /* ---- fixed timestep clock (timestep.js:17-180), host only ------------- */
 

@@ -151,3 +151,48 @@ def test_budget_admission(lib):
     st = tight.stats()
     assert 1 <= tight.admitted < 8 and st["rejected"] == 8 - tight.admitted
     assert st["resident_bytes"] <= per * 3
+
+
+def test_session_checkpoint_restore_and_reset(lib):
+    """A session read out, run on, written back and run again with the same
+    requests ends exactly where the first run did; a pending session refuses
+    to be overwritten; reset returns it to rest."""
+    import vsim.scenes as sc
+    from vsim import _ffi
+    from vsim.server import Server
+
+    bodies, tank = small_pool(3, seed=17)
+    rng = np.random.default_rng(4)
+    drag = sc.drag_request(bodies[1], rng)
+    server = Server(bodies, tank)
+    rest = server.read_state(1)
+
+    def run(requests):
+        for session, frames, d in requests:
+            server.submit(session, frames, d)
+        while server.stats()["pending"]:
+            server.tick()
+        server.poll()
+
+    run([(1, 3, drag), (2, 2, None)])
+    checkpoint = server.read_state(1)
+    run([(1, 4, drag), (0, 1, None)])
+    first = server.read_state(1)
+    assert not np.array_equal(first[0], checkpoint[0])
+
+    server.write_state(1, *checkpoint)
+    assert all(np.array_equal(a, b) for a, b in zip(server.read_state(1), checkpoint))
+    run([(1, 4, drag), (2, 3, None)])  # other sessions' work differs; session 1's must not
+    second = server.read_state(1)
+    for a, b in zip(first, second):
+        assert np.array_equal(a, b)
+
+    server.submit(1, 1)
+    with pytest.raises(_ffi.VsimError):
+        server.write_state(1, *checkpoint)
+    while server.stats()["pending"]:
+        server.tick()
+    server.reset_session(1)
+    for a, b in zip(server.read_state(1), rest):
+        assert np.array_equal(a, b)
+    server.destroy()

@@ -49,6 +49,11 @@ void bezier(const float c[4][3], double t, double p[3], double dp[3]) {
 
 }  // namespace
 
+struct vsim_server;
+namespace {
+int applyHolds(vsim_server* s);
+}
+
 struct vsim_server {
     vsim_sim* sim = nullptr;
     uint32_t admitted = 0, rejected = 0;
@@ -68,6 +73,27 @@ struct vsim_server {
 };
 
 namespace {
+
+// Holds exactly the nodes the sessions' current drags name (held[i] >= 0).
+int applyHolds(vsim_server* s) {
+    std::vector<uint32_t> nodes;
+    for (uint32_t i = 0; i < s->admitted; i++)
+        if (s->held[i] >= 0) nodes.push_back(uint32_t(s->held[i]));
+    const std::vector<float> zero(3 * nodes.size(), 0.0f);
+    return nodes.empty() ? releaseNodes(s->sim) : holdNodes(s->sim, nodes.data(), zero.data(), uint32_t(nodes.size()));
+}
+
+// A session's state may be read, replaced or reset only between its
+// requests; a drag it still holds from its last request is let go first.
+int idleSession(vsim_server* s, uint32_t session) {
+    if (session >= s->admitted) return fail(VSIM_ERR_RANGE, "session is not resident");
+    if (!s->queue[session].empty()) return fail(VSIM_ERR_INVALID, "session has requests pending");
+    if (s->held[session] >= 0) {
+        s->held[session] = -1;
+        return applyHolds(s);
+    }
+    return VSIM_OK;
+}
 
 double seconds(const vsim_server* s) {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - s->origin).count();
@@ -227,11 +253,13 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
         if (want != s->held[i]) {
             holdChanged = true;
             s->held[i] = want;
-            if (want >= 0) {  // a fresh drag starts on its curve (the grab's placement)
-                double p[3], dp[3];
-                bezier(s->queue[i].front().path.control, 0.0, p, dp);
-                for (int a = 0; a < 3; a++) s->prevTarget[3 * i + a] = p[a];
-            }
+        }
+        if (want >= 0 && s->queue[i].front().done == 0) {
+            // A request's drag starts on its curve (the grab's placement),
+            // whatever the session held before.
+            double p[3], dp[3];
+            bezier(s->queue[i].front().path.control, 0.0, p, dp);
+            for (int a = 0; a < 3; a++) s->prevTarget[3 * i + a] = p[a];
         }
         const uint32_t flag = busy ? 1u : 0u;
         if (sim->activeHost[i] != flag) {
@@ -242,11 +270,7 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
     }
     if (active == 0) return VSIM_OK;
     if (holdChanged) {
-        std::vector<uint32_t> nodes;
-        for (uint32_t i = 0; i < s->admitted; i++)
-            if (s->held[i] >= 0) nodes.push_back(uint32_t(s->held[i]));
-        const std::vector<float> zero(3 * nodes.size(), 0.0f);
-        const int rc = nodes.empty() ? releaseNodes(sim) : holdNodes(sim, nodes.data(), zero.data(), uint32_t(nodes.size()));
+        const int rc = applyHolds(s);
         if (rc) return rc;
     }
     // Drag targets advance one frame along their curves at their speed;
@@ -332,6 +356,68 @@ int vsim_server_get_stats(const vsim_server* s, vsim_server_stats* out) {
 
 uint32_t vsim_server_node_count(const vsim_server* s, uint32_t session) {
     return s && session < s->admitted ? s->sim->lat[session].nodeCount : 0;
+}
+
+int vsim_server_read_state(vsim_server* s, uint32_t session, float* pos, float* prev, float* vel,
+                           size_t node_count) {
+    clearError();
+    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
+    vsim_sim* sim = s->sim;
+    DeviceGuard guard(sim->device);
+    if (session >= s->admitted) return fail(VSIM_ERR_RANGE, "session is not resident");
+    if (node_count != sim->lat[session].nodeCount) return fail(VSIM_ERR_CAPACITY, "node_count does not match");
+    const size_t first = sim->offsets[session];
+    float* out[3] = {pos, prev, vel};
+    const float4* from[3] = {sim->d.pos + first, sim->d.prev + first, sim->d.vel + first};
+    for (int a = 0; a < 3; a++)
+        if (out[a])
+            CK(cudaMemcpyAsync(out[a], from[a], node_count * 16, cudaMemcpyDeviceToHost, sim->stream), "read session");
+    CK(cudaStreamSynchronize(sim->stream), "read session");
+    for (int a = 0; a < 3; a++)
+        if (out[a])
+            for (size_t n = 0; n < node_count; n++) out[a][4 * n + 3] = 0.0f;
+    return VSIM_OK;
+}
+
+int vsim_server_write_state(vsim_server* s, uint32_t session, const float* pos, const float* prev, const float* vel,
+                            size_t node_count) {
+    clearError();
+    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
+    vsim_sim* sim = s->sim;
+    DeviceGuard guard(sim->device);
+    int rc = idleSession(s, session);
+    if (rc) return rc;
+    if (node_count != sim->lat[session].nodeCount) return fail(VSIM_ERR_CAPACITY, "node_count does not match");
+    const size_t first = sim->offsets[session];
+    if (pos) {
+        if (!sim->staging) CK(allocN(&sim->staging, sim->nodeCount), "allocate staging");
+        CK(cudaMemcpyAsync(sim->staging, pos, node_count * 16, cudaMemcpyHostToDevice, sim->stream), "write session");
+        CK(launchMergeXyz(sim->stream, sim->staging, uint32_t(node_count), sim->d.pos + first), "write session");
+    }
+    if (prev)
+        CK(cudaMemcpyAsync(sim->d.prev + first, prev, node_count * 16, cudaMemcpyHostToDevice, sim->stream),
+           "write session");
+    if (vel)
+        CK(cudaMemcpyAsync(sim->d.vel + first, vel, node_count * 16, cudaMemcpyHostToDevice, sim->stream),
+           "write session");
+    CK(cudaStreamSynchronize(sim->stream), "write session");
+    return VSIM_OK;
+}
+
+int vsim_server_reset_session(vsim_server* s, uint32_t session) {
+    clearError();
+    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
+    vsim_sim* sim = s->sim;
+    DeviceGuard guard(sim->device);
+    int rc = idleSession(s, session);
+    if (rc) return rc;
+    const size_t first = sim->offsets[session], n = sim->lat[session].nodeCount;
+    const float* rest = sim->restPos.data() + 4 * first;
+    CK(cudaMemcpyAsync(sim->d.pos + first, rest, n * 16, cudaMemcpyHostToDevice, sim->stream), "reset session");
+    CK(cudaMemcpyAsync(sim->d.prev + first, rest, n * 16, cudaMemcpyHostToDevice, sim->stream), "reset session");
+    CK(cudaMemsetAsync(sim->d.vel + first, 0, n * 16, sim->stream), "reset session");
+    CK(cudaStreamSynchronize(sim->stream), "reset session");
+    return VSIM_OK;
 }
 
 int vsim_server_read_positions(vsim_server* s, uint32_t session, float* xyzw, size_t node_count) {

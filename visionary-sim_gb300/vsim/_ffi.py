@@ -166,6 +166,9 @@ SIGNATURES = {
     "vsim_server_get_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "vsim_server_node_count": (C.c_uint32, [_P, C.c_uint32]),
     "vsim_server_read_positions": (C.c_int, [_P, C.c_uint32, _F, _SZ]),
+    "vsim_server_read_state": (C.c_int, [_P, C.c_uint32, _F, _F, _F, _SZ]),
+    "vsim_server_write_state": (C.c_int, [_P, C.c_uint32, _F, _F, _F, _SZ]),
+    "vsim_server_reset_session": (C.c_int, [_P, C.c_uint32]),
     "vsim_step": (C.c_int, [_P, C.c_double]),
     "vsim_request_step": (C.c_int, [_P]),
     "vsim_dispatch": (C.c_int, [_P, C.c_uint32]),

@@ -84,3 +84,21 @@ class Server:
         out = np.zeros((n, 4), np.float32)
         check(lib().vsim_server_read_positions(self._h, int(session), fptr(out), n))
         return out
+
+    def read_state(self, session: int):
+        """(pos, prev, vel) of one session, (n, 4) float32 each, w = 0."""
+        n = int(lib().vsim_server_node_count(self._h, int(session)))
+        out = [np.zeros((n, 4), np.float32) for _ in range(3)]
+        check(lib().vsim_server_read_state(self._h, int(session), fptr(out[0]), fptr(out[1]), fptr(out[2]), n))
+        return tuple(out)
+
+    def write_state(self, session: int, pos, prev, vel):
+        """Restore a checkpoint of an idle session (read_state's arrays)."""
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (pos, prev, vel)]
+        check(lib().vsim_server_write_state(self._h, int(session), fptr(arrs[0]), fptr(arrs[1]), fptr(arrs[2]),
+                                            arrs[0].shape[0]))
+
+    def reset_session(self, session: int):
+        """An idle session back to its rest state."""
+        check(lib().vsim_server_reset_session(self._h, int(session)))
+

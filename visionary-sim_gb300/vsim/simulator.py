@@ -31,8 +31,10 @@ def nearest_node_to_ray(nodes, inv_mass, origin, direction, radius, static) -> i
     """pick.js:41-68: the nearest grabbable node along the ray within `radius`
     of it; -1 if none. Ties along the ray keep the lowest index."""
     d = nodes[:, :3].astype(np.float64) - np.asarray(origin, np.float64)
-    depth = d @ np.asarray(direction, np.float64)
-    off_axis = np.einsum("ij,ij->i", d, d) - depth * depth
+    u = np.asarray(direction, np.float64)
+    # Left to right, as JavaScript evaluates pick.js:57-62.
+    depth = d[:, 0] * u[0] + d[:, 1] * u[1] + d[:, 2] * u[2]
+    off_axis = d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2] - depth * depth
     ok = is_grabbable(inv_mass, static) & (depth > 0) & (off_axis <= radius * radius)
     if not ok.any():
         return -1
@@ -66,7 +68,7 @@ def within_radius(positions, inv_mass, anchor, radius, offsets, static, limit):
     idx = np.arange(start, end)
     ok = is_grabbable(inv_mass[start:end], static[start:end]) & (idx != anchor)
     rel = positions[start:end, :3].astype(np.float64) - positions[anchor, :3].astype(np.float64)
-    dist2 = np.einsum("ij,ij->i", rel, rel)
+    dist2 = rel[:, 0] * rel[:, 0] + rel[:, 1] * rel[:, 1] + rel[:, 2] * rel[:, 2]  # grip.js:118-121
     ok &= dist2 <= radius * radius
     cand = idx[ok]
     order = np.lexsort((cand, dist2[ok]))

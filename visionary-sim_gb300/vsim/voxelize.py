@@ -205,8 +205,23 @@ def voxelize_mesh(mesh: Mesh, bounds, element_size: float, padding: int = DEFAUL
     _mark_edge_cells(mesh, grid, surface)
     grid.occupancy[:] = ((votes >= 2) | (surface == 1)).astype(np.uint8)
     if close:
-        grid.occupancy[:] = _neighbourhood_pass(grid, _neighbourhood_pass(grid, grid.occupancy, True), False)
+        morphological_close(grid)
     return grid
+
+
+def cell_index(grid: OccupancyGrid, i: int, j: int, k: int) -> int:
+    """voxelize.js:76-78."""
+    return i + grid.dims[0] * (j + grid.dims[1] * k)
+
+
+def count_occupied(grid: OccupancyGrid) -> int:
+    """voxelize.js:84-90."""
+    return int(grid.occupancy.sum())
+
+
+def morphological_close(grid: OccupancyGrid) -> None:
+    """voxelize.js:389-391: dilate then erode, in place."""
+    grid.occupancy[:] = _neighbourhood_pass(grid, _neighbourhood_pass(grid, grid.occupancy, True), False)
 
 
 def _cell(grid: OccupancyGrid, i: int, j: int, k: int) -> int:

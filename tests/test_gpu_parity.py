@@ -429,6 +429,30 @@ def test_splat_axes(lib):
     assert np.all(np.abs(np.linalg.norm(rot.astype(np.float64), axis=1) - 1) < 1e-6)
 
 
+def test_captured_cloud_body(lib):
+    """A Gaussian cloud voxelised by the reference's cloud path (stamp, seal,
+    fill) steps as a body, and its own Gaussians deform and sort through the
+    cells they were stamped into, equal to the oracle."""
+    import pyoracle
+    import vsim.scenes as sc
+
+    scene = sc.captured_cloud(count=50_000, radius=0.08, element_size=0.008)
+    sim, orc = make(scene)
+    for frame in range(4):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"frame {frame}")
+    view = (0.0, -0.6, -0.8)
+    sim.deform_splats(view)
+    sim.sort_splats()
+    means, cov, order = sim.read_splats()
+    m, q, s, *_ = scene.splats[0]
+    om, oc, keys = orc.splat_deform(0, m, q, s, view)
+    assert np.array_equal(means, om)
+    assert np.array_equal(cov, oc)
+    assert np.array_equal(order, pyoracle.stable_sort(keys))
+
+
 @pytest.mark.parametrize("n,bits", [(1, 32), (4095, 32), (4097, 8), (1_000_003, 32), (300_000, 20)])
 def test_radix_sort_matches_stable_sort(lib, gpu, n, bits):
     import torch

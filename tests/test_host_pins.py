@@ -276,3 +276,170 @@ def test_grip_radius_zero_is_single_node():
 def test_default_grip_radius():
     # grip.test.js:218-226
     assert vs.DEFAULT_GRIPPED_PART_RADIUS > 0.02 and vs.DEFAULT_GRIPPED_PART_RADIUS * 2 < 0.15
+
+
+# ---- cloudVolume.test.js -----------------------------------------------------------
+
+def _cloud_at(points, radius):
+    """cloudVolume.test.js:26-40: identical unrotated Gaussians."""
+    pos = np.asarray(points, np.float32).reshape(-1, 3)
+    rot = np.zeros((len(pos), 4), np.float32)
+    rot[:, 3] = 1
+    return pos, rot, np.full((len(pos), 3), radius, np.float32)
+
+
+def _sphere_shell(radius, count, cover=1.0):
+    """cloudVolume.test.js:52-66: a golden-angle spiral over the sphere, only
+    the part from the south pole up to `cover`."""
+    golden = math.pi * (3 - math.sqrt(5))
+    points = []
+    for i in range(count):
+        y = 1 - (2 * (i + 0.5)) / count
+        if y > 2 * cover - 1:
+            continue
+        ring = math.sqrt(max(0.0, 1 - y * y))
+        theta = golden * i
+        points += [math.cos(theta) * ring * radius, y * radius, math.sin(theta) * ring * radius]
+    return points
+
+
+def _occupancy_at(grid, point):
+    """cloudVolume.test.js:73-76: asked through `locate`, as the render side asks."""
+    cell, _ = vz.locate(grid.origin, grid.h, grid.dims, *point)
+    return int(grid.occupancy[cell[0] + grid.dims[0] * (cell[1] + grid.dims[1] * cell[2])])
+
+
+_RADIUS = 0.05
+_SPREAD = 0.0008
+_SHELL = _sphere_shell(_RADIUS, 6000)
+_EXACT = 4 / 3 * math.pi * _RADIUS ** 3
+
+
+def test_cloud_centres_in_solid_cells():
+    # cloudVolume.test.js:84-109
+    cloud = _cloud_at(_SHELL, _SPREAD)
+    for element in (0.013, 0.0086, 0.0065, 0.0043, 0.0032):
+        g = vz.voxelize_cloud(*cloud, element)
+        outside = sum(_occupancy_at(g, p) == 0 for p in cloud[0].astype(np.float64).tolist())
+        assert outside == 0, element
+
+
+def test_cloud_shell_becomes_solid():
+    # cloudVolume.test.js:111-130
+    cloud = _cloud_at(_SHELL, _SPREAD)
+    shell = vz.voxelize_cloud(*cloud, 0.005, fill=False)
+    solid = vz.voxelize_cloud(*cloud, 0.005)
+    assert vz.count_occupied(shell) * shell.h ** 3 / _EXACT < 0.7
+    ratio = vz.count_occupied(solid) * solid.h ** 3 / _EXACT
+    assert 1.15 < ratio < 1.45
+
+
+def test_cloud_volume_converges():
+    # cloudVolume.test.js:132-144
+    cloud = _cloud_at(_SHELL, _SPREAD)
+
+    def error(element):
+        g = vz.voxelize_cloud(*cloud, element)
+        return abs(vz.count_occupied(g) * g.h ** 3 - _EXACT) / _EXACT
+
+    assert error(0.0037) < error(0.01) * 0.7
+
+
+def test_cloud_open_capture_stays_hollow():
+    # cloudVolume.test.js:146-156
+    cloud = _cloud_at(_sphere_shell(_RADIUS, 6000, 0.75), _SPREAD)
+    shell = vz.count_occupied(vz.voxelize_cloud(*cloud, 0.005, fill=False))
+    filled = vz.count_occupied(vz.voxelize_cloud(*cloud, 0.005))
+    assert filled < shell * 1.5
+
+
+def test_cloud_padding_ring_clear():
+    # cloudVolume.test.js:158-176
+    g = vz.voxelize_cloud(*_cloud_at(_SHELL, _SPREAD), 0.0065)
+    nx, ny, nz = g.dims
+    occ = g.occupancy.reshape(nz, ny, nx)
+    assert occ[0].sum() + occ[-1].sum() + occ[:, 0].sum() + occ[:, -1].sum() + occ[:, :, 0].sum() \
+        + occ[:, :, -1].sum() == 0
+
+
+def test_cloud_stamps_along_own_axes():
+    # cloudVolume.test.js:178-190: a quarter turn about z puts the long axis on y
+    pos, rot, scale = _cloud_at([0, 0, 0], 1)
+    scale[:] = [0.05, 0.004, 0.004]
+    rot[:] = [0, 0, math.sqrt(0.5), math.sqrt(0.5)]
+    g = vz.voxelize_cloud(pos, rot, scale, 0.0125, fill=False)
+    assert _occupancy_at(g, [0, 0.08, 0]) == 1
+    assert _occupancy_at(g, [0.08, 0, 0]) == 0
+
+
+def test_cloud_refuses_empty_and_flat():
+    # cloudVolume.test.js:192-195
+    with pytest.raises(ValueError, match="no Gaussians"):
+        vz.voxelize_cloud(*_cloud_at([], 0.01), 0.01)
+    with pytest.raises(ValueError, match="no extent"):
+        vz.voxelize_cloud(*_cloud_at([0, 0, 0], 0), 0.01)
+
+
+def test_quat_to_columns_quarter_turn():
+    # cloudVolume.test.js:199-208: column k is where basis vector k lands
+    m = vz.quat_to_columns([0, 0, math.sqrt(0.5), math.sqrt(0.5)])[0]
+    assert np.allclose(m, [0, 1, 0, -1, 0, 0, 0, 0, 1], atol=1e-6)
+
+
+def test_quat_to_columns_orthonormal():
+    # cloudVolume.test.js:210-221
+    q = np.array([0.3, -0.5, 0.2, 0.7])
+    m = vz.quat_to_columns(q / np.linalg.norm(q))[0].astype(np.float64).reshape(3, 3)
+    assert np.allclose(m @ m.T, np.eye(3), atol=1e-6)
+
+
+def test_fill_enclosed_counts_the_cavity():
+    # cloudVolume.js:321-375: a closed 5^3 box shell around a 3^3 cavity fills
+    # exactly the cavity; a hole in one face lets the outside in.
+    g = vz.grid_for_bounds(([0, 0, 0], [1, 1, 1]), 1 / 5)
+    nx, ny, nz = g.dims
+    occ = g.occupancy.reshape(nz, ny, nx)
+    occ[2:7, 2:7, 2:7] = 1
+    occ[3:6, 3:6, 3:6] = 0
+    holed = vz.OccupancyGrid(g.dims, g.origin, g.h, g.occupancy.copy())
+    holed.occupancy.reshape(nz, ny, nx)[4, 4, 2] = 0
+    assert vz.fill_enclosed(g) == 27
+    assert vz.count_occupied(g) == 125
+    assert vz.fill_enclosed(holed) == 0
+
+
+def test_js_hypot_matches_reference_cases():
+    # V8's Math.hypot: zero, infinity before NaN, and the scaled sum
+    assert vz.js_hypot(0.0, 0.0, 0.0) == 0.0
+    assert vz.js_hypot(np.inf, np.nan, 1.0) == np.inf
+    assert np.isnan(vz.js_hypot(np.nan, 1.0, 1.0))
+    assert vz.js_hypot(3.0, 4.0, 12.0) == 13.0
+    assert vz.js_hypot(1e300, 1e300, 0.0) == pytest.approx(math.sqrt(2) * 1e300)
+
+
+def test_voxelize_source_dispatch():
+    # voxelLattice.js:208-226: one table, three kinds, anything else refused
+    cloud = _cloud_at(_SHELL, _SPREAD)
+    assert np.array_equal(vz.voxelize_source("cloud", cloud, 0.01).occupancy,
+                          vz.voxelize_cloud(*cloud, 0.01).occupancy)
+    assert vz.count_occupied(vz.voxelize_source("shape", vz.sphere(0.05), 0.01)) > 0
+    assert vz.count_occupied(vz.voxelize_source("mesh", _box_mesh(0.5), 1 / 8)) > 0
+    with pytest.raises(ValueError, match='kind "points"'):
+        vz.voxelize_source("points", cloud, 0.01)
+
+
+def test_captured_cloud_scene_centres_in_cells():
+    # cloudVolume.js:52-59: the body built from a capture holds every one of
+    # its Gaussians' centres in a solid cell, where the splat deformation
+    # reads them
+    from vsim import scenes as sc
+
+    scene = sc.captured_cloud(count=20_000, radius=0.06, element_size=0.008)
+    body = scene.bodies[0]
+    means = scene.splats[0][0]
+    for p in means.astype(np.float64).tolist():
+        cell, _ = vz.locate(body.origin, body.h, body.cell_dims, *p)
+        assert body.occupancy[cell[0] + body.cell_dims[0] * (cell[1] + body.cell_dims[1] * cell[2])] == 1
+    lowest = min(p[1] for p in means.tolist())
+    assert lowest > scene.tank[0][1]
+    assert 1.0 < body.cell_count * body.h ** 3 / (4 / 3 * math.pi * 0.06 ** 3) < 1.8

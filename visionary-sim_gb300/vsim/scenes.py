@@ -330,3 +330,52 @@ def tank_scene(fixture) -> Scene:
     tank = (tuple(float(v) for v in z["tank_min"]), tuple(float(v) for v in z["tank_max"]))
     return Scene(bodies, tank, step_duration=None, substeps=24, contact=True, self_contact=False)
 
+
+
+def capture_cloud(count: int, radius: float, seed: int):
+    """A synthetic capture: `count` Gaussians on the surface of a sphere of
+    `radius` (golden-angle spiral, radial jitter N(0, (radius/200)^2)), with
+    nothing behind the surface, as a scan gives. Scales log-uniform in
+    [0.4, 1.6] x the sample spacing per axis, uniformly random unit
+    quaternions (x, y, z, w). Returns float32 (positions, rotations,
+    scales)."""
+    rng = np.random.default_rng(seed)
+    i = np.arange(count, dtype=np.float64)
+    y = 1 - 2 * (i + 0.5) / count
+    ring = np.sqrt(np.maximum(0.0, 1 - y * y))
+    theta = math.pi * (3 - math.sqrt(5)) * i
+    r = radius + rng.normal(scale=radius / 200, size=count)
+    positions = np.stack([np.cos(theta) * ring * r, y * r, np.sin(theta) * ring * r], axis=1)
+    spacing = math.sqrt(4 * math.pi * radius * radius / count)
+    scales = log_uniform(rng, 0.4 * spacing, 1.6 * spacing, (count, 3))
+    quats = rng.normal(size=(count, 4))
+    quats /= np.linalg.norm(quats, axis=1, keepdims=True)
+    return (positions.astype(np.float32), quats.astype(np.float32), scales.astype(np.float32))
+
+
+def captured_cloud(count: int = 200_000, radius: float = 0.1, element_size: float = 0.008, seed: int = 5,
+                   lift: float = 0.02) -> Scene:
+    """A captured Gaussian cloud as a body, the reference's "cloud" rest
+    geometry (voxelLattice.js:208-226): `capture_cloud`'s shell lifted so its
+    lowest ellipsoid reach sits `lift` above the ground, voxelised by
+    vsim.voxelize.voxelize_cloud (stamped, sealed, filled), the cloud's own
+    Gaussians as the body's splats (each centre in a solid cell by
+    construction). E = 2e5, nu = 0.45, rho = 1000; ground and self contact;
+    dt = 1/60 in 10 substeps."""
+    from . import voxelize
+
+    positions, quats, scales = capture_cloud(count, radius, seed)
+    grid = voxelize.voxelize_cloud(positions, quats, scales, element_size)
+    drop = lift - (grid.origin[1] + voxelize.DEFAULT_PADDING * grid.h)
+    positions = (positions.astype(np.float64) + [0.0, drop, 0.0]).astype(np.float32)
+    grid = voxelize.voxelize_cloud(positions, quats, scales, element_size)
+    mat = dict(DEFAULT_MATERIAL, youngs_modulus=2e5, poisson_ratio=0.45, density=1000.0)
+    body = Body(tuple(grid.dims), tuple(grid.origin), grid.h, grid.occupancy, mat)
+    hi = [grid.origin[a] + grid.dims[a] * grid.h for a in range(3)]
+    margin = 0.5 * radius
+    tank = ((grid.origin[0] - margin, 0.0, grid.origin[2] - margin), (hi[0] + margin, hi[1] + margin, hi[2] + margin))
+    scene = Scene([body], tank, step_duration=1 / 600, substeps=10, contact=True, self_contact=True)
+    rng = np.random.default_rng(seed + 1)
+    scene.splats[0] = (positions, quats, scales, rng.uniform(0.1, 1.0, count).astype(np.float32),
+                       rng.random((count, 3)).astype(np.float32))
+    return scene

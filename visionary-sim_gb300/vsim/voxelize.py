@@ -13,7 +13,11 @@ vertices stored as float32, as the reference's Float32Array does):
   not needed here);
 - `packages/visionary-sim/src/sim/discretize/lattice/voxelize.js:19-435` --
   `gridForBounds`, `voxelizeSdf`, `voxelizeMesh` (three-axis ray parity with a
-  majority vote, edge marking, 6-neighbourhood close).
+  majority vote, edge marking, 6-neighbourhood close);
+- `packages/visionary-sim/src/sim/discretize/lattice/cloudVolume.js:70-397`
+  -- `voxelizeCloud`: a Gaussian cloud stamped as solid ellipsoids, sealed,
+  flood-filled from the faces and eroded back (with `mat3FromQuat`,
+  `mat3.js:71-87`, and `locate`, `sample.js:42-55`).
 
 The result feeds `vsim_create` as a body's cell grid (cell_dims, origin, h,
 occupancy).
@@ -207,6 +211,196 @@ def voxelize_mesh(mesh: Mesh, bounds, element_size: float, padding: int = DEFAUL
     if close:
         morphological_close(grid)
     return grid
+
+
+# ---- cloudVolume.js -----------------------------------------------------------
+
+CLOUD_SIGMA = 2
+CLOUD_SEAL = 2
+# cloudVolume.js:86: a cell's eight corners (corners.js:12-21 order), then its centre.
+_CELL_SAMPLES = [(c & 1, (c >> 1) & 1, (c >> 2) & 1) for c in range(8)] + [(0.5, 0.5, 0.5)]
+
+
+def quat_to_columns(q) -> np.ndarray:
+    """mat3.js:71-87 (mat3FromQuat) for quaternions (n, 4) in x, y, z, w
+    order: column-major rotations (n, 9), each entry computed in double and
+    stored as float32 like the reference's Float32Array."""
+    q = np.asarray(q, np.float64).reshape(-1, 4)
+    x, y, z, w = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    out = np.empty((len(q), 9), np.float32)
+    out[:, 0] = 1 - 2 * (y * y + z * z)
+    out[:, 1] = 2 * (x * y + z * w)
+    out[:, 2] = 2 * (x * z - y * w)
+    out[:, 3] = 2 * (x * y - z * w)
+    out[:, 4] = 1 - 2 * (x * x + z * z)
+    out[:, 5] = 2 * (y * z + x * w)
+    out[:, 6] = 2 * (x * z + y * w)
+    out[:, 7] = 2 * (y * z - x * w)
+    out[:, 8] = 1 - 2 * (x * x + y * y)
+    return out
+
+
+def js_hypot(a: np.ndarray, b: np.ndarray, c: np.ndarray) -> np.ndarray:
+    """JavaScript's Math.hypot of three arguments as V8 computes it (its
+    published math builtin): each magnitude divided by the largest, squares
+    summed with Kahan compensation, square root times the largest; an
+    infinite argument gives infinity, else a NaN gives NaN."""
+    v = np.abs(np.stack([np.asarray(a, np.float64), np.asarray(b, np.float64), np.asarray(c, np.float64)]))
+    top = v.max(axis=0)
+    safe = np.where(top > 0, top, 1.0)
+    total = np.zeros_like(top)
+    compensation = np.zeros_like(top)
+    with np.errstate(invalid="ignore"):
+        for r in range(3):
+            n = v[r] / safe
+            summand = n * n - compensation
+            preliminary = total + summand
+            compensation = (preliminary - total) - summand
+            total = preliminary
+        out = np.sqrt(total) * top
+    out = np.where(top == 0, 0.0, out)
+    out = np.where(np.isnan(v).any(axis=0), np.nan, out)
+    return np.where(np.isinf(v).any(axis=0), np.inf, out)
+
+
+def _ellipsoids(rotations, scales, sigma: float):
+    """cloudVolume.js:195-210 (ellipsoidOf) for every Gaussian: the float32
+    column-major rotations, the half-axes sigma * scale, and the reach along
+    each world axis (the length of that row of R * diag(radius))."""
+    columns = quat_to_columns(rotations)
+    radius = sigma * np.asarray(scales, np.float32).astype(np.float64).reshape(-1, 3)
+    col = columns.astype(np.float64)
+    half = np.stack([js_hypot(col[:, a] * radius[:, 0], col[:, 3 + a] * radius[:, 1], col[:, 6 + a] * radius[:, 2])
+                     for a in range(3)], axis=1)
+    return col, radius, half
+
+
+def locate(origin, h: float, cell_dims, x: float, y: float, z: float):
+    """sample.js:42-55: the cell holding a world point (clamped into the
+    grid) and the point's local coordinates within it -- how the render side
+    finds a Gaussian's cell."""
+    cell, local = [0, 0, 0], [0.0, 0.0, 0.0]
+    for a, p in enumerate((x, y, z)):
+        g = (float(p) - origin[a]) / h
+        index = min(max(math.floor(g), 0), cell_dims[a] - 1)
+        cell[a] = index
+        local[a] = g - index
+    return cell, local
+
+
+def voxelize_cloud(positions, rotations, scales, element_size: float, padding: int = DEFAULT_PADDING,
+                   sigma: float = CLOUD_SIGMA, seal: int = CLOUD_SEAL, fill: bool = True) -> OccupancyGrid:
+    """cloudVolume.js:101-123 (voxelizeCloud): a Gaussian cloud (centres
+    (n, 3), quaternions (n, 4) x-y-z-w, scales (n, 3), all float32 as the
+    reference stores them) to an occupancy grid. Every Gaussian is stamped as
+    a solid ellipsoid at `sigma` standard deviations, with the cell holding
+    its centre always material; with `fill`, the shell is dilated `seal`
+    times, every cell the outside cannot reach through face neighbours is
+    filled, the result is eroded `seal` times and the stamp is put back."""
+    pos = np.asarray(positions, np.float32).astype(np.float64).reshape(-1, 3)
+    if len(pos) == 0:
+        raise ValueError("voxelizeCloud: a cloud with no Gaussians has no volume")
+    columns, radius, half = _ellipsoids(rotations, scales, sigma)
+    # cloudVolume.js:219-234 (materialBounds)
+    lo = [float(np.min(pos[:, a] - half[:, a])) for a in range(3)]
+    hi = [float(np.max(pos[:, a] + half[:, a])) for a in range(3)]
+    if not (max(hi[a] - lo[a] for a in range(3)) > 0):
+        raise ValueError("voxelizeCloud: a cloud with no extent has no volume")
+    grid = grid_for_bounds((lo, hi), element_size, padding)
+    _stamp_cloud(grid, pos, columns, radius, half)
+    if fill:
+        _seal_and_fill(grid, seal)
+    return grid
+
+
+def _stamp_cloud(grid: OccupancyGrid, pos, columns, radius, half, budget: int = 1 << 22) -> None:
+    """cloudVolume.js:138-178 (stampCloud) with cellMeetsEllipsoid (:252-276).
+    Marking is an OR, so the Gaussians are taken in groups of equal box shape
+    rather than one by one; each sample is the reference's double
+    arithmetic in its order."""
+    dims, origin, h = grid.dims, grid.origin, grid.h
+    occ = grid.occupancy
+    nx, ny = dims[0], dims[1]
+    dims_a = np.asarray(dims)
+    origin_a = np.asarray(origin, np.float64)
+    # cloudVolume.js:384-386 (cellOf): the centre's cell, clamped into the grid
+    centre_cell = np.clip(np.floor((pos - origin_a) / h), 0, dims_a - 1).astype(np.int64)
+    occ[centre_cell[:, 0] + nx * (centre_cell[:, 1] + ny * centre_cell[:, 2])] = 1
+    # cloudVolume.js:395-397 (offFace): the box, one cell inside both faces
+    lo = np.clip(np.floor((pos - half - origin_a) / h), 1, dims_a - 2).astype(np.int64)
+    hi = np.clip(np.floor((pos + half - origin_a) / h), 1, dims_a - 2).astype(np.int64)
+    shape = np.maximum(hi - lo + 1, 0)
+    shapes, group = np.unique(shape, axis=0, return_inverse=True)
+    group = group.reshape(-1)
+    for g, (bx, by, bz) in enumerate(shapes):
+        cells = int(bx) * int(by) * int(bz)
+        if cells == 0:
+            continue
+        members = np.nonzero(group == g)[0]
+        kk, jj, ii = np.meshgrid(np.arange(bz), np.arange(by), np.arange(bx), indexing="ij")
+        offset = np.stack([ii.reshape(-1), jj.reshape(-1), kk.reshape(-1)], axis=1)
+        step = max(1, budget // (cells * len(_CELL_SAMPLES)))
+        for start in range(0, len(members), step):
+            m = members[start:start + step]
+            ijk = lo[m][:, None, :] + offset[None, :, :]                      # (g, cells, 3)
+            hit = np.zeros(ijk.shape[:2], bool)
+            c = columns[m][:, None, :]
+            r = radius[m][:, None, :]
+            centre = pos[m][:, None, :]
+            with np.errstate(divide="ignore", invalid="ignore"):
+                for sample in _CELL_SAMPLES:
+                    d = [origin[a] + (ijk[..., a] + sample[a]) * h - centre[..., a] for a in range(3)]
+                    total = np.zeros(ijk.shape[:2])
+                    for a in range(3):
+                        t = (c[..., 3 * a] * d[0] + c[..., 3 * a + 1] * d[1] + c[..., 3 * a + 2] * d[2]) / r[..., a]
+                        total = total + t * t
+                    hit |= total <= 1
+            sel = ijk[hit]
+            occ[sel[:, 0] + nx * (sel[:, 1] + ny * sel[:, 2])] = 1
+
+
+def _seal_and_fill(grid: OccupancyGrid, seal: int) -> int:
+    """cloudVolume.js:291-306 (sealAndFill)."""
+    stamp = grid.occupancy.copy()
+    for _ in range(seal):
+        grid.occupancy[:] = _neighbourhood_pass(grid, grid.occupancy, True)
+    filled = fill_enclosed(grid)
+    for _ in range(seal):
+        grid.occupancy[:] = _neighbourhood_pass(grid, grid.occupancy, False)
+    grid.occupancy |= stamp
+    return filled
+
+
+def fill_enclosed(grid: OccupancyGrid) -> int:
+    """cloudVolume.js:321-375 (fillEnclosed): every empty cell that no
+    face-connected path of empty cells joins to the grid's faces becomes
+    material; returns how many. The flood from the faces is the set of
+    6-connected empty components touching a face."""
+    from scipy import ndimage
+
+    nx, ny, nz = grid.dims
+    empty = grid.occupancy.reshape(nz, ny, nx) == 0
+    labels, _ = ndimage.label(empty, structure=ndimage.generate_binary_structure(3, 1))
+    faces = np.concatenate([labels[0].ravel(), labels[-1].ravel(), labels[:, 0].ravel(), labels[:, -1].ravel(),
+                            labels[:, :, 0].ravel(), labels[:, :, -1].ravel()])
+    reached = np.isin(labels, np.unique(faces[faces > 0]))
+    enclosed = (empty & ~reached).reshape(-1)
+    grid.occupancy[enclosed] = 1
+    return int(enclosed.sum())
+
+
+def voxelize_source(kind: str, source, element_size: float) -> OccupancyGrid:
+    """voxelLattice.js:208-226 (VOXELIZERS, proxyFor): rest geometry of kind
+    "mesh" (a Mesh, laid out over its own bounds), "shape" (a Shape) or
+    "cloud" (positions, rotations, scales) to its cell grid, cells
+    `element_size` across; any other kind is refused."""
+    if kind == "mesh":
+        return voxelize_mesh(source, mesh_bounds(source.positions), element_size)
+    if kind == "shape":
+        return voxelize_sdf(source, element_size)
+    if kind == "cloud":
+        return voxelize_cloud(*source, element_size)
+    raise ValueError(f'no way to discretise rest geometry of kind "{kind}"')
 
 
 def cell_index(grid: OccupancyGrid, i: int, j: int, k: int) -> int:

@@ -108,6 +108,31 @@ def translate_mesh(mesh: Mesh, offset) -> Mesh:
     return Mesh(p.astype(np.float32), mesh.indices)
 
 
+def hypot_js(*values: float) -> float:
+    """JavaScript's Math.hypot as V8 evaluates it (its published math
+    builtin): infinity if any argument is infinite, else NaN if any is NaN,
+    else 0 if all are 0; otherwise each magnitude is divided by the largest,
+    the squares are summed in argument order with Kahan compensation, and
+    the square root of the sum is multiplied by the largest. Python's
+    math.hypot rounds differently in the last place."""
+    mags = [abs(float(v)) for v in values]
+    if any(math.isinf(m) for m in mags):
+        return math.inf
+    if any(math.isnan(m) for m in mags):
+        return math.nan
+    top = max(mags, default=0.0)
+    if top == 0:
+        return 0.0
+    total = compensation = 0.0
+    for m in mags:
+        n = m / top
+        summand = n * n - compensation
+        preliminary = total + summand
+        compensation = (preliminary - total) - summand
+        total = preliminary
+    return math.sqrt(total) * top
+
+
 # ---- shapes.js ----------------------------------------------------------------
 
 def torus(major_radius: float, minor_radius: float) -> Shape:
@@ -115,15 +140,15 @@ def torus(major_radius: float, minor_radius: float) -> Shape:
     outer = major_radius + minor_radius
 
     def sdf(x, y, z):
-        radial = math.hypot(x, z) - major_radius
-        return math.hypot(radial, y) - minor_radius
+        radial = hypot_js(x, z) - major_radius
+        return hypot_js(radial, y) - minor_radius
 
     return Shape(sdf, ([-outer, -minor_radius, -outer], [outer, minor_radius, outer]))
 
 
 def sphere(radius: float) -> Shape:
     """shapes.js:59-80."""
-    return Shape(lambda x, y, z: math.hypot(x, y, z) - radius, ([-radius] * 3, [radius] * 3))
+    return Shape(lambda x, y, z: hypot_js(x, y, z) - radius, ([-radius] * 3, [radius] * 3))
 
 
 def box(half_extents) -> Shape:
@@ -134,7 +159,7 @@ def box(half_extents) -> Shape:
         dx = abs(x) - hx
         dy = abs(y) - hy
         dz = abs(z) - hz
-        outside = math.hypot(max(dx, 0), max(dy, 0), max(dz, 0))
+        outside = hypot_js(max(dx, 0), max(dy, 0), max(dz, 0))
         inside = min(max(dx, dy, dz), 0)
         return outside + inside
 
@@ -241,10 +266,7 @@ def quat_to_columns(q) -> np.ndarray:
 
 
 def js_hypot(a: np.ndarray, b: np.ndarray, c: np.ndarray) -> np.ndarray:
-    """JavaScript's Math.hypot of three arguments as V8 computes it (its
-    published math builtin): each magnitude divided by the largest, squares
-    summed with Kahan compensation, square root times the largest; an
-    infinite argument gives infinity, else a NaN gives NaN."""
+    """`hypot_js` of three arguments, elementwise over arrays."""
     v = np.abs(np.stack([np.asarray(a, np.float64), np.asarray(b, np.float64), np.asarray(c, np.float64)]))
     top = v.max(axis=0)
     safe = np.where(top > 0, top, 1.0)
@@ -267,7 +289,7 @@ def _ellipsoids(rotations, scales, sigma: float):
     """cloudVolume.js:195-210 (ellipsoidOf) for every Gaussian: the float32
     column-major rotations, the half-axes sigma * scale, and the reach along
     each world axis (the length of that row of R * diag(radius))."""
-    columns = quat_to_columns(rotations)
+    columns = quat_to_columns(np.asarray(rotations, np.float32))
     radius = sigma * np.asarray(scales, np.float32).astype(np.float64).reshape(-1, 3)
     col = columns.astype(np.float64)
     half = np.stack([js_hypot(col[:, a] * radius[:, 0], col[:, 3 + a] * radius[:, 1], col[:, 6 + a] * radius[:, 2])
@@ -304,7 +326,9 @@ def voxelize_cloud(positions, rotations, scales, element_size: float, padding: i
     # cloudVolume.js:219-234 (materialBounds)
     lo = [float(np.min(pos[:, a] - half[:, a])) for a in range(3)]
     hi = [float(np.max(pos[:, a] + half[:, a])) for a in range(3)]
-    if not (max(hi[a] - lo[a] for a in range(3)) > 0):
+    extent = [hi[a] - lo[a] for a in range(3)]
+    # Math.max of the extents is NaN when any is, and the check then fails
+    if any(math.isnan(e) for e in extent) or not (max(extent) > 0):
         raise ValueError("voxelizeCloud: a cloud with no extent has no volume")
     grid = grid_for_bounds((lo, hi), element_size, padding)
     _stamp_cloud(grid, pos, columns, radius, half)
@@ -434,7 +458,7 @@ def _mark_edge_cells(mesh: Mesh, grid: OccupancyGrid, surface: np.ndarray):
             dx = float(b[0]) - float(a[0])
             dy = float(b[1]) - float(a[1])
             dz = float(b[2]) - float(a[2])
-            steps = max(1, math.ceil(math.hypot(dx, dy, dz) / step))
+            steps = max(1, math.ceil(hypot_js(dx, dy, dz) / step))
             ax, ay, az = float(a[0]), float(a[1]), float(a[2])
             for s in range(steps + 1):
                 f = s / steps

@@ -517,6 +517,56 @@ int vsim_clock_set_step_duration(vsim_clock* clock, double step_duration);
 int vsim_clock_reset(vsim_clock* clock);
 int vsim_clock_snapshot(const vsim_clock* clock, vsim_clock_report* out);
 
+/* ---- Gaussian-cloud voxeliser (cloudVolume.js:101-397) ----------------
+ *
+ * voxelizeCloud(cloud, {elementSize, padding, sigma, seal, fill}) on the
+ * device: the occupancy grid of a cloud of Gaussians (centres xyz, unit
+ * quaternions x-y-z-w, per-axis standard deviations, float32 as the
+ * reference's arrays), the same cell for cell as the reference's CPU
+ * voxeliser -- each Gaussian stamped as a solid ellipsoid at `sigma`
+ * standard deviations with the cell holding its centre always material; with
+ * `fill`, the shell dilated `seal` times, every cell the outside cannot
+ * reach through face neighbours filled, eroded back and the stamp put back.
+ * The reference's defaults are padding 2 (voxelize.js), sigma 2, seal 2,
+ * fill on (cloudVolume.js:70,83). A cloud with no Gaussians or no extent
+ * fails with VSIM_ERR_INVALID (the reference's `Error`), a bad element size
+ * with VSIM_ERR_RANGE. Runs on the calling thread's current device and
+ * returns when the grid is built; the result stays on the device in the
+ * returned volume until it is destroyed.
+ */
+typedef struct vsim_cloud_options {
+    double element_size; /* cell edge, metres */
+    double sigma;        /* standard deviations counted as material */
+    uint32_t padding;    /* empty cells added on every side */
+    uint32_t seal;       /* cells the shell is thickened by before the fill */
+    int32_t fill;        /* nonzero: make everything the outside cannot reach material */
+} vsim_cloud_options;
+
+typedef struct vsim_cloud_grid {
+    uint32_t dims[3];  /* cells per axis; occupancy is x fastest */
+    double origin[3];  /* world position of the grid's min corner */
+    double h;          /* cell edge */
+    uint64_t occupied; /* material cells */
+    uint64_t filled;   /* cells the fill made material (fillEnclosed's count) */
+} vsim_cloud_grid;
+
+typedef struct vsim_cloud_volume vsim_cloud_volume;
+
+/* Host arrays: positions 3 x count, rotations 4 x count, scales 3 x count. */
+int vsim_voxelize_cloud(const float* positions, const float* rotations, const float* scales, uint64_t count,
+                        const vsim_cloud_options* options, vsim_cloud_volume** out);
+/* The same arrays already on the device; `stream` (NULL: the legacy default
+ * stream) is synchronised first, so work that wrote them has finished. */
+int vsim_voxelize_cloud_device(const float* d_positions, const float* d_rotations, const float* d_scales,
+                               uint64_t count, const vsim_cloud_options* options, void* stream,
+                               vsim_cloud_volume** out);
+int vsim_cloud_volume_grid(const vsim_cloud_volume* volume, vsim_cloud_grid* out);
+/* Copies the grid's occupancy (one byte per cell, 0 or 1) to `occupancy`;
+ * VSIM_ERR_CAPACITY when `cells` is smaller than the grid. */
+int vsim_cloud_volume_read(vsim_cloud_volume* volume, uint8_t* occupancy, size_t cells);
+/* Frees the volume; NULL is accepted. */
+int vsim_cloud_volume_destroy(vsim_cloud_volume* volume);
+
 /* ---- material arithmetic (material.js:101-140, compliance.js:30-109) -- */
 
 /* Lame parameters after the reference's clamps. */

@@ -1,0 +1,146 @@
+"""The Gaussian-cloud voxeliser on the GPU (`vsim_voxelize_cloud`,
+csrc/cloud_volume.cu) against the host restatement of cloudVolume.js
+(vsim.voxelize.voxelize_cloud), which the reference's own cloud tests pin
+(tests/test_host_pins.py): the same grid (dims, origin, h) and the same
+occupancy byte for byte, and the same occupied and filled counts.
+
+Cases: the reference tests' sphere shell at its element sizes, with and
+without the fill; an open capture; anisotropic randomly rotated Gaussians;
+boxes large enough to go to the block-per-Gaussian stamp; degenerate
+Gaussians; padding under two cells (boxes that leave the grid); seal 0 and
+3, sigma 1; inputs already on the device; the errors.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def vz(vsimlib, gpu):
+    from vsim import voxelize
+
+    return voxelize
+
+
+def _cloud_at(points, radius):
+    pos = np.asarray(points, np.float32).reshape(-1, 3)
+    rot = np.zeros((len(pos), 4), np.float32)
+    rot[:, 3] = 1
+    return pos, rot, np.full((len(pos), 3), radius, np.float32)
+
+
+def _shell(radius, count, cover=1.0):
+    golden = math.pi * (3 - math.sqrt(5))
+    i = np.arange(count, dtype=np.float64)
+    y = 1 - 2 * (i + 0.5) / count
+    keep = y <= 2 * cover - 1
+    ring = np.sqrt(np.maximum(0.0, 1 - y * y))
+    pts = np.stack([np.cos(golden * i) * ring * radius, y * radius, np.sin(golden * i) * ring * radius], axis=1)
+    return pts[keep]
+
+
+def _same(vz, cloud, element, **kw):
+    host_stats, dev_stats = {}, {}
+    host = vz.voxelize_cloud(*cloud, element, stats=host_stats, **kw)
+    dev = vz.voxelize_cloud_on_device(*cloud, element, stats=dev_stats, **kw)
+    assert dev.dims == host.dims, (dev.dims, host.dims)
+    assert dev.origin == host.origin and dev.h == host.h
+    diff = np.flatnonzero(dev.occupancy != host.occupancy)
+    assert diff.size == 0, f"{diff.size} cells differ, first {diff[:8]}"
+    assert dev_stats == host_stats, (dev_stats, host_stats)
+    return dev
+
+
+@pytest.mark.parametrize("element", [0.013, 0.0086, 0.0065, 0.0043, 0.0032])
+def test_sphere_shell_filled(vz, element):
+    _same(vz, _cloud_at(_shell(0.05, 6000), 0.0008), element)
+
+
+def test_sphere_shell_unfilled_and_open(vz):
+    _same(vz, _cloud_at(_shell(0.05, 6000), 0.0008), 0.005, fill=False)
+    g = _same(vz, _cloud_at(_shell(0.05, 6000, 0.75), 0.0008), 0.005)
+    assert vz.count_occupied(g) > 0
+
+
+def test_rotated_anisotropic_capture(vz):
+    import vsim.scenes as sc
+
+    cloud = sc.capture_cloud(60_000, 0.08, seed=11)
+    _same(vz, cloud, 0.004)
+    _same(vz, cloud, 0.0025, seal=3, sigma=1.0)
+    _same(vz, cloud, 0.006, seal=0)
+
+
+def test_large_boxes_take_the_block_stamp(vz):
+    # Gaussians reaching ~6 cells each way: boxes of ~13^3 cells, far over
+    # the 64 a thread stamps inline, mixed with small ones
+    rng = np.random.default_rng(3)
+    n = 400
+    pos = rng.uniform(-0.1, 0.1, (n, 3)).astype(np.float32)
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    scale = np.where(rng.random((n, 1)) < 0.5, 0.006, 0.0004) * rng.uniform(0.5, 1.5, (n, 3))
+    _same(vz, (pos, q.astype(np.float32), scale.astype(np.float32)), 0.002)
+    long = _cloud_at([0, 0, 0], 1)
+    long[2][:] = [0.05, 0.004, 0.004]
+    long[1][:] = [0, 0, math.sqrt(0.5), math.sqrt(0.5)]
+    g = _same(vz, long, 0.0125, fill=False)
+    cell, _ = vz.locate(g.origin, g.h, g.dims, 0, 0.08, 0)
+    assert g.occupancy[cell[0] + g.dims[0] * (cell[1] + g.dims[1] * cell[2])] == 1
+
+
+def test_degenerate_gaussians(vz):
+    # zero and denormal scales mixed in: their axes divide to inf or NaN and
+    # test nothing, their centre cells are still marked
+    rng = np.random.default_rng(5)
+    pos, rot, scale = _cloud_at(_shell(0.04, 3000), 0.0008)
+    scale[::7] = 0
+    scale[3::11, 1] = 1e-40
+    rot[5::13] = [0.5, -0.5, 0.5, 0.5]
+    _same(vz, (pos, rot, scale), 0.004)
+    flat = pos.copy()
+    flat[:, 1] = 0.01  # a flat cloud: extent only from the ellipsoids on y
+    _same(vz, (flat, rot, scale), 0.004)
+
+
+@pytest.mark.parametrize("padding", [0, 1, 3])
+def test_padding_edges(vz, padding):
+    # under two cells of padding the stamp's box can leave the grid, and the
+    # reference's typed array ignores those indices
+    rng = np.random.default_rng(9)
+    pos = rng.uniform(-0.02, 0.02, (500, 3)).astype(np.float32)
+    cloud = _cloud_at(pos, 0.002)
+    _same(vz, cloud, 0.003, padding=padding)
+    flat = pos.copy()
+    flat[:, 2] = 0.0
+    _same(vz, _cloud_at(flat, 0.0), 0.003, padding=padding)
+
+
+def test_device_inputs(vz):
+    import torch
+    import vsim.scenes as sc
+
+    cloud = sc.capture_cloud(20_000, 0.05, seed=2)
+    host = vz.voxelize_cloud(*cloud, 0.003)
+    dev = vz.voxelize_cloud_on_device(*[torch.from_numpy(a).cuda() for a in cloud], 0.003)
+    assert dev.dims == host.dims and dev.origin == host.origin
+    assert np.array_equal(dev.occupancy, host.occupancy)
+
+
+def test_errors(vz):
+    from vsim import _ffi
+
+    with pytest.raises(_ffi.VsimError, match="no Gaussians"):
+        vz.voxelize_cloud_on_device(*_cloud_at([], 0.01), 0.01)
+    with pytest.raises(_ffi.VsimError, match="no extent"):
+        vz.voxelize_cloud_on_device(*_cloud_at([0, 0, 0], 0), 0.01)
+    nan = _cloud_at([[0, 0, 0], [np.nan, 0, 0]], 0.01)
+    with pytest.raises(_ffi.VsimError, match="no extent"):
+        vz.voxelize_cloud_on_device(*nan, 0.01)
+    with pytest.raises(_ffi.VsimRangeError):
+        vz.voxelize_cloud_on_device(*_cloud_at([0, 0, 0], 0.01), 0.0)
+    with pytest.raises(_ffi.VsimRangeError):
+        vz.voxelize_cloud_on_device(*_cloud_at([0, 0, 0], 0.01), float("inf"))

@@ -129,6 +129,16 @@ class GrabResult(C.Structure):
                 ("found", C.c_uint32)]
 
 
+class CloudOptions(C.Structure):
+    _fields_ = [("element_size", C.c_double), ("sigma", C.c_double), ("padding", C.c_uint32), ("seal", C.c_uint32),
+                ("fill", C.c_int32)]
+
+
+class CloudGrid(C.Structure):
+    _fields_ = [("dims", C.c_uint32 * 3), ("origin", C.c_double * 3), ("h", C.c_double), ("occupied", C.c_uint64),
+                ("filled", C.c_uint64)]
+
+
 VSIM_GRIP_SINGLE_NODE = 0
 VSIM_GRIP_WITHIN_RADIUS = 1
 
@@ -213,6 +223,11 @@ SIGNATURES = {
     "vsim_splats_read_axes": (C.c_int, [_P, _F, _F, _SZ]),
     "vsim_splats_read": (C.c_int, [_P, _F, _F, _U, _SZ]),
     "vsim_radix_sort_u32": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P, C.POINTER(_SZ), _P]),
+    "vsim_voxelize_cloud": (C.c_int, [_F, _F, _F, C.c_uint64, C.POINTER(CloudOptions), C.POINTER(_P)]),
+    "vsim_voxelize_cloud_device": (C.c_int, [_P, _P, _P, C.c_uint64, C.POINTER(CloudOptions), _P, C.POINTER(_P)]),
+    "vsim_cloud_volume_grid": (C.c_int, [_P, C.POINTER(CloudGrid)]),
+    "vsim_cloud_volume_read": (C.c_int, [_P, C.POINTER(C.c_uint8), _SZ]),
+    "vsim_cloud_volume_destroy": (C.c_int, [_P]),
     "vsim_radix_sort_u32_noalloc": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P]),
     "vsim_profile_frame": (C.c_int, [_P, C.c_uint32, C.c_int, _F, C.POINTER(Profile)]),
     "vsim_color_counts": (C.c_int, [_P, _U]),

@@ -311,14 +311,16 @@ def locate(origin, h: float, cell_dims, x: float, y: float, z: float):
 
 
 def voxelize_cloud(positions, rotations, scales, element_size: float, padding: int = DEFAULT_PADDING,
-                   sigma: float = CLOUD_SIGMA, seal: int = CLOUD_SEAL, fill: bool = True) -> OccupancyGrid:
+                   sigma: float = CLOUD_SIGMA, seal: int = CLOUD_SEAL, fill: bool = True,
+                   stats: dict | None = None) -> OccupancyGrid:
     """cloudVolume.js:101-123 (voxelizeCloud): a Gaussian cloud (centres
     (n, 3), quaternions (n, 4) x-y-z-w, scales (n, 3), all float32 as the
     reference stores them) to an occupancy grid. Every Gaussian is stamped as
     a solid ellipsoid at `sigma` standard deviations, with the cell holding
     its centre always material; with `fill`, the shell is dilated `seal`
     times, every cell the outside cannot reach through face neighbours is
-    filled, the result is eroded `seal` times and the stamp is put back."""
+    filled, the result is eroded `seal` times and the stamp is put back.
+    With `stats`, the occupied cells and the fill's count are stored in it."""
     pos = np.asarray(positions, np.float32).astype(np.float64).reshape(-1, 3)
     if len(pos) == 0:
         raise ValueError("voxelizeCloud: a cloud with no Gaussians has no volume")
@@ -332,9 +334,48 @@ def voxelize_cloud(positions, rotations, scales, element_size: float, padding: i
         raise ValueError("voxelizeCloud: a cloud with no extent has no volume")
     grid = grid_for_bounds((lo, hi), element_size, padding)
     _stamp_cloud(grid, pos, columns, radius, half)
-    if fill:
-        _seal_and_fill(grid, seal)
+    filled = _seal_and_fill(grid, seal) if fill else 0
+    if stats is not None:
+        stats.update(occupied=count_occupied(grid), filled=filled)
     return grid
+
+
+def voxelize_cloud_on_device(positions, rotations, scales, element_size: float, padding: int = DEFAULT_PADDING,
+                             sigma: float = CLOUD_SIGMA, seal: int = CLOUD_SEAL, fill: bool = True,
+                             stats: dict | None = None) -> OccupancyGrid:
+    """`voxelize_cloud` on the GPU through libvsim (`vsim_voxelize_cloud`,
+    csrc/cloud_volume.cu): the same grid, cell for cell. `positions`,
+    `rotations` and `scales` are host arrays, or CUDA torch tensors (then
+    nothing is copied in). With `stats`, the occupied and filled cell counts
+    are stored in it. Raises when the library is not built."""
+    import ctypes as C
+
+    from . import _ffi
+
+    lib = _ffi.lib()
+    opts = _ffi.CloudOptions(float(element_size), float(sigma), int(padding), int(seal), 1 if fill else 0)
+    vol = C.c_void_p()
+    if hasattr(positions, "data_ptr"):
+        count = int(positions.numel() // 3)
+        tensors = [t.contiguous().float() for t in (positions, rotations, scales)]
+        _ffi.check(lib.vsim_voxelize_cloud_device(tensors[0].data_ptr(), tensors[1].data_ptr(), tensors[2].data_ptr(),
+                                                  count, C.byref(opts), None, C.byref(vol)))
+    else:
+        arrays = [np.ascontiguousarray(np.asarray(a, np.float32)) for a in (positions, rotations, scales)]
+        count = arrays[0].size // 3
+        _ffi.check(lib.vsim_voxelize_cloud(_ffi.fptr(arrays[0]), _ffi.fptr(arrays[1]), _ffi.fptr(arrays[2]), count,
+                                           C.byref(opts), C.byref(vol)))
+    try:
+        g = _ffi.CloudGrid()
+        _ffi.check(lib.vsim_cloud_volume_grid(vol, C.byref(g)))
+        dims = [int(v) for v in g.dims]
+        occupancy = np.zeros(dims[0] * dims[1] * dims[2], np.uint8)
+        _ffi.check(lib.vsim_cloud_volume_read(vol, occupancy.ctypes.data_as(C.POINTER(C.c_uint8)), occupancy.size))
+        if stats is not None:
+            stats.update(occupied=int(g.occupied), filled=int(g.filled))
+        return OccupancyGrid(dims, [float(v) for v in g.origin], float(g.h), occupancy)
+    finally:
+        lib.vsim_cloud_volume_destroy(vol)
 
 
 def _stamp_cloud(grid: OccupancyGrid, pos, columns, radius, half, budget: int = 1 << 22) -> None:
@@ -379,8 +420,12 @@ def _stamp_cloud(grid: OccupancyGrid, pos, columns, radius, half, budget: int = 
                         t = (c[..., 3 * a] * d[0] + c[..., 3 * a + 1] * d[1] + c[..., 3 * a + 2] * d[2]) / r[..., a]
                         total = total + t * t
                     hit |= total <= 1
-            sel = ijk[hit]
-            occ[sel[:, 0] + nx * (sel[:, 1] + ny * sel[:, 2])] = 1
+            # the reference's cellIndex of the box coordinates; with padding
+            # under two cells a box can leave the grid, and like its typed
+            # array the grid ignores an index outside it
+            index = ijk[..., 0] + nx * (ijk[..., 1] + ny * ijk[..., 2])
+            hit &= (index >= 0) & (index < occ.size)
+            occ[index[hit]] = 1
 
 
 def _seal_and_fill(grid: OccupancyGrid, seal: int) -> int:

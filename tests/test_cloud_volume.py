@@ -8,7 +8,9 @@ Cases: the reference tests' sphere shell at its element sizes, with and
 without the fill; an open capture; anisotropic randomly rotated Gaussians;
 boxes large enough to go to the block-per-Gaussian stamp; degenerate
 Gaussians; padding under two cells (boxes that leave the grid); seal 0 and
-3, sigma 1; inputs already on the device; the errors.
+3, sigma 1; samples exactly on an ellipsoid's surface and one float ulp
+off it (which the stamp's float test must hand to its double evaluation);
+inputs already on the device; the errors.
 """
 import math
 
@@ -144,3 +146,19 @@ def test_errors(vz):
         vz.voxelize_cloud_on_device(*_cloud_at([0, 0, 0], 0.01), 0.0)
     with pytest.raises(_ffi.VsimRangeError):
         vz.voxelize_cloud_on_device(*_cloud_at([0, 0, 0], 0.01), float("inf"))
+
+
+def test_samples_on_the_surface(vz):
+    # Binary-exact layout: h = 1/4, centres on cell corners, radius one cell
+    # (sigma 2 x scale 1/8), so samples one cell away along an axis give a
+    # sum of exactly 1 (inside); scales one float ulp smaller put the same
+    # samples just outside. The float test cannot call either; both go to
+    # the double evaluation.
+    rng = np.random.default_rng(12)
+    pos = (rng.integers(-20, 20, (300, 3)) * 0.25).astype(np.float32)
+    exact = _cloud_at(pos, 0.125)
+    _same(vz, exact, 0.25, fill=False)
+    below = _cloud_at(pos, float(np.nextafter(np.float32(0.125), np.float32(0))))
+    _same(vz, below, 0.25, fill=False)
+    mixed = (pos, exact[1], np.where(rng.random((300, 1)) < 0.5, exact[2], below[2]).astype(np.float32))
+    _same(vz, mixed, 0.25)

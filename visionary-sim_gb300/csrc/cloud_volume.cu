@@ -104,9 +104,8 @@ __device__ double hypotV8(double a, double b, double c) {
 }
 
 // mat3.js:71-87 (mat3FromQuat), each entry rounded to float32 as its output
-// array does; then cloudVolume.js:196-209.
-__device__ Ellipsoid ellipsoidOf(const CloudInput& in, uint32_t i) {
-    Ellipsoid e;
+// array does, and the half-axes sigma * scale (cloudVolume.js:196-199).
+__device__ void frameOf(const CloudInput& in, uint32_t i, Ellipsoid& e) {
     const double x = in.rot[4 * size_t(i)], y = in.rot[4 * size_t(i) + 1];
     const double z = in.rot[4 * size_t(i) + 2], w = in.rot[4 * size_t(i) + 3];
     e.col[0] = double(float(1.0 - 2.0 * (y * y + z * z)));
@@ -119,6 +118,12 @@ __device__ Ellipsoid ellipsoidOf(const CloudInput& in, uint32_t i) {
     e.col[7] = double(float(2.0 * (y * z - x * w)));
     e.col[8] = double(float(1.0 - 2.0 * (x * x + y * y)));
     for (int a = 0; a < 3; a++) e.radius[a] = in.sigma * double(in.scale[3 * size_t(i) + a]);
+}
+
+// cloudVolume.js:201-209: the reach along each world axis.
+__device__ Ellipsoid ellipsoidOf(const CloudInput& in, uint32_t i) {
+    Ellipsoid e;
+    frameOf(in, i, e);
     for (int a = 0; a < 3; a++)
         e.half[a] = hypotV8(e.col[a] * e.radius[0], e.col[3 + a] * e.radius[1], e.col[6 + a] * e.radius[2]);
     return e;
@@ -150,13 +155,16 @@ __device__ __forceinline__ unsigned long long warpMax64(unsigned long long v) {
 
 // cloudVolume.js:219-234 (materialBounds): keys[0..2] the smallest
 // position - reach per axis, keys[3..5] the largest position + reach; a NaN
-// anywhere raises *nan (Math.min and Math.max then give NaN).
-__global__ void cloudBoundsKernel(CloudInput in, unsigned long long* __restrict__ keys, uint32_t* __restrict__ nan) {
+// anywhere raises *nan (Math.min and Math.max then give NaN). Each
+// Gaussian's reach is stored in `reach` for the stamp.
+__global__ void cloudBoundsKernel(CloudInput in, unsigned long long* __restrict__ keys, uint32_t* __restrict__ nan,
+                                  double* __restrict__ reach) {
     unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
     bool sawNan = false;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < in.count; i += gridDim.x * blockDim.x) {
         const Ellipsoid e = ellipsoidOf(in, i);
         for (int a = 0; a < 3; a++) {
+            reach[3 * size_t(i) + a] = e.half[a];  // kept for the stamp
             const double p = in.pos[3 * size_t(i) + a];
             const double l = p - e.half[a], u = p + e.half[a];
             sawNan |= isnan(l) || isnan(u);
@@ -184,36 +192,28 @@ __device__ __forceinline__ int64_t clampedCell(double v, double origin, double h
     return static_cast<int64_t>(fmin(fmax(f, double(lo)), double(hi)));
 }
 
-// cloudVolume.js:252-276 (cellMeetsEllipsoid): any of the cell's eight
-// corners (corners.js:12-21 order) or its centre inside the ellipsoid.
-__device__ bool cellMeetsEllipsoid(const GridView& g, int64_t i, int64_t j, int64_t k, const double c[3],
-                                   const Ellipsoid& e) {
-    for (int s = 0; s < 9; s++) {
-        const double ox = s == 8 ? 0.5 : double(s & 1);
-        const double oy = s == 8 ? 0.5 : double((s >> 1) & 1);
-        const double oz = s == 8 ? 0.5 : double((s >> 2) & 1);
-        const double dx = g.origin[0] + (double(i) + ox) * g.h - c[0];
-        const double dy = g.origin[1] + (double(j) + oy) * g.h - c[1];
-        const double dz = g.origin[2] + (double(k) + oz) * g.h - c[2];
-        double sum = 0.0;
-        for (int a = 0; a < 3; a++) {
-            const double t = (e.col[3 * a] * dx + e.col[3 * a + 1] * dy + e.col[3 * a + 2] * dz) / e.radius[a];
-            sum += t * t;
-        }
-        if (sum <= 1.0) return true;
-    }
-    return false;
+// One of a cell's nine sample points (its eight corners in corners.js:12-21
+// order, then its centre) tested against the ellipsoid in the reference's
+// double arithmetic and order (cloudVolume.js:255-273).
+__device__ __forceinline__ void sampleOffset(int s, double& ox, double& oy, double& oz) {
+    ox = s == 8 ? 0.5 : double(s & 1);
+    oy = s == 8 ? 0.5 : double((s >> 1) & 1);
+    oz = s == 8 ? 0.5 : double((s >> 2) & 1);
 }
 
-// cloudVolume.js:170-173 for one cell of a box. The index is the reference's
-// cellIndex of the (possibly out-of-grid, when the padding is under two
-// cells) coordinates, and like a typed array the grid ignores an index
-// outside it.
-__device__ __forceinline__ void stampCell(const GridView& g, uint8_t* occ, int64_t i, int64_t j, int64_t k,
-                                          const double c[3], const Ellipsoid& e) {
-    const int64_t cell = i + int64_t(g.dims[0]) * (j + int64_t(g.dims[1]) * k);
-    if (cell < 0 || cell >= int64_t(g.cells) || occ[cell] != 0) return;
-    if (cellMeetsEllipsoid(g, i, j, k, c, e)) occ[cell] = 1;
+__device__ bool sampleInside(const GridView& g, int64_t i, int64_t j, int64_t k, int s, const double c[3],
+                             const Ellipsoid& e) {
+    double ox, oy, oz;
+    sampleOffset(s, ox, oy, oz);
+    const double dx = g.origin[0] + (double(i) + ox) * g.h - c[0];
+    const double dy = g.origin[1] + (double(j) + oy) * g.h - c[1];
+    const double dz = g.origin[2] + (double(k) + oz) * g.h - c[2];
+    double sum = 0.0;
+    for (int a = 0; a < 3; a++) {
+        const double t = (e.col[3 * a] * dx + e.col[3 * a + 1] * dy + e.col[3 * a + 2] * dz) / e.radius[a];
+        sum += t * t;
+    }
+    return sum <= 1.0;
 }
 
 struct Box {
@@ -222,19 +222,133 @@ struct Box {
     __device__ int64_t cells() const { return extent(0) * extent(1) * extent(2); }
 };
 
-__device__ Box boxOf(const GridView& g, const double c[3], const Ellipsoid& e) {
+// The sample test in float, with a bound on how far its sum of squares can
+// be from the double evaluation's; a sample whose float sum is further than
+// the bound from 1 is decided by it, every other one is evaluated in double.
+// Same answers, far fewer double operations (a double division costs tens
+// of float operations on this part). The bound, per Gaussian and box:
+//   offset: float(base) + off * float(h), with base = origin + lo h - c (in
+//     double) and off = i - lo + ox exact, against the double sequence
+//     origin + (i + ox) h - c: within 2^-22 X + A, where X = |base| +
+//     (extent + 1) h bounds |base|, off h and the offset, and A = 2^-50
+//     (|origin| + |c| + (|lo| + extent + 1) h) the double sequence's own
+//     rounding;
+//   dot with column a (float entries, exact): the propagated offset errors
+//     plus 2^-22 sum_k |col| X_k for its own three roundings;
+//   t = dot / r: that over r (held x4 in `err`, a factor of 4 to spare),
+//     plus 2^-23 |t| for the float reciprocal and product (taken x4);
+//   sum of squares: sum_a (2|t_a| + e_a) e_a, plus 2^-21 s for its roundings,
+//     plus a floor of 2^-20 so that 1 +- the bound is never rounded away.
+// A Gaussian whose bound is not small (err >= 1e-3), whose half-axes or cell
+// are outside [1e-30, 1e30], or whose box is wider than 2^20 cells is tested
+// in double throughout.
+struct FloatTest {
+    float base[3];
+    float h;
+    float col[9];
+    float inv[3];
+    float err[3];
+};
+
+__device__ bool floatTestOf(const GridView& g, const Box& b, const double c[3], const Ellipsoid& e, FloatTest& f) {
+    if (!(g.h > 1e-30 && g.h < 1e30)) return false;
+    double X[3], ex[3];
+    for (int a = 0; a < 3; a++) {
+        if (b.extent(a) > (1 << 20)) return false;
+        const double base = (g.origin[a] + double(b.lo[a]) * g.h) - c[a];
+        const double span = double(b.extent(a) + 1) * g.h;
+        X[a] = fabs(base) + span;
+        ex[a] = 0x1p-22 * X[a] + 0x1p-50 * (fabs(g.origin[a]) + fabs(c[a]) + fabs(double(b.lo[a])) * g.h + span);
+        f.base[a] = float(base);
+    }
+    f.h = float(g.h);
+    for (int q = 0; q < 9; q++) f.col[q] = float(e.col[q]);
+    for (int a = 0; a < 3; a++) {
+        const double r = e.radius[a];
+        if (!(r > 1e-30 && r < 1e30)) return false;
+        double dotErr = 0.0;
+        for (int k = 0; k < 3; k++) dotErr += fabs(e.col[3 * a + k]) * (ex[k] + 0x1p-22 * X[k]);
+        const double err = 4.0 * dotErr / r;
+        if (!(err < 1e-3)) return false;
+        f.err[a] = float(err);
+        f.inv[a] = float(1.0 / r);
+    }
+    return true;
+}
+
+// 1 inside, 0 outside, -1 too close to call in float.
+__device__ __forceinline__ int floatSample(const FloatTest& f, float ox, float oy, float oz) {
+    const float dx = f.base[0] + ox * f.h, dy = f.base[1] + oy * f.h, dz = f.base[2] + oz * f.h;
+    float sum = 0.0f, bound = 0.0f;
+    for (int a = 0; a < 3; a++) {
+        const float t = (f.col[3 * a] * dx + f.col[3 * a + 1] * dy + f.col[3 * a + 2] * dz) * f.inv[a];
+        const float at = fabsf(t);
+        const float et = f.err[a] + 0x1p-21f * at;
+        sum += t * t;
+        bound += (2.0f * at + et) * et;
+    }
+    bound += 0x1p-20f * sum + 0x1p-20f;
+    if (sum > 1.0f + bound) return 0;
+    if (sum < 1.0f - bound) return 1;
+    return -1;
+}
+
+// cloudVolume.js:170-173 for one cell of a box: any sample inside. The index
+// is the reference's cellIndex of the (possibly out-of-grid, when the
+// padding is under two cells) coordinates, and like a typed array the grid
+// ignores an index outside it. The double frame is rebuilt only for a sample
+// the float test cannot call.
+__device__ void stampCell(const CloudInput& in, uint32_t gaussian, const GridView& g, uint8_t* occ, const Box& b,
+                          int64_t i, int64_t j, int64_t k, const double c[3], const FloatTest* f) {
+    const int64_t cell = i + int64_t(g.dims[0]) * (j + int64_t(g.dims[1]) * k);
+    if (cell < 0 || cell >= int64_t(g.cells) || occ[cell] != 0) return;
+    Ellipsoid e;
+    bool haveFrame = false;
+    for (int s = 0; s < 9; s++) {
+        double ox, oy, oz;
+        sampleOffset(s, ox, oy, oz);
+        int inside = -1;
+        if (f)
+            inside = floatSample(*f, float(i - b.lo[0]) + float(ox), float(j - b.lo[1]) + float(oy),
+                                 float(k - b.lo[2]) + float(oz));
+        if (inside < 0) {
+            if (!haveFrame) {
+                frameOf(in, gaussian, e);
+                haveFrame = true;
+            }
+            inside = sampleInside(g, i, j, k, s, c, e) ? 1 : 0;
+        }
+        if (inside) {
+            occ[cell] = 1;
+            return;
+        }
+    }
+}
+
+__device__ Box boxOf(const GridView& g, const double c[3], const double* half) {
     Box b;
     for (int a = 0; a < 3; a++) {
-        b.lo[a] = clampedCell(c[a] - e.half[a], g.origin[a], g.h, 1, int64_t(g.dims[a]) - 2);
-        b.hi[a] = clampedCell(c[a] + e.half[a], g.origin[a], g.h, 1, int64_t(g.dims[a]) - 2);
+        b.lo[a] = clampedCell(c[a] - half[a], g.origin[a], g.h, 1, int64_t(g.dims[a]) - 2);
+        b.hi[a] = clampedCell(c[a] + half[a], g.origin[a], g.h, 1, int64_t(g.dims[a]) - 2);
     }
     return b;
+}
+
+// The Gaussian's box and its float test (false: test in double).
+__device__ bool prepareStamp(const CloudInput& in, uint32_t i, const GridView& g, const double* __restrict__ reach,
+                             const double c[3], Box& b, FloatTest& f) {
+    const double half[3] = {reach[3 * size_t(i)], reach[3 * size_t(i) + 1], reach[3 * size_t(i) + 2]};
+    b = boxOf(g, c, half);
+    Ellipsoid e;
+    frameOf(in, i, e);
+    return floatTestOf(g, b, c, e, f);
 }
 
 // cloudVolume.js:147-177 for one Gaussian per thread: the centre's cell
 // unconditionally, then the box; a box of more than kInlineBoxCells cells is
 // listed for cloudStampBoxKernel.
-__global__ void cloudStampKernel(CloudInput in, GridView g, uint8_t* __restrict__ occ, uint32_t* __restrict__ big,
+__global__ void cloudStampKernel(CloudInput in, GridView g, const double* __restrict__ reach,
+                                 uint8_t* __restrict__ occ, uint32_t* __restrict__ big,
                                  uint32_t* __restrict__ bigCount) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= in.count) return;
@@ -242,30 +356,33 @@ __global__ void cloudStampKernel(CloudInput in, GridView g, uint8_t* __restrict_
     int64_t at[3];
     for (int a = 0; a < 3; a++) at[a] = clampedCell(c[a], g.origin[a], g.h, 0, int64_t(g.dims[a]) - 1);
     occ[at[0] + int64_t(g.dims[0]) * (at[1] + int64_t(g.dims[1]) * at[2])] = 1;
-    const Ellipsoid e = ellipsoidOf(in, i);
-    const Box b = boxOf(g, c, e);
+    Box b;
+    FloatTest f;
+    const bool fast = prepareStamp(in, i, g, reach, c, b, f);
     if (b.cells() > kInlineBoxCells) {
         big[atomicAdd(bigCount, 1u)] = i;  // at most one slot per Gaussian: `big` holds count
         return;
     }
     for (int64_t k = b.lo[2]; k <= b.hi[2]; k++)
         for (int64_t j = b.lo[1]; j <= b.hi[1]; j++)
-            for (int64_t i2 = b.lo[0]; i2 <= b.hi[0]; i2++) stampCell(g, occ, i2, j, k, c, e);
+            for (int64_t i2 = b.lo[0]; i2 <= b.hi[0]; i2++) stampCell(in, i, g, occ, b, i2, j, k, c, fast ? &f : nullptr);
 }
 
 // The listed large boxes, a block each, its threads over the box's cells.
-__global__ void cloudStampBoxKernel(CloudInput in, GridView g, uint8_t* __restrict__ occ,
-                                    const uint32_t* __restrict__ big, const uint32_t* __restrict__ bigCount) {
+__global__ void cloudStampBoxKernel(CloudInput in, GridView g, const double* __restrict__ reach,
+                                    uint8_t* __restrict__ occ, const uint32_t* __restrict__ big,
+                                    const uint32_t* __restrict__ bigCount) {
     const uint32_t listed = *bigCount;
     for (uint32_t n = blockIdx.x; n < listed; n += gridDim.x) {
         const uint32_t i = big[n];
         const double c[3] = {in.pos[3 * size_t(i)], in.pos[3 * size_t(i) + 1], in.pos[3 * size_t(i) + 2]};
-        const Ellipsoid e = ellipsoidOf(in, i);
-        const Box b = boxOf(g, c, e);
+        Box b;
+        FloatTest f;
+        const bool fast = prepareStamp(in, i, g, reach, c, b, f);
         const int64_t ex = b.extent(0), exy = ex * b.extent(1), total = b.cells();
         for (int64_t t = threadIdx.x; t < total; t += blockDim.x) {
             const int64_t k = b.lo[2] + t / exy, r = t % exy;
-            stampCell(g, occ, b.lo[0] + r % ex, b.lo[1] + r / ex, k, c, e);
+            stampCell(in, i, g, occ, b, b.lo[0] + r % ex, b.lo[1] + r / ex, k, c, fast ? &f : nullptr);
         }
     }
 }
@@ -438,7 +555,10 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     CloudScalars init{};
     for (int a = 0; a < 3; a++) init.keys[a] = ~0ull;
     CK(cudaMemcpyAsync(sc, &init, sizeof init, cudaMemcpyHostToDevice, st), "cloud scratch");
-    cloudBoundsKernel<<<streamGrid(in.count, sms), kCloudBlock, 0, st>>>(in, sc->keys, &sc->nan);
+    DeviceBuffer reachBuf;
+    CK(cudaMalloc(&reachBuf.p, size_t(in.count) * 3 * sizeof(double)), "cloud scratch");
+    auto* reach = static_cast<double*>(reachBuf.p);
+    cloudBoundsKernel<<<streamGrid(in.count, sms), kCloudBlock, 0, st>>>(in, sc->keys, &sc->nan, reach);
     CK(cudaGetLastError(), "cloud bounds");
     CloudScalars got{};
     CK(cudaMemcpyAsync(&got, sc, sizeof got, cudaMemcpyDeviceToHost, st), "cloud bounds");
@@ -486,9 +606,9 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     DeviceBuffer bigBuf;
     CK(cudaMalloc(&bigBuf.p, size_t(in.count) * 4), "cloud scratch");
     cloudStampKernel<<<(in.count + kCloudBlock - 1) / kCloudBlock, kCloudBlock, 0, st>>>(
-        in, g, v->occupancy, static_cast<uint32_t*>(bigBuf.p), &sc->bigCount);
-    cloudStampBoxKernel<<<uint32_t(sms) * 4, kCloudBlock, 0, st>>>(in, g, v->occupancy,
-                                                                  static_cast<const uint32_t*>(bigBuf.p), &sc->bigCount);
+        in, g, reach, v->occupancy, static_cast<uint32_t*>(bigBuf.p), &sc->bigCount);
+    cloudStampBoxKernel<<<uint32_t(sms) * 4, kCloudBlock, 0, st>>>(
+        in, g, reach, v->occupancy, static_cast<const uint32_t*>(bigBuf.p), &sc->bigCount);
     CK(cudaGetLastError(), "cloud stamp");
 
     // 4. seal and fill

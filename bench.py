@@ -373,6 +373,76 @@ def stress(quick: bool, hbm: float, frames: int = 3):
     return out
 
 
+def cloud_voxelize(quick: bool, reps: int = 5):
+    """The Gaussian-cloud voxeliser (cloudVolume.js's voxelizeCloud) on a
+    synthetic capture: 2M Gaussians on a 0.3 m sphere (vsim.scenes.
+    capture_cloud, seed 7), 2 mm cells (a 311^3 grid), sigma 2, seal 2, fill
+    on. `gaussians_per_s`: the cloud resident on the device, the grid left
+    there (vsim_voxelize_cloud_device returns with it built); `e2e`: from
+    pinned host arrays to the occupancy in pinned host memory
+    (vsim_voxelize_cloud + vsim_cloud_volume_read); `cpu`: the host
+    restatement of the reference's voxeliser (numpy, one core) on the same
+    cloud, with its grid compared to the device's."""
+    import ctypes as C
+
+    import torch
+
+    import vsim.scenes as sc
+    from vsim import _ffi
+    from vsim import voxelize as vz
+
+    n = 200_000 if quick else 2_000_000
+    element = 0.004 if quick else 0.002
+    cloud = sc.capture_cloud(n, 0.3, seed=7)
+    lib = _ffi.lib()
+    opts = _ffi.CloudOptions(element, 2.0, 2, 2, 1)
+    dev = [torch.from_numpy(a).cuda() for a in cloud]
+    pinned = [torch.from_numpy(a).pin_memory() for a in cloud]
+    fp = [C.cast(t.data_ptr(), C.POINTER(C.c_float)) for t in pinned]
+
+    def on_device():
+        vol = C.c_void_p()
+        _ffi.check(lib.vsim_voxelize_cloud_device(dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), n,
+                                                  C.byref(opts), None, C.byref(vol)))
+        return vol
+
+    grid = _ffi.CloudGrid()
+    lib.vsim_cloud_volume_destroy(on_device())
+    torch.cuda.synchronize()
+    device_s = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        vol = on_device()
+        device_s.append(time.perf_counter() - t)
+        _ffi.check(lib.vsim_cloud_volume_grid(vol, C.byref(grid)))
+        lib.vsim_cloud_volume_destroy(vol)
+    dims = [int(v) for v in grid.dims]
+    cells = dims[0] * dims[1] * dims[2]
+    occupancy = torch.empty(cells, dtype=torch.uint8).pin_memory()
+    out_ptr = C.cast(occupancy.data_ptr(), C.POINTER(C.c_uint8))
+    e2e_s = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        vol = C.c_void_p()
+        _ffi.check(lib.vsim_voxelize_cloud(fp[0], fp[1], fp[2], n, C.byref(opts), C.byref(vol)))
+        _ffi.check(lib.vsim_cloud_volume_read(vol, out_ptr, cells))
+        e2e_s.append(time.perf_counter() - t)
+        lib.vsim_cloud_volume_destroy(vol)
+    t = time.perf_counter()
+    host = vz.voxelize_cloud(*cloud, element)
+    cpu_s = time.perf_counter() - t
+    med, e2e_med = statistics.median(device_s), statistics.median(e2e_s)
+    return {"workload": f"synthetic capture, {n} Gaussians on a 0.3 m sphere, {element * 1e3:g} mm cells "
+                        f"({dims[0]}x{dims[1]}x{dims[2]} grid), sigma 2, seal 2, fill",
+            "gaussians_per_s": round(n / med), "ms": round(med * 1e3, 3),
+            "occupied": int(grid.occupied), "filled": int(grid.filled),
+            "e2e": {"gaussians_per_s": round(n / e2e_med), "ms": round(e2e_med * 1e3, 3),
+                    "h2d_bytes": 40 * n, "d2h_bytes": cells},
+            "cpu": {"gaussians_per_s": round(n / cpu_s), "s": round(cpu_s, 2), "cores": 1,
+                    "kind": "host restatement (numpy)"},
+            "grid_equal_to_host": host.dims == dims and bool(np.array_equal(host.occupancy, occupancy.numpy()))}
+
+
 def drift(frames: int = 300):
     """The 16 x 4 x 4 bar for `frames` frames on the GPU against the oracle
     in double precision from the same start: the float trajectory's
@@ -534,6 +604,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
+    ap.add_argument("--no-cloud", action="store_true")
     ap.add_argument("--stress-only", action="store_true", help="only the stress workload's frames (for captures)")
     ap.add_argument("--capture-after", type=int, default=None, metavar="N",
                     help="profiler capture mode: run N frames of the bench workload, then bracket one more frame "
@@ -626,6 +697,8 @@ def main():
         detail["serving"] = serving_sweep(args.quick)
     if rank == 0 and not args.no_stress:
         detail["stress"] = stress(args.quick, hbm)
+    if rank == 0 and not args.no_cloud:
+        detail["cloud_voxelize"] = cloud_voxelize(args.quick)
     if rank == 0:
         detail["drift_vs_fp64"] = drift(30 if args.quick else 300)
     cpu = None

@@ -17,14 +17,15 @@
 //      the empty cells from the grid's faces (fillEnclosed, :321-375); the
 //      cells a flood reaches are exactly the face-connected components of
 //      empty cells that touch a face, found here by a concurrent union-find
-//      (links by atomicMin on roots, path halving by plain stores) instead
-//      of a serial flood.
+//      (x runs seeded by warp ballots, links by atomicMin on roots, path
+//      halving by plain stores) instead of a serial flood.
 // Marking is an OR (a cell is set by any Gaussian that reaches it), and the
 // components of a graph do not depend on the order edges are merged, so no
 // step's result depends on thread timing.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include <math_constants.h>
 
@@ -94,7 +95,8 @@ __device__ double hypotV8(double a, double b, double c) {
     const double v[3] = {a, b, c};
     double total = 0.0, compensation = 0.0;
     for (int r = 0; r < 3; r++) {
-        const double n = v[r] / top;
+        // x / x is exactly 1 and 0 / x exactly 0: those divisions are skipped
+        const double n = v[r] == top ? 1.0 : v[r] == 0.0 ? 0.0 : v[r] / top;
         const double summand = n * n - compensation;
         const double preliminary = total + summand;
         compensation = (preliminary - total) - summand;
@@ -266,12 +268,16 @@ __device__ bool floatTestOf(const GridView& g, const Box& b, const double c[3], 
     for (int a = 0; a < 3; a++) {
         const double r = e.radius[a];
         if (!(r > 1e-30 && r < 1e30)) return false;
+        // the float reciprocal of float(r): within 2^-23 of 1 / r, inside the
+        // 2^-21 |t| allowance
+        f.inv[a] = __frcp_rn(float(r));
         double dotErr = 0.0;
         for (int k = 0; k < 3; k++) dotErr += fabs(e.col[3 * a + k]) * (ex[k] + 0x1p-22 * X[k]);
-        const double err = 4.0 * dotErr / r;
+        // above 4 dotErr / r: the reciprocal's error and every rounding of
+        // this product are covered by the (1 + 2^-20)
+        const double err = 4.0 * dotErr * double(f.inv[a]) * (1.0 + 0x1p-20);
         if (!(err < 1e-3)) return false;
         f.err[a] = float(err);
-        f.inv[a] = float(1.0 / r);
     }
     return true;
 }
@@ -454,20 +460,46 @@ __device__ void unite(uint32_t* L, uint32_t a, uint32_t b, uint32_t* err) {
     atomicOr(err, 1u);
 }
 
-__global__ void labelInitKernel(uint32_t* __restrict__ L, uint32_t cells) {
-    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < cells; idx += gridDim.x * blockDim.x)
-        L[idx] = idx;
+// The labels seeded with x runs: a block takes kCloudBlock consecutive
+// cells (a chunk starts at a multiple of kCloudBlock), and an empty cell
+// whose -x neighbour is empty, in the same row and the same chunk, takes the
+// label of its run's first cell (by ballot within a warp, then the last run
+// start of the warps before it); every other cell labels itself. This joins
+// the x edges inside a chunk without atomics.
+__global__ void labelRunsKernel(const uint8_t* __restrict__ occ, uint32_t* __restrict__ L, Dims d) {
+    __shared__ int lastStart[kCloudBlock / 32];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t base = blockIdx.x * kCloudBlock; base < d.cells; base += gridDim.x * kCloudBlock) {
+        const uint32_t idx = base + threadIdx.x;
+        const bool empty = idx < d.cells && occ[idx] == 0;
+        const bool linked = empty && threadIdx.x > 0 && occ[idx - 1] == 0 && idx % d.nx != 0;
+        const uint32_t starts = __ballot_sync(0xffffffffu, !linked);
+        if (lane == 31) lastStart[warp] = starts ? int(warp * 32 + 31 - __clz(starts)) : -1;
+        __syncthreads();
+        const uint32_t mine = starts & (0xffffffffu >> (31 - lane));
+        int start = mine ? int(warp * 32 + 31 - __clz(mine)) : -1;
+        for (int w = int(warp) - 1; start < 0 && w >= 0; w--) start = lastStart[w];
+        // thread 0 is never linked, so every thread finds a start
+        if (idx < d.cells) L[idx] = base + uint32_t(start);
+        __syncthreads();
+    }
 }
 
-// Every empty cell joined with its empty -x, -y and -z neighbours: together
-// each face-adjacent pair of empty cells once (cloudVolume.js:88-89, 359-364).
+// The remaining face-adjacent pairs of empty cells joined
+// (cloudVolume.js:88-89, 359-364): an x edge across a chunk boundary; a y
+// (z) edge unless the two cells' -x neighbours are both empty, in which case
+// it is implied by edges already joined (cell ~ its -x neighbour ~ that
+// one's -y (-z) neighbour ~ the cell's -y (-z) neighbour), so each stretch
+// of overlapping runs is joined once, at its first cell.
 __global__ void labelMergeKernel(const uint8_t* __restrict__ occ, uint32_t* L, Dims d, uint32_t* err) {
+    const uint32_t plane = d.nx * d.ny;
     for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < d.cells; idx += gridDim.x * blockDim.x) {
         if (occ[idx] != 0) continue;
-        const uint32_t i = idx % d.nx, j = (idx / d.nx) % d.ny, k = idx / (d.nx * d.ny);
-        if (i > 0 && occ[idx - 1] == 0) unite(L, idx, idx - 1, err);
-        if (j > 0 && occ[idx - d.nx] == 0) unite(L, idx, idx - d.nx, err);
-        if (k > 0 && occ[idx - d.nx * d.ny] == 0) unite(L, idx, idx - d.nx * d.ny, err);
+        const uint32_t i = idx % d.nx, j = (idx / d.nx) % d.ny, k = idx / plane;
+        const bool left = i > 0 && occ[idx - 1] == 0;
+        if (left && idx % kCloudBlock == 0) unite(L, idx, idx - 1, err);
+        if (j > 0 && occ[idx - d.nx] == 0 && !(left && occ[idx - 1 - d.nx] == 0)) unite(L, idx, idx - d.nx, err);
+        if (k > 0 && occ[idx - plane] == 0 && !(left && occ[idx - 1 - plane] == 0)) unite(L, idx, idx - plane, err);
     }
 }
 
@@ -531,12 +563,42 @@ struct CloudScalars {
     uint32_t pad;
 };
 
+// Scratch comes from a stream-ordered memory pool of this library's own, one
+// per device, that keeps what a call frees for the next call instead of
+// unmapping it: repeated voxelisations do not remap hundreds of megabytes.
+// The pool holds the largest scratch any call needed until the process exits.
+int scratchPool(int device, cudaMemPool_t* out) {
+    static std::mutex lock;
+    static cudaMemPool_t pools[64] = {};
+    if (device < 0 || device >= 64) return fail(VSIM_ERR_INVALID, "device ordinal out of range");
+    std::lock_guard<std::mutex> hold(lock);
+    if (!pools[device]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        CK(cudaMemPoolCreate(&pools[device], &props), "memory pool");
+        uint64_t keep = ~0ull;
+        CK(cudaMemPoolSetAttribute(pools[device], cudaMemPoolAttrReleaseThreshold, &keep), "memory pool");
+    }
+    *out = pools[device];
+    return VSIM_OK;
+}
+
+// A pool allocation freed, in stream order, when it goes out of scope.
 struct DeviceBuffer {
     void* p = nullptr;
+    cudaStream_t stream = nullptr;
     ~DeviceBuffer() {
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, stream);
     }
 };
+
+#define POOL_ALLOC(buffer, bytes, pool, st, what)                                         \
+    do {                                                                                   \
+        (buffer).stream = (st);                                                            \
+        CK(cudaMallocFromPoolAsync(&(buffer).p, (bytes), (pool), (st)), what);             \
+    } while (0)
 
 uint32_t streamGrid(uint64_t items, int sms) {
     const uint64_t want = (items + kCloudBlock - 1) / kCloudBlock;
@@ -547,16 +609,18 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     cudaStream_t st = v->stream;
     int sms = 1;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, v->device), "device attributes");
+    cudaMemPool_t pool;
+    if (int rc = scratchPool(v->device, &pool)) return rc;
 
     // 1. bounds
     DeviceBuffer scalarsBuf;
-    CK(cudaMalloc(&scalarsBuf.p, sizeof(CloudScalars)), "cloud scratch");
+    POOL_ALLOC(scalarsBuf, sizeof(CloudScalars), pool, st, "cloud scratch");
     auto* sc = static_cast<CloudScalars*>(scalarsBuf.p);
     CloudScalars init{};
     for (int a = 0; a < 3; a++) init.keys[a] = ~0ull;
     CK(cudaMemcpyAsync(sc, &init, sizeof init, cudaMemcpyHostToDevice, st), "cloud scratch");
     DeviceBuffer reachBuf;
-    CK(cudaMalloc(&reachBuf.p, size_t(in.count) * 3 * sizeof(double)), "cloud scratch");
+    POOL_ALLOC(reachBuf, size_t(in.count) * 3 * sizeof(double), pool, st, "cloud scratch");
     auto* reach = static_cast<double*>(reachBuf.p);
     cloudBoundsKernel<<<streamGrid(in.count, sms), kCloudBlock, 0, st>>>(in, sc->keys, &sc->nan, reach);
     CK(cudaGetLastError(), "cloud bounds");
@@ -599,12 +663,12 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     g.h = h;
     g.cells = n;
 
-    CK(cudaMalloc(&v->occupancy, n), "cloud occupancy");
+    CK(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&v->occupancy), n, pool, st), "cloud occupancy");
     CK(cudaMemsetAsync(v->occupancy, 0, n, st), "cloud occupancy");
 
     // 3. stamp
     DeviceBuffer bigBuf;
-    CK(cudaMalloc(&bigBuf.p, size_t(in.count) * 4), "cloud scratch");
+    POOL_ALLOC(bigBuf, size_t(in.count) * 4, pool, st, "cloud scratch");
     cloudStampKernel<<<(in.count + kCloudBlock - 1) / kCloudBlock, kCloudBlock, 0, st>>>(
         in, g, reach, v->occupancy, static_cast<uint32_t*>(bigBuf.p), &sc->bigCount);
     cloudStampBoxKernel<<<uint32_t(sms) * 4, kCloudBlock, 0, st>>>(
@@ -616,7 +680,7 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     if (o.fill) {
         // stamp copy, a ping-pong buffer, labels, reached flags
         DeviceBuffer work;
-        CK(cudaMalloc(&work.p, size_t(n) * 7 + 64), "cloud fill scratch");
+        POOL_ALLOC(work, size_t(n) * 7 + 64, pool, st, "cloud fill scratch");
         auto* labels = static_cast<uint32_t*>(work.p);
         uint8_t* stamp = reinterpret_cast<uint8_t*>(labels + n);
         uint8_t* other = stamp + n;
@@ -628,7 +692,7 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
             std::swap(cur, other);
         }
         CK(cudaMemsetAsync(reached, 0, n, st), "cloud fill");
-        labelInitKernel<<<grid, kCloudBlock, 0, st>>>(labels, n);
+        labelRunsKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, d);
         labelMergeKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, d, &sc->err);
         markFaceRootsKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, reached, d, &sc->err);
         fillEnclosedKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, reached, n, &sc->filled, &sc->err);
@@ -678,7 +742,7 @@ int newVolume(vsim_cloud_volume** out, vsim_cloud_volume** made) {
 
 void destroyVolume(vsim_cloud_volume* v) {
     if (!v) return;
-    if (v->occupancy) cudaFree(v->occupancy);
+    if (v->occupancy) cudaFreeAsync(v->occupancy, v->stream);
     if (v->stream) cudaStreamDestroy(v->stream);
     delete v;
 }
@@ -700,12 +764,9 @@ int vsim_voxelize_cloud_device(const float* d_positions, const float* d_rotation
     if (int rc = newVolume(out, &v)) return rc;
     // the caller's work on the inputs finishes first
     cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) {
-        destroyVolume(v);
-        return cudaFail(e, "caller stream");
-    }
-    const CloudInput in{d_positions, d_rotations, d_scales, uint32_t(count), options->sigma};
-    const int rc = voxelizeCloud(v, in, *options);
+    int rc = e == cudaSuccess ? VSIM_OK : cudaFail(e, "caller stream");
+    if (!rc) rc = voxelizeCloud(v, CloudInput{d_positions, d_rotations, d_scales, uint32_t(count), options->sigma},
+                                *options);
     if (rc) {
         cudaStreamSynchronize(v->stream);
         destroyVolume(v);
@@ -715,21 +776,41 @@ int vsim_voxelize_cloud_device(const float* d_positions, const float* d_rotation
     return VSIM_OK;
 }
 
+namespace {
+
+// Host inputs copied into pool memory on the volume's stream, then the device path.
+int voxelizeHostCloud(vsim_cloud_volume* v, const float* positions, const float* rotations, const float* scales,
+                      size_t n, const vsim_cloud_options& o) {
+    cudaMemPool_t pool;
+    if (int rc = scratchPool(v->device, &pool)) return rc;
+    DeviceBuffer inputs;
+    POOL_ALLOC(inputs, n * 40, pool, v->stream, "cloud inputs");
+    auto* dPos = static_cast<float*>(inputs.p);
+    float* dRot = dPos + 3 * n;
+    float* dScale = dRot + 4 * n;
+    CK(cudaMemcpyAsync(dPos, positions, n * 12, cudaMemcpyHostToDevice, v->stream), "cloud inputs");
+    CK(cudaMemcpyAsync(dRot, rotations, n * 16, cudaMemcpyHostToDevice, v->stream), "cloud inputs");
+    CK(cudaMemcpyAsync(dScale, scales, n * 12, cudaMemcpyHostToDevice, v->stream), "cloud inputs");
+    return voxelizeCloud(v, CloudInput{dPos, dRot, dScale, uint32_t(n), o.sigma}, o);
+}
+
+}  // namespace
+
 int vsim_voxelize_cloud(const float* positions, const float* rotations, const float* scales, uint64_t count,
                         const vsim_cloud_options* options, vsim_cloud_volume** out) {
     clearError();
     if (int rc = checkOptions(options, count)) return rc;
     if (!positions || !rotations || !scales) return fail(VSIM_ERR_INVALID, "NULL cloud array");
-    DeviceBuffer inputs;
-    const size_t n = size_t(count);
-    CK(cudaMalloc(&inputs.p, n * 40), "cloud inputs");
-    auto* dPos = static_cast<float*>(inputs.p);
-    float* dRot = dPos + 3 * n;
-    float* dScale = dRot + 4 * n;
-    CK(cudaMemcpy(dPos, positions, n * 12, cudaMemcpyHostToDevice), "cloud inputs");
-    CK(cudaMemcpy(dRot, rotations, n * 16, cudaMemcpyHostToDevice), "cloud inputs");
-    CK(cudaMemcpy(dScale, scales, n * 12, cudaMemcpyHostToDevice), "cloud inputs");
-    return vsim_voxelize_cloud_device(dPos, dRot, dScale, count, options, nullptr, out);
+    vsim_cloud_volume* v = nullptr;
+    if (int rc = newVolume(out, &v)) return rc;
+    const int rc = voxelizeHostCloud(v, positions, rotations, scales, size_t(count), *options);
+    if (rc) {
+        cudaStreamSynchronize(v->stream);
+        destroyVolume(v);
+        return rc;
+    }
+    *out = v;
+    return VSIM_OK;
 }
 
 int vsim_cloud_volume_grid(const vsim_cloud_volume* volume, vsim_cloud_grid* out) {

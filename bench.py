@@ -606,6 +606,7 @@ def main():
     ap.add_argument("--no-stress", action="store_true")
     ap.add_argument("--no-cloud", action="store_true")
     ap.add_argument("--stress-only", action="store_true", help="only the stress workload's frames (for captures)")
+    ap.add_argument("--cloud-only", action="store_true", help="only the cloud voxeliser section (for captures)")
     ap.add_argument("--capture-after", type=int, default=None, metavar="N",
                     help="profiler capture mode: run N frames of the bench workload, then bracket one more frame "
                          "(or --capture-substeps substeps) with cudaProfilerStart/Stop for "
@@ -649,6 +650,9 @@ def main():
     torch.cuda.set_device(local)
     if args.stress_only:
         print(json.dumps({"stress": stress(args.quick, peaks()[0], frames=args.steps)}))
+        return
+    if args.cloud_only:
+        print(json.dumps({"cloud_voxelize": cloud_voxelize(args.quick)}))
         return
     if args.capture_after is not None:
         sim = Simulator(scene)

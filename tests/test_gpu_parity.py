@@ -473,3 +473,55 @@ def test_radix_sort_matches_stable_sort(lib, gpu, n, bits):
     got = do.cpu().numpy().view(np.uint32)
     assert np.array_equal(got, pyoracle.stable_sort(keys, bits))
     assert np.array_equal(dk.cpu().numpy().view(np.uint32), keys)  # input untouched
+
+
+def test_scene_with_no_bodies(lib):
+    """A scene can be all backdrop (simulator.js:162-187): nothing steps, no
+    body limits the CFL, and every call still answers."""
+    import vsim.scenes as sc
+
+    scene = sc.Scene([], ((-1.0, 0.0, -1.0), (1.0, 1.0, 1.0)), step_duration=1 / 600, substeps=10)
+    sim, orc = make(scene)
+    assert sim.node_count == 0
+    sim.dispatch(10)
+    sim.step(1 / 60)
+    sim.synchronize()
+    assert sim.read_positions().shape == (0, 4)
+    st = sim.stats()
+    assert st["body_count"] == 0 and st["limited_by"] == -1 and st["cells"] == 0
+    assert sim.contact_pairs().shape[0] == 0
+    sim.reset()
+    sim.destroy()
+
+
+def test_degenerate_bodies_dispatch_zero_and_pause(lib):
+    """A body with no occupied cell beside a normal one and a body whose
+    every node is static: frames equal the oracle and the static body never
+    moves; dispatch(0) changes nothing; a paused simulator takes a step only
+    when one is requested (simulator.js:239-318)."""
+    import vsim.scenes as sc
+
+    live = sc.Body((4, 4, 4), (0.0, 0.02, 0.0), sc.H, np.ones(64, np.uint8))
+    empty = sc.Body((3, 3, 3), (0.2, 0.02, 0.0), sc.H, np.zeros(27, np.uint8))
+    pinned = sc.Body((4, 4, 4), (0.4, 0.02, 0.0), sc.H, np.ones(64, np.uint8),
+                     static_nodes=np.arange(125, dtype=np.uint32))
+    scene = sc.Scene([live, empty, pinned], ((-1.0, 0.0, -1.0), (1.0, 1.0, 1.0)), step_duration=1 / 600,
+                     substeps=10)
+    sim, orc = make(scene)
+    rest = sim.read_positions()
+    sim.dispatch(0)
+    assert np.array_equal(sim.read_positions(), rest)
+    for frame in range(5):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"frame {frame}")
+    first = sim.offsets[2]
+    assert np.array_equal(sim.read_positions()[first:first + 125], rest[first:first + 125])
+    sim.paused = True
+    before = sim.read_positions()
+    sim.step(1 / 60)
+    assert np.array_equal(sim.read_positions(), before)
+    sim.request_step()
+    sim.step(1 / 60)
+    orc.dispatch(1)
+    assert_same(sim, orc, scene, "requested step while paused")

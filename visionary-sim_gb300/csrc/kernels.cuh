@@ -177,6 +177,7 @@ cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, c
 cudaError_t launchZeroW(cudaStream_t st, const uint32_t* nodes, uint32_t n, float4* pos);
 cudaError_t launchRefreshW(cudaStream_t st, uint32_t first, uint32_t n, const float* base, float4* pos);
 cudaError_t launchMergeXyz(cudaStream_t st, const float4* in, uint32_t n, float4* pos);
+cudaError_t launchDropW(cudaStream_t st, const float4* in, uint32_t n, float4* out);
 
 // ---- splats ---------------------------------------------------------------
 

@@ -366,17 +366,8 @@ int vsim_server_read_state(vsim_server* s, uint32_t session, float* pos, float* 
     DeviceGuard guard(sim->device);
     if (session >= s->admitted) return fail(VSIM_ERR_RANGE, "session is not resident");
     if (node_count != sim->lat[session].nodeCount) return fail(VSIM_ERR_CAPACITY, "node_count does not match");
-    const size_t first = sim->offsets[session];
-    float* out[3] = {pos, prev, vel};
-    const float4* from[3] = {sim->d.pos + first, sim->d.prev + first, sim->d.vel + first};
-    for (int a = 0; a < 3; a++)
-        if (out[a])
-            CK(cudaMemcpyAsync(out[a], from[a], node_count * 16, cudaMemcpyDeviceToHost, sim->stream), "read session");
-    CK(cudaStreamSynchronize(sim->stream), "read session");
-    for (int a = 0; a < 3; a++)
-        if (out[a])
-            for (size_t n = 0; n < node_count; n++) out[a][4 * n + 3] = 0.0f;
-    return VSIM_OK;
+    float* const out[3] = {pos, prev, vel};
+    return readNodes(sim, sim->offsets[session], node_count, out);
 }
 
 int vsim_server_write_state(vsim_server* s, uint32_t session, const float* pos, const float* prev, const float* vel,

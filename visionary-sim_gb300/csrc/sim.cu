@@ -372,6 +372,23 @@ int runFrame(vsim_sim* s, uint32_t steps) {
     return VSIM_OK;
 }
 
+// Nodes [first, first + count) of pos, prev and vel (those of `out` not
+// NULL) to the host as xyzw with w = 0, the ABI's form: w is cleared on the
+// device into the staging buffer, one array at a time (stream order keeps
+// the next clear behind the previous copy), so the host gets each array in
+// one copy and touches nothing after it.
+int readNodes(vsim_sim* s, size_t first, size_t count, float* const out[3]) {
+    const float4* from[3] = {s->d.pos + first, s->d.prev + first, s->d.vel + first};
+    if (count > 0 && !s->staging) CK(allocN(&s->staging, s->nodeCount), "allocate staging");
+    for (int a = 0; a < 3; a++) {
+        if (!out[a] || count == 0) continue;
+        CK(launchDropW(s->stream, from[a], uint32_t(count), s->staging), "read state");
+        CK(cudaMemcpyAsync(out[a], s->staging, count * 16, cudaMemcpyDeviceToHost, s->stream), "read state");
+    }
+    CK(cudaStreamSynchronize(s->stream), "read state");
+    return VSIM_OK;
+}
+
 void freeSim(vsim_sim* s) {
     dropGraphs(s);
     DeviceState& d = s->d;
@@ -749,16 +766,8 @@ int vsim_read_positions(vsim_sim* s, float* xyzw, size_t node_count) {
 int vsim_read_state(vsim_sim* s, float* pos, float* prev, float* vel, size_t node_count) {
     SIM_GUARD(s);
     if (node_count != s->nodeCount) return fail(VSIM_ERR_CAPACITY, "node_count does not match the simulator");
-    float* out[3] = {pos, prev, vel};
-    const float4* from[3] = {s->d.pos, s->d.prev, s->d.vel};
-    for (int a = 0; a < 3; a++)
-        if (out[a])
-            CK(cudaMemcpyAsync(out[a], from[a], node_count * 16, cudaMemcpyDeviceToHost, s->stream), "read state");
-    CK(cudaStreamSynchronize(s->stream), "read state");
-    for (int a = 0; a < 3; a++)
-        if (out[a])
-            for (size_t n = 0; n < node_count; n++) out[a][4 * n + 3] = 0.0f;
-    return VSIM_OK;
+    float* const out[3] = {pos, prev, vel};
+    return readNodes(s, 0, node_count, out);
 }
 
 int vsim_write_state(vsim_sim* s, const float* pos, const float* prev, const float* vel, size_t node_count) {

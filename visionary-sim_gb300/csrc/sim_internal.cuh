@@ -142,6 +142,8 @@ int syncParams(vsim_sim* s);
 // Replaces the held set (global nodes, offsets xyz), keeping the hard law's
 // prescription in step.
 int holdNodes(vsim_sim* s, const uint32_t* nodes, const float* offsets, uint32_t count);
+// Node state to the host as xyzw with w = 0 (vsim_read_state's form).
+int readNodes(vsim_sim* s, size_t first, size_t count, float* const out[3]);
 int releaseNodes(vsim_sim* s);
 uint32_t bodyOfNode(const vsim_sim* s, uint32_t node);
 Grid bodyGrid(const Lattice& L, const vsim_tank& tank);

@@ -985,6 +985,15 @@ __global__ void mergeXyzKernel(const float4* __restrict__ in, uint32_t n, float4
     }
 }
 
+// out := (in.xyz, 0): a state read out (positions cross the ABI with w 0).
+__global__ void dropWKernel(const float4* __restrict__ in, uint32_t n, float4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float4 a = in[i];
+        out[i] = make_float4(a.x, a.y, a.z, 0.0f);
+    }
+}
+
 // ------------------------------------------------------------ launchers --
 
 namespace {
@@ -1110,6 +1119,12 @@ cudaError_t launchZeroW(cudaStream_t st, const uint32_t* nodes, uint32_t n, floa
 cudaError_t launchRefreshW(cudaStream_t st, uint32_t first, uint32_t n, const float* base, float4* pos) {
     if (n == 0) return cudaSuccess;
     refreshWKernel<<<blocks(n, 256), 256, 0, st>>>(first, n, base, pos);
+    return cudaGetLastError();
+}
+
+cudaError_t launchDropW(cudaStream_t st, const float4* in, uint32_t n, float4* out) {
+    if (n == 0) return cudaSuccess;
+    dropWKernel<<<blocks(n, 256), 256, 0, st>>>(in, n, out);
     return cudaGetLastError();
 }
 

@@ -76,15 +76,18 @@ def test_rotated_anisotropic_capture(vz):
     _same(vz, cloud, 0.006, seal=0)
 
 
-def test_large_boxes_take_the_block_stamp(vz):
-    # Gaussians reaching ~6 cells each way: boxes of ~13^3 cells, far over
-    # the 64 a thread stamps inline, mixed with small ones
+@pytest.mark.parametrize("large", [0.006, 0.0025])
+def test_box_sizes_and_stamp_paths(vz, large):
+    # Gaussians reaching ~6 cells each way (boxes of ~13^3 cells, over the
+    # 64 a thread stamps inline, so a block each) or ~2.5 (boxes of 125-343
+    # cells, also a block each, a few rounds of its threads), mixed with
+    # small ones
     rng = np.random.default_rng(3)
     n = 400
     pos = rng.uniform(-0.1, 0.1, (n, 3)).astype(np.float32)
     q = rng.normal(size=(n, 4))
     q /= np.linalg.norm(q, axis=1, keepdims=True)
-    scale = np.where(rng.random((n, 1)) < 0.5, 0.006, 0.0004) * rng.uniform(0.5, 1.5, (n, 3))
+    scale = np.where(rng.random((n, 1)) < 0.5, large, 0.0004) * rng.uniform(0.5, 1.5, (n, 3))
     _same(vz, (pos, q.astype(np.float32), scale.astype(np.float32)), 0.002)
     long = _cloud_at([0, 0, 0], 1)
     long[2][:] = [0.05, 0.004, 0.004]

@@ -412,7 +412,9 @@ int vsim_radix_sort_u32_noalloc(const uint32_t* d_keys, uint32_t* d_order, uint3
 /*
  * No counterpart in the reference (one simulator per page). A server holds a
  * pool of sessions -- one body each, isolated from one another -- resident on
- * the device, admitted in order while their state fits an HBM budget.
+ * the device, admitted in order while their state fits an HBM budget; which
+ * sessions are resident can be changed between ticks (eviction: the state of
+ * a session that leaves is kept on the host and restored when it returns).
  * Requests ask a session to advance some frames, optionally dragging one of
  * its nodes (hard law) toward a target moving along a cubic Bezier curve.
  * Every tick runs one frame for every session with a pending request, in one
@@ -446,9 +448,9 @@ typedef struct vsim_completion {
 } vsim_completion;
 
 typedef struct vsim_server_stats {
-    uint32_t sessions;        /* admitted */
-    uint32_t rejected;        /* not admitted: over the budget */
-    double resident_bytes;    /* device bytes the admitted sessions hold */
+    uint32_t sessions;        /* resident */
+    uint32_t rejected;        /* not admitted at creation: over the budget */
+    double resident_bytes;    /* device bytes the resident sessions hold */
     uint64_t ticks;
     uint64_t session_frames;  /* frames run, summed over sessions */
     uint64_t cell_updates;    /* occupied cells x substeps, summed over frames run */
@@ -461,11 +463,25 @@ typedef struct vsim_server_stats {
 int vsim_server_create(const vsim_body_desc* sessions, uint32_t count, const vsim_tank* tank,
                        const vsim_server_config* config, void* stream, vsim_server** out);
 int vsim_server_destroy(vsim_server* server);
-/* Sessions 0 .. admitted-1 are resident; the rest did not fit the budget. */
+/* How many sessions are resident. At creation they are sessions
+   0 .. admitted-1 (the rest did not fit the budget). */
 uint32_t vsim_server_admitted(const vsim_server* server);
+/* The resident sessions, in the order of the device pool (NULL sessions:
+   only *count). VSIM_ERR_CAPACITY when `capacity` is smaller. */
+int vsim_server_resident(const vsim_server* server, uint32_t* sessions, uint32_t capacity, uint32_t* count);
+/* Makes exactly `sessions` resident, in that order. Every session leaving
+   the device must be idle (no request queued or running, else
+   VSIM_ERR_INVALID); its state is kept on the host and written back when it
+   is made resident again -- it then continues exactly as if it had stayed
+   (a session never run starts at rest). The set must fit the budget (else
+   VSIM_ERR_NOMEM, nothing changed). Drags still held from finished requests
+   are let go. The device pool is rebuilt: the cost is that of creating it
+   (lattices, uploads), paid once per call. */
+int vsim_server_set_resident(vsim_server* server, const uint32_t* sessions, uint32_t count);
 /* Seconds on the server's monotonic clock. */
 double vsim_server_clock(const vsim_server* server);
-/* Queue `frames` frames for `session` (FIFO per session); drag may be NULL. */
+/* Queue `frames` frames for `session` (FIFO per session); drag may be NULL.
+   The session must be resident (else VSIM_ERR_RANGE). */
 int vsim_server_submit(vsim_server* server, uint32_t session, uint32_t frames, const vsim_drag* drag,
                        uint64_t* request);
 /* Run one frame for every session with a pending request and wait for it;

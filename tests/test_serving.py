@@ -196,3 +196,66 @@ def test_session_checkpoint_restore_and_reset(lib):
     for a, b in zip(server.read_state(1), rest):
         assert np.array_equal(a, b)
     server.destroy()
+
+
+def test_eviction_and_readmission(lib):
+    """Sessions evicted to the host and made resident again -- in another
+    pool order, beside other sessions -- continue exactly as in a server
+    that never moved them; a session with requests pending cannot leave; a
+    set over the budget is refused and changes nothing; a session that is
+    not resident takes no requests; a session never run arrives at rest."""
+    import vsim.scenes as sc
+    from vsim import _ffi
+    from vsim.server import Server
+
+    bodies, tank = small_pool(6, seed=23)
+    rng = np.random.default_rng(8)
+    drags = {s: sc.drag_request(bodies[s], rng) for s in (1, 4)}
+    plan1 = [(0, 3, None), (1, 2, drags[1]), (2, 4, None), (3, 1, None), (4, 2, drags[4]), (5, 3, None)]
+    plan2 = [(0, 2, None), (1, 3, drags[1]), (3, 2, None), (4, 1, drags[4])]
+
+    def run(server, requests):
+        for session, frames, d in requests:
+            server.submit(session, frames, d)
+        while server.stats()["pending"]:
+            server.tick()
+        server.poll()
+
+    kept = Server(bodies, tank)
+    run(kept, plan1)
+    run(kept, plan2)
+
+    moved = Server(bodies, tank)
+    run(moved, plan1)
+    moved.set_resident([5, 2])
+    assert moved.resident == [5, 2] and moved.admitted == 2 and moved.stats()["sessions"] == 2
+    with pytest.raises(_ffi.VsimError):
+        moved.submit(0, 1)
+    moved.set_resident([4, 3, 1, 0, 2])
+    run(moved, plan2)
+    for s in range(5):
+        for a, b in zip(kept.read_state(s), moved.read_state(s)):
+            assert np.array_equal(a, b), f"session {s}"
+
+    moved.submit(0, 1)
+    with pytest.raises(_ffi.VsimError):
+        moved.set_resident([1, 2])
+    run(moved, [])
+    assert moved.resident == [4, 3, 1, 0, 2]
+
+    per = kept.stats()["resident_bytes"] / 6
+    tight = Server(bodies, tank, budget_bytes=per * 2.5)
+    before = tight.resident
+    with pytest.raises(_ffi.VsimError):
+        tight.set_resident([0, 1, 2, 3, 4, 5])
+    assert tight.resident == before == list(range(tight.admitted))
+
+    fresh = Server(bodies, tank)
+    rest = fresh.read_state(5)
+    fresh.set_resident([])
+    assert fresh.admitted == 0 and fresh.resident == []
+    fresh.set_resident([5])
+    for a, b in zip(fresh.read_state(5), rest):
+        assert np.array_equal(a, b)
+    for server in (kept, moved, tight, fresh):
+        server.destroy()

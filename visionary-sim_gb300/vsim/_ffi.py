@@ -169,6 +169,8 @@ SIGNATURES = {
                                      C.POINTER(_P)]),
     "vsim_server_destroy": (C.c_int, [_P]),
     "vsim_server_admitted": (C.c_uint32, [_P]),
+    "vsim_server_resident": (C.c_int, [_P, _U, C.c_uint32, _U]),
+    "vsim_server_set_resident": (C.c_int, [_P, _U, C.c_uint32]),
     "vsim_server_clock": (C.c_double, [_P]),
     "vsim_server_submit": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(Drag), C.POINTER(C.c_uint64)]),
     "vsim_server_tick": (C.c_int, [_P, C.POINTER(C.c_uint32)]),

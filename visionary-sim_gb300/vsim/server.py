@@ -22,8 +22,12 @@ class Server:
                                        C.byref(cfg), C.c_void_p(stream), C.byref(handle)))
         self._h = handle
         self.bodies = list(bodies)
-        self.admitted = int(lib().vsim_server_admitted(handle))
         self._buf = (_ffi.Completion * 4096)()
+
+    @property
+    def admitted(self) -> int:
+        """How many sessions are resident (vsim_server_admitted)."""
+        return int(lib().vsim_server_admitted(self._h))
 
     def destroy(self):
         if self._h:
@@ -38,6 +42,23 @@ class Server:
 
     def clock(self) -> float:
         return float(lib().vsim_server_clock(self._h))
+
+    @property
+    def resident(self) -> list:
+        """The resident sessions, in device-pool order (vsim_server_resident)."""
+        count = C.c_uint32()
+        check(lib().vsim_server_resident(self._h, None, 0, C.byref(count)))
+        out = np.zeros(count.value, np.uint32)
+        check(lib().vsim_server_resident(self._h, out.ctypes.data_as(C.POINTER(C.c_uint32)), count.value,
+                                         C.byref(count)))
+        return [int(v) for v in out]
+
+    def set_resident(self, sessions):
+        """Make exactly `sessions` resident (vsim_server_set_resident): sessions
+        leaving are checkpointed on the host, sessions returning resume from
+        their checkpoint."""
+        ids = np.ascontiguousarray(np.asarray(list(sessions), np.uint32))
+        check(lib().vsim_server_set_resident(self._h, ids.ctypes.data_as(C.POINTER(C.c_uint32)), int(ids.size)))
 
     def submit(self, session: int, frames: int, drag=None) -> int:
         """Queue `frames` frames for `session`; drag = (node, control 4x3, speed)."""

@@ -112,7 +112,6 @@ void frameParams(vsim_sim* s) {
     f.perBodyGrab = s->perBodyGrab ? 1u : 0u;
     f.selfContact = s->selfContact ? 1u : 0u;
     f.activeCount = s->activeCount;
-    f.maxRadius = s->maxRadius;
 }
 
 // Uploads what changed since the last frame, in stream order.
@@ -521,7 +520,6 @@ int createSim(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, v
     }
     s->surfaceCount = uint32_t(s->surfHost.size());
     s->recordBodyStart[n] = s->surfaceCount;
-    s->maxRadius = float(widest);
     if (!s->isolated) {
         s->grids.push_back(contactGrid(s->tank, widest, lo, hi));
     } else {

@@ -71,7 +71,6 @@ struct vsim_sim {
     std::vector<float> baseW;    // invMass with static nodes zeroed
     std::vector<float> restPos;  // xyzw per node, w = baseW
     uint32_t nodeCount = 0, activeCount = 0, cellCount = 0, surfaceCount = 0;
-    float maxRadius = 0;  // largest contact radius of a surface record
     uint32_t colorStart[9] = {};
     std::vector<uint4> surfHost;
     vsim_tank tank{};

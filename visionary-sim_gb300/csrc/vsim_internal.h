@@ -135,7 +135,6 @@ struct FrameParams {
     uint32_t selfContact;
     uint32_t activeCount;
     uint32_t perBodyGrab;  // drive targets come from the per-body table, not grabTarget
-    float maxRadius;       // the largest contact radius of any surface record
 };
 
 }  // namespace vsim

@@ -218,6 +218,12 @@ class Oracle:
     def set_step_duration(self, seconds):
         lib().vo_set_step_duration(self._h, float(seconds))
 
+    def set_contact(self, enabled: bool):
+        lib().vo_set_contact(self._h, int(bool(enabled)))
+
+    def set_self_contact(self, enabled: bool):
+        lib().vo_set_self_contact(self._h, int(bool(enabled)))
+
     def splat_deform(self, body, means, quats, scales, view_dir=(0.0, 0.0, -1.0)):
         n = means.shape[0]
         means = np.ascontiguousarray(means, np.float32)

@@ -525,3 +525,68 @@ def test_degenerate_bodies_dispatch_zero_and_pause(lib):
     sim.step(1 / 60)
     orc.dispatch(1)
     assert_same(sim, orc, scene, "requested step while paused")
+
+
+@pytest.mark.parametrize("block,brick", [(128, 0), (512, 4), (256, 8)])
+def test_launch_shapes_agree(lib, block, brick):
+    """Every elastic block size and cell order (lattice order, 4^3 and 8^3
+    bricks) the autotuner chooses from gives the oracle's frames: cells of
+    one colour share no node, so their order cannot change a result."""
+    import vsim.scenes as sc
+
+    scene = sc.box_batch(12, seed=7)
+    sim, orc = make(scene)
+    sim.set_launch_shape(block, brick)
+    for frame in range(4):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"block {block} brick {brick} frame {frame}")
+
+
+def test_tune_keeps_state(lib):
+    """vsim_tune times every shape on the live state, puts the state back,
+    and keeps a valid shape; frames afterwards equal the oracle's."""
+    import vsim.scenes as sc
+
+    scene = sc.box_batch(12, seed=7)
+    sim, orc = make(scene)
+    for frame in range(2):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+    before = sim.read_state()
+    block, brick = sim.tune(1)
+    assert block in (128, 256, 512) and brick in (0, 4, 8)
+    for a, b in zip(before, sim.read_state()):
+        assert np.array_equal(a, b)
+    for frame in range(3):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"after tuning, frame {frame}")
+
+
+def test_gravity_and_contact_switched_midrun(lib):
+    """params.gravity and setContact (simulator.js:60-66, 470-480) changed
+    between frames: the blob's frames equal the oracle's with the same
+    switches -- contact off and on again, self contact off, sideways
+    gravity."""
+    import vsim.scenes as sc
+
+    scene = sc.noise_blob(n=16, seed=3, splats=0)
+    sim, orc = make(scene)
+    steps = [("frames", 3), ("contact", False), ("frames", 2), ("contact", True), ("self", False),
+             ("frames", 2), ("gravity", (2.0, -4.0, 1.0)), ("frames", 3), ("self", True), ("frames", 2)]
+    for what, arg in steps:
+        if what == "contact":
+            sim.set_contact(arg)
+            orc.set_contact(arg)
+        elif what == "self":
+            sim.set_self_contact(arg)
+            orc.set_self_contact(arg)
+        elif what == "gravity":
+            sim.gravity = arg
+            orc.set_gravity(arg)
+        else:
+            for frame in range(arg):
+                sim.dispatch(scene.substeps)
+                orc.dispatch(scene.substeps)
+                assert_same(sim, orc, scene, f"{what} {frame}")

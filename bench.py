@@ -443,6 +443,59 @@ def cloud_voxelize(quick: bool, reps: int = 5):
             "grid_equal_to_host": host.dims == dims and bool(np.array_equal(host.occupancy, occupancy.numpy()))}
 
 
+def tick_sweep(quick: bool, capture: int | None = None, reps: int = 25, settle_frames: int = 30):
+    """Tick time of the session server against the number of sessions a tick
+    runs: the 1000-session pool of the serving workload (64 with --quick),
+    settled for `settle_frames` frames, then ticks of k = 1, 3, 10, 40, 200,
+    1000 sessions (random, one frame each), median host-timed tick over
+    `reps` ticks after 5 unrecorded. With `capture` = k, one tick of k
+    sessions is bracketed by cudaProfilerStart/Stop for
+    `ncu --profile-from-start off` instead."""
+    import torch
+
+    import vsim.scenes as sc
+    from vsim.server import Server
+
+    count = 64 if quick else 1000
+    bodies, tank = sc.session_pool(count, seed=3)
+    server = Server(bodies, tank, budget_bytes=150e9)
+    n = server.admitted
+    for s in range(n):
+        server.submit(s, settle_frames)
+    while server.stats()["pending"]:
+        server.tick()
+        server.poll()
+    rng = np.random.default_rng(1)
+    if capture is not None:
+        for _ in range(3):
+            for s in rng.choice(n, capture, replace=False):
+                server.submit(int(s), 1)
+            server.tick()
+            server.poll()
+        for s in rng.choice(n, capture, replace=False):
+            server.submit(int(s), 1)
+        torch.cuda.profiler.start()
+        server.tick()
+        torch.cuda.profiler.stop()
+        server.poll()
+        return {"captured_tick_sessions": capture}
+    out = {}
+    for k in (1, 3, 10, 40, 200, 1000):
+        k = min(k, n)
+        ts = []
+        for rep in range(reps + 5):
+            for s in rng.choice(n, k, replace=False):
+                server.submit(int(s), 1)
+            t = time.perf_counter()
+            server.tick()
+            ts.append(time.perf_counter() - t)
+            server.poll()
+        out[str(k)] = round(statistics.median(ts[5:]) * 1e3, 3)
+    server.destroy()
+    return {"workload": f"{n} sessions resident, settled {settle_frames} frames; ticks of k sessions, one frame each",
+            "tick_ms_by_sessions": out}
+
+
 def drift(frames: int = 300):
     """The 16 x 4 x 4 bar for `frames` frames on the GPU against the oracle
     in double precision from the same start: the float trajectory's
@@ -607,6 +660,9 @@ def main():
     ap.add_argument("--no-cloud", action="store_true")
     ap.add_argument("--stress-only", action="store_true", help="only the stress workload's frames (for captures)")
     ap.add_argument("--cloud-only", action="store_true", help="only the cloud voxeliser section (for captures)")
+    ap.add_argument("--tick-sweep", action="store_true", help="only the server's tick time against sessions per tick")
+    ap.add_argument("--capture-tick", type=int, default=None, metavar="K",
+                    help="profiler capture mode: one server tick of K sessions, for `ncu --profile-from-start off`")
     ap.add_argument("--capture-after", type=int, default=None, metavar="N",
                     help="profiler capture mode: run N frames of the bench workload, then bracket one more frame "
                          "(or --capture-substeps substeps) with cudaProfilerStart/Stop for "
@@ -653,6 +709,9 @@ def main():
         return
     if args.cloud_only:
         print(json.dumps({"cloud_voxelize": cloud_voxelize(args.quick)}))
+        return
+    if args.tick_sweep or args.capture_tick is not None:
+        print(json.dumps({"tick_sweep": tick_sweep(args.quick, args.capture_tick)}))
         return
     if args.capture_after is not None:
         sim = Simulator(scene)

@@ -5,7 +5,6 @@ import ctypes as C
 import math
 
 import numpy as np
-import pytest
 
 
 def test_exports_every_header_symbol(vsimlib):

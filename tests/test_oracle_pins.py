@@ -10,7 +10,6 @@ import ctypes as C
 import math
 
 import numpy as np
-import pytest
 
 H = 0.03125                 # elastic.test.js:190
 DT = 1 / (60 * 20)          # elastic.test.js:193

@@ -330,6 +330,24 @@ def batched_vs_plain(frames: int, quick: bool):
     return out
 
 
+def single_body_pass(quick: bool, hbm: float):
+    """The colour pass of one large body alone: the stress workload's 192^3
+    noise blob without the sheet (48^3 with --quick), timed as
+    colour_pass_rate times it."""
+    import vsim.scenes as sc
+    from vsim import Simulator
+
+    scene = sc.noise_blob(n=48 if quick else 192, seed=4, splats=0)
+    sim = Simulator(scene)
+    per_launch, per_launch_s = colour_pass_rate(sim)
+    achieved = per_launch / per_launch_s / 1e9
+    out = {"workload": f"noise blob {scene.bodies[0].cell_dims[0]}^3 alone, {scene.cells} cells",
+           "achieved_gbs": round(achieved, 1), "frac_of_measured_hbm": round(achieved / hbm, 4),
+           "bytes_per_launch": round(per_launch), "avg_launch_us": round(per_launch_s * 1e6, 2)}
+    sim.destroy()
+    return out
+
+
 def stress(quick: bool, hbm: float, frames: int = 3):
     """The stress workload: a 192^3 noise blob with a 192 x 192 x 2 sheet above it
     (E 5e5, nu 0.48), ground, self and body contact, 20 substeps of 2
@@ -364,6 +382,7 @@ def stress(quick: bool, hbm: float, frames: int = 3):
                             "bytes_per_launch": round(per_launch), "avg_launch_us": round(per_launch_s * 1e6, 2),
                             "isolated_launch_us": round(1e3 * ms / launches, 2),
                             "method": "10 sweeps x 8 colour passes back to back in one graph"},
+           "single_body_elastic_pass": single_body_pass(quick, hbm),
            "splat_deform_gbs": round(92 * n_splats / (splat_ms / 1e3) / 1e9, 1) if splat_ms else None,
            "sort_keys_per_s": round(n_splats / (sort_ms / 1e3)) if sort_ms else None,
            "kernel_groups_one_frame": {k: {"ms": round(v[0], 3), "launches": v[1]} for k, v in prof.items()},

@@ -707,7 +707,9 @@ __device__ __forceinline__ bool admitted(uint4 a, uint4 b, uint32_t selfContact)
 //   concatenated in the reference's order (buckets dz, dy, dx; entries in
 //   bucket order) -- are dealt to the lanes 32 at a time: lane q < 27 sizes
 //   neighbour bucket q, a warp scan turns the sizes into offsets, and each
-//   lane finds its candidate's run by binary search. The record's chain of
+//   lane finds its candidate's run as the last one starting at or before it
+//   (a ballot of the runs starting in the round, the run carried over from
+//   the round before). The record's chain of
 //   dependent candidate loads is spread over 32 lanes, which is what a
 //   launch too small to fill the GPU needs;
 // - many records: one thread per record, scanning the runs itself, which

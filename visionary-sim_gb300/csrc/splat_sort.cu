@@ -180,6 +180,8 @@ size_t radixSortTempBytes(uint32_t n) { return sortTempBytes(n); }
 __global__ void __launch_bounds__(kSortThreads) sortHistKernel(const uint32_t* __restrict__ keys, uint32_t n,
                                                                uint32_t shift, uint32_t mask, uint32_t tiles,
                                                                uint32_t* __restrict__ hist) {
+    pdlWait();  // the keys and counts come from the kernel before
+    pdlLaunchNext();
     __shared__ uint32_t bins[256];
     bins[threadIdx.x] = 0;
     __syncthreads();
@@ -226,6 +228,8 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
 // Scan, level 1: each block sums its chunk.
 __global__ void __launch_bounds__(kSortThreads) scanReduceKernel(const uint32_t* __restrict__ in, uint32_t n,
                                                                  uint32_t* __restrict__ partial) {
+    pdlWait();  // the keys and counts come from the kernel before
+    pdlLaunchNext();
     __shared__ uint32_t warpSums[kWarps + 1];
     const uint32_t base = blockIdx.x * kScanChunk;
     uint32_t sum = 0;
@@ -240,6 +244,8 @@ __global__ void __launch_bounds__(kSortThreads) scanReduceKernel(const uint32_t*
 
 // Scan, level 2: one block scans the chunk sums (at most kScanMaxChunks).
 __global__ void __launch_bounds__(kSortThreads) scanPartialKernel(uint32_t* __restrict__ partial, uint32_t chunks) {
+    pdlWait();  // the keys and counts come from the kernel before
+    pdlLaunchNext();
     __shared__ uint32_t warpSums[kWarps + 1];
     constexpr uint32_t per = kScanMaxChunks / kSortThreads;
     uint32_t v[per];
@@ -263,6 +269,8 @@ __global__ void __launch_bounds__(kSortThreads) scanPartialKernel(uint32_t* __re
 // Scan, level 3: each block scans its chunk from its offset, in place.
 __global__ void __launch_bounds__(kSortThreads) scanDownKernel(uint32_t* __restrict__ data, uint32_t n,
                                                                const uint32_t* __restrict__ partial) {
+    pdlWait();  // the keys and counts come from the kernel before
+    pdlLaunchNext();
     __shared__ uint32_t warpSums[kWarps + 1];
     constexpr uint32_t per = kScanChunk / kSortThreads;
     const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * per;
@@ -288,6 +296,8 @@ __global__ void __launch_bounds__(kSortThreads) sortScatterKernel(const uint32_t
                                                                   const uint32_t* __restrict__ offsets,
                                                                   uint32_t* __restrict__ keysOut,
                                                                   uint32_t* __restrict__ valsOut) {
+    pdlWait();  // the keys and counts come from the kernel before
+    pdlLaunchNext();
     __shared__ uint32_t sKeys[kSortTile];
     __shared__ uint32_t sVals[kSortTile];
     __shared__ uint32_t warpHist[kWarps][256];
@@ -353,6 +363,24 @@ __global__ void __launch_bounds__(kSortThreads) sortScatterKernel(const uint32_t
     }
 }
 
+namespace {
+// A sort kernel launched with programmatic dependent launch: its blocks may
+// start while the kernel before finishes, and wait (pdlWait) before reading.
+template <class... KArgs, class... Args>
+void pdl(void (*kernel)(KArgs...), uint32_t grid, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kSortThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+}  // namespace
+
 cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint32_t keyBits, void* temp,
                          size_t tempBytes, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
@@ -379,11 +407,11 @@ cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint
         const bool last = pass + 1 == passes;
         uint32_t* kout = last ? nullptr : (pass % 2 == 0 ? keysA : keysB);
         uint32_t* vout = last ? order : (pass % 2 == 0 ? valsA : valsB);
-        sortHistKernel<<<tiles, kSortThreads, 0, st>>>(kin, n, shift, mask, tiles, hist);
-        scanReduceKernel<<<chunks, kSortThreads, 0, st>>>(hist, histCount, partial);
-        scanPartialKernel<<<1, kSortThreads, 0, st>>>(partial, chunks);
-        scanDownKernel<<<chunks, kSortThreads, 0, st>>>(hist, histCount, partial);
-        sortScatterKernel<<<tiles, kSortThreads, 0, st>>>(kin, vin, n, shift, mask, tiles, hist, kout, vout);
+        pdl(sortHistKernel, tiles, st, kin, n, shift, mask, tiles, hist);
+        pdl(scanReduceKernel, chunks, st, (const uint32_t*)hist, histCount, partial);
+        pdl(scanPartialKernel, 1u, st, partial, chunks);
+        pdl(scanDownKernel, chunks, st, hist, histCount, (const uint32_t*)partial);
+        pdl(sortScatterKernel, tiles, st, kin, vin, n, shift, mask, tiles, (const uint32_t*)hist, kout, vout);
         kin = kout;
         vin = vout;
     }

@@ -84,9 +84,14 @@ __global__ void __launch_bounds__(256) splatDeformKernel(const float4* __restric
                                                          float4* __restrict__ axesScale) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    // The splat's embedding, scale and rotation do not change between
+    // frames: loaded before waiting for the frame that moves the nodes.
     const float4 e = embed[i];
     const float4 sb = scaleBody[i];
+    const float4 q4 = quat[i];
     const SplatBody B = bodies[__float_as_uint(sb.w)];
+    pdlWait();
+    pdlLaunchNext();
     const uint32_t node0 = __float_as_uint(e.w);
     const float local[3] = {e.x, e.y, e.z};
     const float inv = B.inv;
@@ -107,7 +112,6 @@ __global__ void __launch_bounds__(256) splatDeformKernel(const float4* __restric
         col2 = col2 + p * g.z;
     }
     const M F{{col0, col1, col2}};
-    const float4 q4 = quat[i];
     const float x = q4.x, y = q4.y, z = q4.z, w = q4.w;
     const V r0 = mk(1.0f - 2.0f * (y * y + z * z), 2.0f * (x * y + z * w), 2.0f * (x * z - y * w));
     const V r1 = mk(2.0f * (x * y - z * w), 1.0f - 2.0f * (x * x + z * z), 2.0f * (y * z + x * w));
@@ -139,15 +143,24 @@ __global__ void __launch_bounds__(256) splatDeformKernel(const float4* __restric
 cudaError_t launchSplatDeform(cudaStream_t st, const SplatState& s, const float4* pos, uint32_t n, float vx, float vy,
                               float vz, bool axes) {
     if (n == 0) return cudaSuccess;
+    // Programmatic dependent launch: the constant loads above overlap the
+    // tail of the frame's last kernel.
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((n + 255) / 256);
+    cfg.blockDim = dim3(256);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
     if (axes)
-        splatDeformKernel<true><<<(n + 255) / 256, 256, 0, st>>>(s.embed, s.quat, s.scaleBody, s.bodies, pos, n, vx,
-                                                                 vy, vz, s.meanDepth, s.cov, s.keys, s.order,
-                                                                 s.axesRotation, s.axesScale);
-    else
-        splatDeformKernel<false><<<(n + 255) / 256, 256, 0, st>>>(s.embed, s.quat, s.scaleBody, s.bodies, pos, n, vx,
-                                                                  vy, vz, s.meanDepth, s.cov, s.keys, s.order,
-                                                                  nullptr, nullptr);
-    return cudaGetLastError();
+        return cudaLaunchKernelEx(&cfg, splatDeformKernel<true>, (const float4*)s.embed, (const float4*)s.quat,
+                                  (const float4*)s.scaleBody, (const SplatBody*)s.bodies, pos, n, vx, vy, vz,
+                                  s.meanDepth, s.cov, s.keys, s.order, s.axesRotation, s.axesScale);
+    return cudaLaunchKernelEx(&cfg, splatDeformKernel<false>, (const float4*)s.embed, (const float4*)s.quat,
+                              (const float4*)s.scaleBody, (const SplatBody*)s.bodies, pos, n, vx, vy, vz, s.meanDepth,
+                              s.cov, s.keys, s.order, (float4*)nullptr, (float4*)nullptr);
 }
 
 // --------------------------------------------------------- radix sort --

@@ -590,3 +590,44 @@ def test_gravity_and_contact_switched_midrun(lib):
                 sim.dispatch(scene.substeps)
                 orc.dispatch(scene.substeps)
                 assert_same(sim, orc, scene, f"{what} {frame}")
+
+
+@pytest.mark.parametrize("law", ["hard", "compliant"])
+def test_grab_respects_static_material(lib, law):
+    """staticPrescription.test.js:104-149 on the device: a sphere (radius
+    0.04 m, 0.02 m cells) whose z < 0 half is static. A ray along +z from
+    z = -0.2 grabs past the static material (the anchor has z >= 0) and
+    holds several nodes within the grip radius; a single-node grip holds
+    one; frames under the drag leave every static node where it rests; a
+    body that is static everywhere is missed."""
+    import vsim.scenes as sc
+    from vsim import Simulator
+    from vsim import voxelize as vz
+
+    grid = vz.voxelize_sdf(vz.sphere(0.04), 0.02)
+    base = sc.Body(tuple(grid.dims), tuple(grid.origin), grid.h, grid.occupancy)
+    tank = ((-0.2, -0.2, -0.2), (0.2, 0.2, 0.2))
+    body = sc.with_static_region(base, lambda x, y, z: z < 0)
+    assert 0 < body.static_nodes.size < body.node_count
+    sim = Simulator(sc.Scene([body], tank, contact=False))
+    sim.set_drive_law(law)
+    rest = sim.read_positions()
+    hit = sim.grab((0.0, 0.0, -0.2), (0.0, 0.0, 1.0))
+    assert hit is not None and hit["held"] > 1 and hit["position"][2] >= 0
+    statics = body.static_nodes.astype(np.int64)
+    near = np.linalg.norm(rest[statics, :3] - np.asarray(hit["position"], np.float32), axis=1)
+    assert np.any((sim.inv_mass[statics] > 0) & (near < sim.grip["radius"]))  # static material was within reach
+    for _ in range(3):
+        sim.move_grab(np.asarray(hit["position"]) + [0.0, 0.01, 0.0])
+        sim.dispatch(10)
+    assert np.array_equal(sim.read_positions()[statics], rest[statics])
+    sim.release_grab()
+    sim.set_grip("singleNode")
+    assert sim.grab((0.0, 0.0, -0.2), (0.0, 0.0, 1.0))["held"] == 1
+    sim.destroy()
+
+    pinned = sc.with_static_region(base, lambda x, y, z: True)
+    sim = Simulator(sc.Scene([pinned], tank, contact=False))
+    sim.set_drive_law(law)
+    assert sim.grab((0.0, 0.0, -0.2), (0.0, 0.0, 1.0)) is None
+    sim.destroy()

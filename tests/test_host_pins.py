@@ -443,3 +443,28 @@ def test_captured_cloud_scene_centres_in_cells():
     lowest = min(p[1] for p in means.tolist())
     assert lowest > scene.tank[0][1]
     assert 1.0 < body.cell_count * body.h ** 3 / (4 / 3 * math.pi * 0.06 ** 3) < 1.8
+
+
+# ---- staticPrescription.test.js ---------------------------------------------------
+
+def test_static_region_classifies_positions():
+    # staticPrescription.test.js:11-22
+    from vsim import scenes as sc
+
+    positions = np.array([-1, 2, 3, 1, 2, 3, -1, 3, 3, -2, 1, 3], np.float32)
+    region = lambda x, y, z: x < 0 and y <= 2 and z == 3  # noqa: E731
+    assert sc.static_nodes_in_region(positions, region).tolist() == [0, 3]
+    assert sc.static_nodes_in_region(positions).tolist() == []
+    assert sc.static_nodes_in_region(positions, lambda x, y, z: True).tolist() == [0, 1, 2, 3]
+    assert sc.static_nodes_in_region(np.zeros(0, np.float32), region).tolist() == []
+
+
+def test_rest_positions_are_the_lattice_nodes():
+    # lattice.js:171-179: float32 of origin + index * h, x fastest
+    from vsim import scenes as sc
+
+    body = sc.Body((2, 1, 1), (0.1, -0.2, 0.3), 0.016, np.ones(2, np.uint8))
+    rest = sc.rest_positions(body)
+    assert rest.dtype == np.float32 and rest.shape == (12, 3)
+    assert rest[1].tolist() == [np.float32(0.1 + 0.016), np.float32(-0.2), np.float32(0.3)]
+    assert rest[11].tolist() == [np.float32(0.1 + 2 * 0.016), np.float32(-0.2 + 0.016), np.float32(0.3 + 0.016)]

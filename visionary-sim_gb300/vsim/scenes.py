@@ -99,6 +99,33 @@ class Descs:
         self.tank.max[:] = [float(v) for v in scene.tank[1]]
 
 
+def rest_positions(body: Body) -> np.ndarray:
+    """lattice.js:171-179: every node's rest position, float32 (origin + (i,
+    j, k) h in double, stored as the reference's Float32Array), (n, 3) in
+    node order."""
+    nx, ny, nz = body.node_dims
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    ijk = np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1).astype(np.float64)
+    return (np.asarray(body.origin, np.float64) + ijk * body.h).astype(np.float32)
+
+
+def static_nodes_in_region(positions, region=None) -> np.ndarray:
+    """staticPrescription.js:9-20: the nodes whose rest position (x, y, z,
+    float32 values) the body's declaration `region(x, y, z)` accepts, in
+    node order, inactive nodes included; none without a declaration."""
+    if region is None:
+        return np.zeros(0, np.uint32)
+    p = np.asarray(positions, np.float32).reshape(-1, 3).astype(np.float64)
+    return np.asarray([n for n in range(len(p)) if region(p[n, 0], p[n, 1], p[n, 2])], np.uint32)
+
+
+def with_static_region(body: Body, region) -> Body:
+    """The body with its static nodes sampled from a declaration on its rest
+    positions (simulator.js:64)."""
+    return Body(body.cell_dims, body.origin, body.h, body.occupancy, dict(body.material),
+                static_nodes_in_region(rest_positions(body), region))
+
+
 def node_index(dims, i, j, k):
     nx, ny, _ = dims
     return i + nx * (j + ny * k)

@@ -631,3 +631,85 @@ def test_grab_respects_static_material(lib, law):
     sim.set_drive_law(law)
     assert sim.grab((0.0, 0.0, -0.2), (0.0, 0.0, 1.0)) is None
     sim.destroy()
+
+
+def test_simulator_timing(lib):
+    """simulatorTiming.test.js:23-150 through vsim_step and the stats, on the
+    pinned bar with a 0.002 s step: render dt becomes a count of fixed
+    steps with the remainder banked; paused frames bank nothing; a
+    requested step runs once, paused or not, and a running frame's time
+    stays banked; a scene with no bodies does no timing work; reset clears
+    the clock; garbage dt is no time; a material change shortens only
+    future steps and keeps the backlog."""
+    import vsim.scenes as sc
+    from vsim import Simulator
+
+    def fresh(step=0.002):
+        scene = sc.single_box()
+        scene.step_duration = None
+        sim = Simulator(scene)
+        if step:
+            sim.set_step_duration(step)
+        return sim
+
+    sim = fresh()
+    sim.step(0.005)
+    st = sim.stats()
+    assert st["last_steps"] == 2 and abs(st["backlog_time"] - 0.001) < 1e-12
+    sim.step(0.001)
+    st = sim.stats()
+    assert st["last_steps"] == 1 and st["steps"] == 3
+
+    sim = fresh()
+    sim.paused = True
+    sim.step(10)
+    st = sim.stats()
+    assert st["steps"] == 0 and st["backlog_time"] == 0 and st["dropped_time"] == 0
+    sim.request_step()
+    sim.step(10)
+    st = sim.stats()
+    assert st["steps"] == 1 and abs(st["simulated_time"] - 0.002) < 1e-12 and st["dropped_time"] == 0
+    sim.step(10)
+    assert sim.stats()["steps"] == 1  # the request was used up
+
+    empty = Simulator(sc.Scene([], ((-1.0, 0.0, -1.0), (1.0, 1.0, 1.0))))
+    empty.request_step()
+    empty.step(1)
+    assert empty.stats()["steps"] == 0 and empty.stats()["simulated_time"] == 0
+    empty.destroy()
+
+    sim = fresh()
+    sim.step(0.2)
+    sim.request_step()
+    sim.reset()
+    st = sim.stats()
+    assert st["steps"] == 0 and st["simulated_time"] == 0 and st["backlog_time"] == 0 and st["dropped_time"] == 0
+    sim.step(0.001)
+    assert sim.stats()["steps"] == 0  # no request survived the reset
+
+    sim = fresh()
+    sim.request_step()
+    sim.step(0.0005)
+    st = sim.stats()
+    assert st["last_steps"] == 1 and abs(st["backlog_time"] - 0.0005) < 1e-12 and st["dropped_time"] == 0
+
+    sim = fresh()
+    sim.request_step()
+    sim.step(0.003)
+    st = sim.stats()
+    assert st["last_steps"] == 1 and abs(st["backlog_time"] - 0.001) < 1e-12
+
+    sim = fresh()
+    for dt in (-1.0, float("nan"), float("inf")):
+        sim.step(dt)
+    st = sim.stats()
+    assert st["backlog_time"] == 0 and st["steps"] == 0
+
+    sim = fresh(step=None)  # the CFL rule sets the step
+    sim.set_material(0, {"youngs_modulus": 2e3, "density": 700.0})
+    before = sim.stats()["step_duration"]
+    sim.step(before / 2)
+    backlog = sim.stats()["backlog_time"]
+    sim.set_material(0, {"youngs_modulus": 1e5})
+    st = sim.stats()
+    assert st["step_duration"] < before and st["backlog_time"] == backlog

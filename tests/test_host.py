@@ -171,3 +171,44 @@ def test_scene_generators():
     assert scales.min() >= 1e-3 * 0.999 and scales.max() <= 1e-2 * 1.001
     lo = np.asarray(s0.bodies[0].origin)
     assert np.all(means >= lo - 1e-6) and np.all(means <= lo + np.array([16, 4, 4]) * sc.H + 1e-6)
+
+
+# ---- material.test.js ----------------------------------------------------------------
+
+def _lame(vsimlib, youngs, nu, density=1000.0):
+    m = vsimlib.Material(youngs, nu, density, 0.4, 0.6, 0.012, 0.0)
+    mu, lam = C.c_double(), C.c_double()
+    assert vsimlib.lib().vsim_lame_parameters(C.byref(m), C.byref(mu), C.byref(lam)) == 0
+    return mu.value, lam.value
+
+
+def _engineering(mu, lam):
+    """The inverse of the Lame conversion: E and nu."""
+    return mu * (3 * lam + 2 * mu) / (lam + mu), lam / (2 * (lam + mu))
+
+
+def test_material_round_trips_through_lame(vsimlib):
+    # material.test.js:19-28
+    for youngs in (1e4, 1.2e5, 5e6):
+        for nu in (0.25, 0.3, 0.35, 0.4, 0.45, 0.49):
+            e, n = _engineering(*_lame(vsimlib, youngs, nu))
+            assert abs(e - youngs) < 0.05 and abs(n - nu) < 5e-9
+
+
+def test_material_clamps_poisson_ratio(vsimlib):
+    # material.test.js:30-43: finite, lambda > 0, nu back inside [0.25, 0.49]
+    for nu in (-1.0, 0.0, 0.5, 0.99):
+        mu, lam = _lame(vsimlib, 1e5, nu)
+        assert math.isfinite(mu) and math.isfinite(lam) and lam > 0
+        _, back = _engineering(mu, lam)
+        assert 0.25 - 1e-9 <= back <= 0.49 + 1e-9
+
+
+def test_material_wave_speed(vsimlib):
+    # material.test.js:46-59
+    def speed(youngs, density, nu=0.4):
+        return vsimlib.lib().vsim_wave_speed(C.byref(vsimlib.Material(youngs, nu, density, 0.4, 0.6, 0.012, 0.0)))
+
+    assert speed(1e7, 1000.0) > speed(1e5, 1000.0)
+    assert speed(1e5, 4000.0) < speed(1e5, 1000.0)
+    assert 5 < speed(1e5, 1000.0, 0.35) < 30

@@ -713,3 +713,55 @@ def test_simulator_timing(lib):
     sim.set_material(0, {"youngs_modulus": 1e5})
     st = sim.stats()
     assert st["step_duration"] < before and st["backlog_time"] == backlog
+
+
+def test_lattice_masses_follow_density(lib):
+    """discretize.test.js:59-140 through the library: a sphere (radius
+    0.05 m, 0.1/8 m cells) whose lumped node masses sum to density x volume;
+    a density change doubles them and leaves material-less nodes inert; a
+    chain of density edits comes back to the original masses; every kind of
+    rest geometry (shape, mesh, cloud) becomes a body with material."""
+    import vsim.scenes as sc
+    from vsim import Simulator
+    from vsim import voxelize as vz
+    from vsim._ffi import fptr
+
+    def inverse_masses(sim):
+        out = np.zeros(sim.node_count, np.float32)
+        assert lib.lib().vsim_read_inv_mass(sim.handle, fptr(out), sim.node_count) == 0
+        return out
+
+    def lumped(inv):
+        live = inv[inv > 0].astype(np.float64)
+        return float(np.sum(1.0 / live))
+
+    grid = vz.voxelize_sdf(vz.sphere(0.05), 0.1 / 8)
+    body = sc.Body(tuple(grid.dims), tuple(grid.origin), grid.h, grid.occupancy,
+                   dict(sc.DEFAULT_MATERIAL, density=1000.0))
+    tank = ((-1.0, -1.0, -1.0), (1.0, 1.0, 1.0))
+    sim = Simulator(sc.Scene([body], tank, contact=False))
+    volume = body.cell_count * grid.h ** 3
+    first = inverse_masses(sim)
+    assert abs(lumped(first) - 1000.0 * volume) < 1e-5 * 1000.0 * volume
+    inert = int(np.count_nonzero(first == 0))
+    sim.set_material(0, {"density": 2000.0})
+    doubled = inverse_masses(sim)
+    assert abs(lumped(doubled) - 2000.0 * volume) < 1e-5 * 2000.0 * volume
+    assert int(np.count_nonzero(doubled == 0)) == inert
+    for density in (1500.0, 700.0, 2400.0, 1000.0):
+        sim.set_material(0, {"density": density})
+    assert np.all(np.abs(inverse_masses(sim) - first) < 5e-4)
+    sim.destroy()
+
+    cube = vz.box([0.04, 0.04, 0.04])
+    corners = [[x, y, z] for x in (-0.04, 0.04) for y in (-0.04, 0.04) for z in (-0.04, 0.04)]
+    mesh = vz.Mesh(np.asarray(corners, np.float32), np.asarray(
+        [[0, 1, 3], [0, 3, 2], [4, 6, 7], [4, 7, 5], [0, 4, 5], [0, 5, 1], [2, 3, 7], [2, 7, 6],
+         [0, 2, 6], [0, 6, 4], [1, 5, 7], [1, 7, 3]], np.uint32))
+    cloud = sc.capture_cloud(3000, 0.04, seed=2)
+    for kind, source in (("shape", cube), ("mesh", mesh), ("cloud", cloud)):
+        g = vz.voxelize_source(kind, source, 0.01)
+        b = sc.Body(tuple(g.dims), tuple(g.origin), g.h, g.occupancy)
+        s = Simulator(sc.Scene([b], tank, contact=False))
+        assert s.stats()["cells"] > 0 and lumped(inverse_masses(s)) > 0, kind
+        s.destroy()

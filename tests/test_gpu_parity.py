@@ -765,3 +765,47 @@ def test_lattice_masses_follow_density(lib):
         s = Simulator(sc.Scene([b], tank, contact=False))
         assert s.stats()["cells"] > 0 and lumped(inverse_masses(s)) > 0, kind
         s.destroy()
+
+
+@pytest.mark.parametrize("shape", ["sphere", "box"])
+def test_lattice_proxy_contract(lib, shape):
+    """proxyGeometry.test.js:150-338 for the lattice the library builds, on
+    its shapes (a 0.05 m sphere, a 0.04 x 0.02 x 0.03 m box, 0.015 m cells):
+    finite, non-negative inverse masses with material on some nodes; every
+    contact node carries material and the surface is listed in ascending
+    node order; the material nodes' nearest-neighbour distance is the cell
+    edge; a positive stability number; a fourfold density divides every
+    inverse mass by four and gives no empty node material."""
+    import vsim.scenes as sc
+    from vsim import Simulator
+    from vsim import voxelize as vz
+    from vsim._ffi import fptr
+
+    source = vz.sphere(0.05) if shape == "sphere" else vz.box([0.04, 0.02, 0.03])
+    grid = vz.voxelize_sdf(source, 0.015)
+    body = sc.Body(tuple(grid.dims), tuple(grid.origin), grid.h, grid.occupancy,
+                   dict(sc.DEFAULT_MATERIAL, density=1000.0))
+    sim = Simulator(sc.Scene([body], ((-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)), contact=True))
+
+    def inverse_masses():
+        out = np.zeros(sim.node_count, np.float32)
+        assert lib.lib().vsim_read_inv_mass(sim.handle, fptr(out), sim.node_count) == 0
+        return out
+
+    inv = inverse_masses()
+    assert np.all(np.isfinite(inv)) and np.all(inv >= 0) and np.count_nonzero(inv) > 0
+    nodes, bodies = sim.contact_surface()
+    assert nodes.size > 0 and np.all(bodies == 0) and np.all(nodes < sim.node_count)
+    assert np.all(np.diff(nodes.astype(np.int64)) > 0)
+    assert np.all(inv[nodes] > 0)
+    rest = sc.rest_positions(body).astype(np.float64)[inv > 0]
+    d = np.linalg.norm(rest[:, None, :] - rest[None, :, :], axis=2)
+    np.fill_diagonal(d, np.inf)
+    nearest = d.min(axis=1)
+    assert abs(nearest.min() - grid.h) <= 1e-5 * grid.h and abs(nearest.max() - grid.h) <= 1e-5 * grid.h
+    assert sim.cfl_number() > 0 and np.isfinite(sim.cfl_number())
+    sim.set_material(0, {"density": 4000.0})
+    after = inverse_masses()
+    assert np.all(after[inv == 0] == 0)
+    assert np.all(np.abs(after[inv > 0] - inv[inv > 0] / 4) <= 1e-6 * inv[inv > 0])
+    sim.destroy()

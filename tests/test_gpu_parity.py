@@ -809,3 +809,30 @@ def test_lattice_proxy_contract(lib, shape):
     assert np.all(after[inv == 0] == 0)
     assert np.all(np.abs(after[inv > 0] - inv[inv > 0] / 4) <= 1e-6 * inv[inv > 0])
     sim.destroy()
+
+
+@pytest.mark.parametrize("mapping", ["warp", "thread"])
+def test_contact_bucket_overflow(lib, mapping):
+    """Buckets holding more records than their 32 visible slots
+    (contacts.wgsl:75; sort.wgsl:27-40 keeps the 32 lowest record indices):
+    a blob squeezed to a fifth of its size about its centre puts up to ~80
+    surface records in one bucket and ~65 buckets over capacity. The pair
+    set and the frames equal the oracle's under both gather mappings."""
+    import pyoracle
+    import vsim.scenes as sc
+
+    scene = sc.noise_blob(n=20, seed=5, splats=0)
+    sim, orc = make(scene)
+    sim.set_gather_mapping(mapping)
+    pos, prev, vel = orc.state()
+    live = orc.inv_mass() > 0
+    centre = pos[live, :3].mean(axis=0)
+    squeezed = pos.copy()
+    squeezed[:, :3] = centre + (squeezed[:, :3] - centre) * 0.2
+    sim.write_state(squeezed, squeezed, np.zeros_like(vel))
+    orc.set_state(squeezed, squeezed, np.zeros_like(vel))
+    assert np.array_equal(sim.contact_pairs(), orc.contact_pairs())
+    for frame in range(3):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"{mapping} frame {frame}")

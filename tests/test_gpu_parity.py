@@ -836,3 +836,27 @@ def test_contact_bucket_overflow(lib, mapping):
         sim.dispatch(scene.substeps)
         orc.dispatch(scene.substeps)
         assert_same(sim, orc, scene, f"{mapping} frame {frame}")
+
+
+def test_splats_on_many_bodies(lib):
+    """Splats bound to several bodies of uneven sizes (each body's splats
+    embedded in its own lattice, concatenated in body order): after two
+    frames their means and covariances equal the oracle's body by body, and
+    the depth order over all of them equals a stable sort of the oracle's
+    keys."""
+    import pyoracle
+    import vsim.scenes as sc
+
+    scene = sc.box_batch(6, seed=3, splats_per_body=700)
+    sim, orc = make(scene)
+    for frame in range(2):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+    view = (0.2, -0.5, -0.84)
+    sim.deform_splats(view)
+    sim.sort_splats()
+    means, cov, order = sim.read_splats()
+    parts = [orc.splat_deform(b, *scene.splats[b][:3], view) for b in sorted(scene.splats)]
+    assert np.array_equal(means, np.concatenate([p[0] for p in parts]))
+    assert np.array_equal(cov, np.concatenate([p[1] for p in parts]))
+    assert np.array_equal(order, pyoracle.stable_sort(np.concatenate([p[2] for p in parts])))

@@ -860,3 +860,31 @@ def test_splats_on_many_bodies(lib):
     assert np.array_equal(means, np.concatenate([p[0] for p in parts]))
     assert np.array_equal(cov, np.concatenate([p[1] for p in parts]))
     assert np.array_equal(order, pyoracle.stable_sort(np.concatenate([p[2] for p in parts])))
+
+
+def test_reset_releases_the_grab(lib):
+    """reset() lets the grab go and returns every node to rest
+    (simulator.js:495-500 calls releaseGrab): after a dragged frame and a
+    reset, frames equal a fresh oracle's, with no node held."""
+    import pyoracle
+    import vsim.scenes as sc
+
+    scene = sc.single_box()
+    sim, _ = make(scene)
+    rest = sim.read_positions()
+    dims = scene.bodies[0].node_dims
+    tip = [sc.node_index(dims, 16, j, k) for j in range(5) for k in range(5)]
+    offsets = (rest[tip, :3] - rest[tip[0], :3]).astype(np.float32)
+    sim.hold(tip, offsets)
+    sim.place_grab(rest[tip[0], :3].astype(np.float64))
+    sim.move_grab(rest[tip[0], :3].astype(np.float64) + [0.0, 0.05, 0.0])
+    sim.dispatch(scene.substeps)
+    assert not np.array_equal(sim.read_positions(), rest)
+    sim.reset()
+    assert np.array_equal(sim.read_positions(), rest)
+    assert sim.stats()["driven"] == 0
+    orc = pyoracle.Oracle(scene, 32)
+    for frame in range(3):
+        sim.dispatch(scene.substeps)
+        orc.dispatch(scene.substeps)
+        assert_same(sim, orc, scene, f"after reset, frame {frame}")

@@ -31,9 +31,11 @@ struct DeviceState {
     uint32_t* start = nullptr;    // per bucket
     uint32_t* cursor = nullptr;
     float4* delta = nullptr;
-    uint4* sMeta = nullptr;       // visible bucket entries in bucket order: their records
-    float4* sPos = nullptr;       //   ... and their nodes' positions
-    uint32_t* sRec = nullptr;     //   ... and their record indices
+    uint4* sMeta = nullptr;       // every bucket entry in bucket order (visible prefix first): its record
+    float4* sPos = nullptr;       //   ... its node's position
+    float4* sMoved = nullptr;     //   ... its motion over the substep, its body's friction
+    uint32_t* sRec = nullptr;     //   ... its record index
+    uint32_t* sKey = nullptr;     //   ... its bucket
     // drive
     uint32_t* driven = nullptr;
     float4* drivenOffset = nullptr;

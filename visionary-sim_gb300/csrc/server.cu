@@ -137,7 +137,7 @@ double sessionBytes(const Lattice& L, const Grid& g) {
     const double nodes = L.nodeCount, surface = double(L.surface.size());
     return nodes * (3 * 16 + 4 * 4)            // pos, prev, vel; mass, active list, body, record
            + double(L.cellCount) * 16          // cell records
-           + surface * (16 + 4 + 4 + 4 + 16 + 16 + 16 + 4)  // record, key, rank, entry, correction, runs
+           + surface * (16 + 4 + 4 + 4 + 16 + 16 + 16 + 16 + 4 + 4)  // record, key, rank, entry, correction, runs
            + double(g.count()) * 8             // bucket counts and starts
            + sizeof(DevBody) + 2 * 16 + 4;     // constants, drag target, activity
 }

@@ -393,7 +393,7 @@ void freeSim(vsim_sim* s) {
     DeviceState& d = s->d;
     void* ptrs[] = {d.pos, d.prev, d.vel, d.baseW, d.active, d.activeBody, d.cells, d.bodies, d.fp,
                     d.surf, d.key, d.rank, d.entries, d.count, d.start, d.cursor, d.delta, d.driven,
-                    d.drivenOffset, d.nodeRecord, d.sMeta, d.sPos, d.sRec, d.bodyActive, d.grabs,
+                    d.drivenOffset, d.nodeRecord, d.sMeta, d.sPos, d.sMoved, d.sRec, d.sKey, d.bodyActive, d.grabs,
                     s->chunkDev, s->staging, s->pairs, s->pairCount, s->sp.embed, s->sp.quat,
                     s->sp.scaleBody, s->sp.bodies, s->sp.meanDepth, s->sp.cov, s->sp.keys, s->sp.order,
                     s->sp.sortTemp};
@@ -567,6 +567,8 @@ int createSim(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, v
     CK(allocN(&d.sMeta, s->surfaceCount), "allocate contact runs");
     CK(allocN(&d.sPos, s->surfaceCount), "allocate contact runs");
     CK(allocN(&d.sRec, s->surfaceCount), "allocate contact runs");
+    CK(allocN(&d.sKey, s->surfaceCount), "allocate contact runs");
+    CK(allocN(&d.sMoved, s->surfaceCount), "allocate contact runs");
     CK(allocN(&d.nodeRecord, N), "allocate node records");
     CK(allocN(&d.count, s->bucketTotal), "allocate contact grid");
     CK(allocN(&d.start, s->bucketTotal), "allocate contact grid");

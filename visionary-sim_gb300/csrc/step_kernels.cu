@@ -592,62 +592,53 @@ __global__ void scatterKernel(const FrameParams* __restrict__ fp, Work work, con
     });
 }
 
-// Buckets of at most this many entries are ordered in registers.
-constexpr uint32_t kSmallBucket = 8;
-
-// Ascending sort of eight keys: a 19-comparator network.
-__device__ __forceinline__ void sortSmall(uint32_t (&v)[kSmallBucket]) {
-    auto cx = [&](int a, int b) {
-        const uint32_t lo = min(v[a], v[b]), hi = max(v[a], v[b]);
-        v[a] = lo;
-        v[b] = hi;
-    };
-    cx(0, 2), cx(1, 3), cx(4, 6), cx(5, 7);
-    cx(0, 4), cx(1, 5), cx(2, 6), cx(3, 7);
-    cx(0, 1), cx(2, 3), cx(4, 5), cx(6, 7);
-    cx(2, 4), cx(3, 5);
-    cx(1, 4), cx(3, 6);
-    cx(1, 2), cx(3, 4), cx(5, 6);
-}
-
 // sort.wgsl:14-53: the bucket's visible entries -- its kBucketSlots lowest
-// record indices -- in ascending order at the front of its segment; then
-// their records and positions copied out in that order, so the gather reads
-// each neighbour bucket as one contiguous run.
+// record indices -- in ascending order at the front of its segment, the
+// rest after them; every entry's record, position, motion over the substep
+// (position - its substep start, as collide.wgsl:100-101 subtracts them)
+// with its body's friction, record index and bucket copied out in that
+// order, so the gather reads each neighbour bucket's visible entries as one
+// contiguous run and both a record's own data and a candidate's one load
+// deep.
+//
+// A bucket of at most kBucketSlots entries is all visible: each of its
+// records finds its own place (how many of the bucket's records have a lower
+// index) and copies itself there, all records at once. A larger bucket is
+// ordered by its first-arriving record alone, an insertion sort that keeps
+// the lowest kBucketSlots in front (rare: 32 surface nodes in one bucket of
+// edge h).
 __global__ void canonKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ key,
                             const uint32_t* __restrict__ rank, const uint32_t* __restrict__ start,
                             const uint32_t* __restrict__ count, uint32_t* __restrict__ entries,
-                            const uint4* __restrict__ surf, const float4* __restrict__ pos, uint4* __restrict__ sMeta,
-                            float4* __restrict__ sPos, uint32_t* __restrict__ sRec) {
+                            const uint4* __restrict__ surf, const float4* __restrict__ pos,
+                            const float4* __restrict__ prevState, const DevBody* __restrict__ bodies,
+                            uint4* __restrict__ sMeta, float4* __restrict__ sPos, float4* __restrict__ sMoved,
+                            uint32_t* __restrict__ sRec, uint32_t* __restrict__ sKey) {
     pdlWait();
     pdlLaunchNext();
     forEachItem(work, [&](uint32_t r) {
-        const uint32_t first = rank[r], b = key[r];
-        if (first != 0) return;
+        const uint32_t b = key[r];
+        if (b == kIdle) return;
         const uint32_t n = count[b];
         const uint32_t base = start[b];
         uint32_t* e = entries + base;
-        const uint32_t m = n < kBucketSlots ? n : kBucketSlots;
-        if (n <= kSmallBucket) {
-            // In registers: all loads of a step issued together.
-            uint32_t v[kSmallBucket];
-#pragma unroll
-            for (uint32_t k = 0; k < kSmallBucket; k++) v[k] = k < n ? e[k] : 0xffffffffu;
-            sortSmall(v);
-            uint4 rec[kSmallBucket];
-#pragma unroll
-            for (uint32_t k = 0; k < kSmallBucket; k++)
-                if (k < n) rec[k] = surf[v[k]];
-#pragma unroll
-            for (uint32_t k = 0; k < kSmallBucket; k++)
-                if (k < n) {
-                    e[k] = v[k];
-                    sMeta[base + k] = rec[k];
-                    sPos[base + k] = pos[rec[k].x];
-                    sRec[base + k] = v[k];
-                }
+        auto copyOut = [&](uint32_t at, uint32_t record, uint4 rec) {
+            const float4 P = pos[rec.x], R = prevState[rec.x];
+            sMeta[at] = rec;
+            sPos[at] = P;
+            sMoved[at] = withW(xyz(P) - xyz(R), bodies[rec.y].friction);
+            sRec[at] = record;
+            sKey[at] = b;
+        };
+        if (n <= kBucketSlots) {
+            const uint4 mine = surf[r];
+            uint32_t place = 0;
+            for (uint32_t j = 0; j < n; j++) place += e[j] < r ? 1u : 0u;
+            copyOut(base + place, r, mine);
             return;
         }
+        if (rank[r] != 0) return;
+        const uint32_t m = kBucketSlots;
         for (uint32_t i = 1; i < m; i++) {
             const uint32_t v = e[i];
             uint32_t at = i;
@@ -669,12 +660,9 @@ __global__ void canonKernel(const FrameParams* __restrict__ fp, Work work, const
             }
             e[at] = v;
         }
-        for (uint32_t k = 0; k < m; k++) {
+        for (uint32_t k = 0; k < n; k++) {
             const uint32_t other = e[k];
-            const uint4 rec = surf[other];
-            sMeta[base + k] = rec;
-            sPos[base + k] = pos[rec.x];
-            sRec[base + k] = other;
+            copyOut(base + k, other, surf[other]);
         }
     });
 }
@@ -698,8 +686,9 @@ __device__ __forceinline__ bool admitted(uint4 a, uint4 b, uint32_t selfContact)
 // (r, other) is also appended to `pairs` (capacity-checked), for the
 // pair-set checks.
 //
-// Records are taken in bucket order (`entries`, the counting sort's output,
-// `*cursor` long), so neighbouring records read the same runs. Two mappings
+// Records are taken in bucket order (the counting sort's output as canonKernel
+// copied it, `*cursor` long), so neighbouring records read the same runs.
+// Two mappings
 // of records to threads, chosen per launch from the number of records:
 //
 // - few records (below `warpModeBelow`): one warp per record. The record's
@@ -726,10 +715,9 @@ struct Contactor {
 };
 
 // The per-hit arithmetic of collide.wgsl:70-118 for a candidate that passed
-// the three skips; returns the correction to add.
-__device__ __forceinline__ V contactCorrection(const Contactor& c, uint4 them, float4 Q, float dist2,
-                                               const float4* __restrict__ prevState,
-                                               const DevBody* __restrict__ bodies) {
+// the three skips (M: its motion over the substep, its body's friction);
+// returns the correction to add.
+__device__ __forceinline__ V contactCorrection(const Contactor& c, uint4 them, float4 Q, float4 M, float dist2) {
     const uint32_t mate = them.x;
     const V pj = xyz(Q);
     const V d = c.pi - pj;
@@ -740,11 +728,11 @@ __device__ __forceinline__ V contactCorrection(const Contactor& c, uint4 them, f
     if (dist > 1e-9f) normal = d / dist;
     const float depth = reach - dist;
     V correction = normal * (depth * share);
-    const V sliding = c.movedI - (pj - xyz(prevState[mate]));
+    const V sliding = c.movedI - xyz(M);
     const V tangent = sliding - normal * dot(sliding, normal);
     const float slid = length(tangent);
     if (slid > 1e-9f) {
-        const float mu = fminf(c.frictionI, bodies[them.y].friction);
+        const float mu = fminf(c.frictionI, M.w);
         correction = correction - tangent * (share * fminf(1.0f, mu * depth / slid));
     }
     return correction;
@@ -765,35 +753,37 @@ __device__ __forceinline__ uint32_t divBy(uint32_t n, uint64_t m) { return m ? u
 constexpr uint32_t kCollideBlock = 256;
 
 template <bool EMIT>
-__global__ void __launch_bounds__(kCollideBlock) collideKernel(
-    const FrameParams* __restrict__ fp, uint32_t items, uint32_t warpModeBelow, const uint32_t* __restrict__ entries,
-    const uint32_t* __restrict__ key, const uint32_t* __restrict__ cursor, const uint4* __restrict__ surf,
-    const DevBody* __restrict__ bodies,
-    const float4* __restrict__ pos, const float4* __restrict__ prevState, const uint32_t* __restrict__ start,
-    const uint32_t* __restrict__ count, const uint4* __restrict__ sMeta, const float4* __restrict__ sPos,
-    const uint32_t* __restrict__ sRec, float4* __restrict__ delta, uint32_t* __restrict__ pairs, uint32_t capacity,
-    unsigned long long* __restrict__ pairCount) {
+__global__ void __launch_bounds__(kCollideBlock, 5) collideKernel(
+    const FrameParams* __restrict__ fp, uint32_t items, uint32_t warpModeBelow, const uint32_t* __restrict__ cursor,
+    const DevBody* __restrict__ bodies, const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
+    const uint4* __restrict__ sMeta, const float4* __restrict__ sPos, const float4* __restrict__ sMoved,
+    const uint32_t* __restrict__ sRec, const uint32_t* __restrict__ sKey, float4* __restrict__ delta,
+    uint32_t* __restrict__ pairs, uint32_t capacity, unsigned long long* __restrict__ pairCount) {
     pdlWait();
     pdlLaunchNext();
     constexpr unsigned kAll = 0xffffffffu;
     const uint32_t total = min(items, *cursor);
     const uint32_t selfContact = fp->selfContact;
     const uint32_t thread = blockIdx.x * blockDim.x + threadIdx.x;
-    auto setup = [&](uint32_t r, int centre[3]) {
+    // Entry i of the bucket order: its record r, position, motion and bucket
+    // as canonKernel copied them (positions have not moved since), five
+    // independent loads.
+    auto setup = [&](uint32_t i, uint32_t& r, int centre[3]) {
         Contactor c;
-        c.me = surf[r];
+        r = sRec[i];
+        c.me = sMeta[i];
         c.node = c.me.x;
         c.radius = __uint_as_float(c.me.w);
-        const float4 P = pos[c.node];
+        const float4 P = sPos[i], M = sMoved[i];
         c.wi = P.w;
         c.pi = xyz(P);
-        c.movedI = c.pi - xyz(prevState[c.node]);
+        c.movedI = xyz(M);
+        c.frictionI = M.w;
         const DevBody* grid = bodies + c.me.y;
-        c.frictionI = grid->friction;
-        // The record's bucket coordinates, from the bucket binKernel gave it
-        // (positions have not moved since): integer division by the grid's
-        // dimensions rather than bucketOf's three float divides.
-        const uint32_t linear = key[r] - grid->gridBase;
+        // The record's bucket coordinates, from the bucket binKernel gave it:
+        // integer division by the grid's dimensions rather than bucketOf's
+        // three float divides.
+        const uint32_t linear = sKey[i] - grid->gridBase;
         const uint32_t z = divBy(linear, grid->divXY);
         const uint32_t rest = linear - z * (grid->gridDims[0] * grid->gridDims[1]);
         const uint32_t y = divBy(rest, grid->divX);
@@ -819,9 +809,9 @@ __global__ void __launch_bounds__(kCollideBlock) collideKernel(
 
     if (total >= warpModeBelow) {
         for (uint32_t i = thread; i < total; i += gridDim.x * blockDim.x) {
-            const uint32_t r = entries[i];
+            uint32_t r;
             int centre[3];
-            const Contactor c = setup(r, centre);
+            const Contactor c = setup(i, r, centre);
             const DevBody* grid = bodies + c.me.y;
             uint32_t live = 0;  // which neighbour buckets hold entries: 27 independent loads
 #pragma unroll
@@ -842,10 +832,10 @@ __global__ void __launch_bounds__(kCollideBlock) collideKernel(
                 const uint32_t at = start[b];
                 for (uint32_t k = 0; k < held; k++) {
                     const uint4 them = sMeta[at + k];
-                    const float4 Q = sPos[at + k];
+                    const float4 Q = sPos[at + k], M = sMoved[at + k];
                     float dist2;
                     if (!contactHit(c, them, Q, selfContact, dist2)) continue;
-                    sum = sum + contactCorrection(c, them, Q, dist2, prevState, bodies);
+                    sum = sum + contactCorrection(c, them, Q, M, dist2);
                     hits = hits + 1.0f;
                     if (EMIT) emit(r, at + k);
                 }
@@ -862,18 +852,19 @@ __global__ void __launch_bounds__(kCollideBlock) collideKernel(
     uint32_t* starting = runAt[threadIdx.x >> 5];
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t i = thread >> 5; i < total; i += warps) {
-        const uint32_t r = entries[i];
+        uint32_t r;
         int centre[3];
-        const Contactor c = setup(r, centre);
+        const Contactor c = setup(i, r, centre);
         const DevBody* grid = bodies + c.me.y;
         uint32_t held = 0, first = 0;
         if (lane < 27) {
             bool inside;
             const uint32_t b = neighbour(grid, centre, int(lane), inside);
             if (inside) {
+                // loaded together (start[b] is stale and unused when empty)
                 const uint32_t n = count[b];
+                first = start[b];
                 held = n < kBucketSlots ? n : kBucketSlots;
-                if (held) first = start[b];
             }
         }
         // Inclusive prefix of the run lengths: lane q's run is [end - held, end).
@@ -911,11 +902,11 @@ __global__ void __launch_bounds__(kCollideBlock) collideKernel(
             V correction = mk(0.0f, 0.0f, 0.0f);
             if (cand < candidates) {
                 const uint4 them = sMeta[at];
-                const float4 Q = sPos[at];
+                const float4 Q = sPos[at], M = sMoved[at];
                 float dist2;
                 if (contactHit(c, them, Q, selfContact, dist2)) {
                     hit = true;
-                    correction = contactCorrection(c, them, Q, dist2, prevState, bodies);
+                    correction = contactCorrection(c, them, Q, M, dist2);
                     if (EMIT) emit(r, at);
                 }
             }
@@ -1083,7 +1074,8 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& 
         return e;
     if ((e = launch(c, canonKernel, g, b, s.fp, w, (const uint32_t*)s.key, (const uint32_t*)s.rank,
                     (const uint32_t*)s.start, (const uint32_t*)s.count, s.entries, (const uint4*)s.surf,
-                    (const float4*)s.pos, s.sMeta, s.sPos, s.sRec)))
+                    (const float4*)s.pos, (const float4*)s.prev, (const DevBody*)s.bodies, s.sMeta, s.sPos,
+                    s.sMoved, s.sRec, s.sKey)))
         return e;
     // The gather runs over the bucket-ordered entries (at most recordItems),
     // a warp each while fewer than 2048 per SM, else a thread each.
@@ -1092,11 +1084,10 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& 
                                    : mapping == VSIM_GATHER_THREAD ? 0u
                                                                    : 2048 * c.sms;
     auto collide = [&](auto kernel, uint32_t* out, uint32_t cap, unsigned long long* n) {
-        return launch(c, kernel, cg, kCollideBlock, s.fp, recordItems, warpModeBelow, (const uint32_t*)s.entries,
-                      (const uint32_t*)s.key, (const uint32_t*)s.cursor,
-                      (const uint4*)s.surf, (const DevBody*)s.bodies, (const float4*)s.pos, (const float4*)s.prev,
-                      (const uint32_t*)s.start, (const uint32_t*)s.count, (const uint4*)s.sMeta,
-                      (const float4*)s.sPos, (const uint32_t*)s.sRec, s.delta, out, cap, n);
+        return launch(c, kernel, cg, kCollideBlock, s.fp, recordItems, warpModeBelow, (const uint32_t*)s.cursor,
+                      (const DevBody*)s.bodies, (const uint32_t*)s.start, (const uint32_t*)s.count,
+                      (const uint4*)s.sMeta, (const float4*)s.sPos, (const float4*)s.sMoved,
+                      (const uint32_t*)s.sRec, (const uint32_t*)s.sKey, s.delta, out, cap, n);
     };
     if (mode == ContactMode::Pairs) {
         if ((e = collide(collideKernel<true>, pairs, capacity, pairCount))) return e;

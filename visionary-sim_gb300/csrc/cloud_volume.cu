@@ -3,14 +3,20 @@
 // the reference's "cloud" rest geometry (voxelLattice.js:208-226).
 //
 // The reference runs it on the CPU in JavaScript doubles. Here every step is
-// a kernel, in the same double arithmetic and order, so the grid is the same
-// cell for cell:
+// a kernel whose every decision equals the one the same double arithmetic
+// and order would take, so the grid is the same cell for cell. Double
+// arithmetic is slow on this part, so decisions are taken in float wherever
+// a proven error bound shows float gives the same answer, and in double
+// only where it cannot:
 //   1. bounds: each Gaussian's ellipsoid reach (materialBounds, :219-234),
-//      reduced with order-preserving 64-bit keys;
+//      estimated in float with a relative bound; the extremes reduced with
+//      order-preserving 64-bit keys, then evaluated exactly for the few
+//      Gaussians whose bracket can hold an extreme;
 //   2. the grid laid out on the host from the bounds (gridForBounds,
 //      voxelize.js:40-67);
 //   3. stamp: a thread per Gaussian marks its centre cell and tests the
-//      cells of its box against the ellipsoid (stampCloud, :138-178); a box
+//      cells of its box against the ellipsoid (stampCloud, :138-178), box
+//      edges and samples decided in float unless too close to call; a box
 //      of more than kInlineBoxCells cells is handed to a block instead;
 //   4. seal and fill (:291-306): 6-neighbourhood dilations, the fill, as
 //      many erosions, the stamp put back. The reference fills by flooding
@@ -62,22 +68,26 @@ struct CloudInput {
     const float* scale;  // standard deviations per axis, metres
     uint32_t count;
     double sigma;
+    float sigmaF;        // float(sigma)
 };
 
 struct GridView {
     uint32_t dims[3];
     double origin[3];
     double h;
+    float invH;  // float(1 / h), 0 outside [2^-40, 2^40]
+    float hF;    // float(h)
+    float originMag[3];  // max(|float(origin)|, 2^-100)
+    bool floatBound;     // h in [2^-30, 2^30] and |origin| <= 2^40 on every axis
     uint32_t cells;
 };
 
 // One Gaussian as an ellipsoid (cloudVolume.js:195-210): the column-major
 // rotation as the reference's Float32Array holds it, the half-axes in the
-// Gaussian's frame, the reach along each world axis.
+// Gaussian's frame.
 struct Ellipsoid {
     double col[9];
     double radius[3];
-    double half[3];
 };
 
 // JavaScript's Math.hypot as V8 evaluates it (its published math builtin):
@@ -122,15 +132,6 @@ __device__ void frameOf(const CloudInput& in, uint32_t i, Ellipsoid& e) {
     for (int a = 0; a < 3; a++) e.radius[a] = in.sigma * double(in.scale[3 * size_t(i) + a]);
 }
 
-// cloudVolume.js:201-209: the reach along each world axis.
-__device__ Ellipsoid ellipsoidOf(const CloudInput& in, uint32_t i) {
-    Ellipsoid e;
-    frameOf(in, i, e);
-    for (int a = 0; a < 3; a++)
-        e.half[a] = hypotV8(e.col[a] * e.radius[0], e.col[3 + a] * e.radius[1], e.col[6 + a] * e.radius[2]);
-    return e;
-}
-
 // Doubles ordered as unsigned integers: the sign bit flipped on positives,
 // every bit on negatives.
 __device__ __forceinline__ unsigned long long orderedKey(double v) {
@@ -155,20 +156,75 @@ __device__ __forceinline__ unsigned long long warpMax64(unsigned long long v) {
     return v;
 }
 
-// cloudVolume.js:219-234 (materialBounds): keys[0..2] the smallest
-// position - reach per axis, keys[3..5] the largest position + reach; a NaN
-// anywhere raises *nan (Math.min and Math.max then give NaN). Each
-// Gaussian's reach is stored in `reach` for the stamp.
+// The float side of the bounds and the stamp. For each Gaussian the bounds
+// pass keeps, per world axis a, frames[3 i + a] = (row a of its frame as the
+// float32 values frameOf rounds to, a float estimate of its reach along a);
+// the estimate is NaN where it cannot be trusted, and only then is V8's
+// hypot evaluated in double (FP64 runs at a small fraction of the float rate
+// on this part: a double division costs about a hundred float operations).
+//
+// The estimate, sqrtf of the float sum of the float products' squares, is
+// within 2^-21 of V8's hypot of the double products (relative): the float
+// products are within 2^-22.9 of the double ones (the radius and the product
+// each rounded once), their squares and two sums add under 2^-22, the square
+// root halves that, and V8's own evaluation is within 2^-50 of the exact
+// hypot. kReachSlack, 8 times that, brackets the exact reach:
+//   hf (1 - kReachSlack) <= reach <= hf (1 + kReachSlack),
+// both products rounded in double well inside the slack. It holds while
+// every nonzero product lies in [2^-60, 2^60] (squares and sums stay normal
+// floats) and the radii are 0 or in [2^-100, 2^100].
+constexpr double kReachSlack = 0x1p-18;
+
+__device__ float reachEstimate(const float col[9], const float r[3], int a) {
+    float sum = 0.0f;
+    for (int k = 0; k < 3; k++) {
+        const float c = col[3 * k + a];
+        const float v = c * r[k];
+        if (c != 0.0f && r[k] != 0.0f && !(fabsf(v) >= 0x1p-60f && fabsf(v) <= 0x1p60f)) return CUDART_NAN_F;
+        sum += v * v;
+    }
+    return sqrtf(sum);
+}
+
+// The radii sigma * scale in double, as cloudVolume.js:196-199 computes them,
+// and as floats for the estimate (NaN where out of its range).
+__device__ void radiiOf(const CloudInput& in, uint32_t i, double r[3], float rf[3]) {
+    for (int a = 0; a < 3; a++) {
+        r[a] = in.sigma * double(in.scale[3 * size_t(i) + a]);
+        const double m = fabs(r[a]);
+        rf[a] = (r[a] == 0.0 || (m >= 0x1p-100 && m <= 0x1p100)) ? float(r[a]) : CUDART_NAN_F;
+    }
+}
+
+// cloudVolume.js:219-234 (materialBounds), first pass: per axis the smallest
+// upper bound on position - reach (keys[0..2]) and the largest lower bound on
+// position + reach (keys[3..5]) over all Gaussians, from the reach estimates;
+// exact values where a Gaussian has no estimate. A NaN anywhere raises *nan
+// (Math.min and Math.max then give NaN). Fills `frames`.
 __global__ void cloudBoundsKernel(CloudInput in, unsigned long long* __restrict__ keys, uint32_t* __restrict__ nan,
-                                  double* __restrict__ reach) {
+                                  float4* __restrict__ frames) {
     unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
     bool sawNan = false;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < in.count; i += gridDim.x * blockDim.x) {
-        const Ellipsoid e = ellipsoidOf(in, i);
+        Ellipsoid e;
+        frameOf(in, i, e);
+        float col[9], rf[3];
+        for (int q = 0; q < 9; q++) col[q] = float(e.col[q]);
+        radiiOf(in, i, e.radius, rf);
         for (int a = 0; a < 3; a++) {
-            reach[3 * size_t(i) + a] = e.half[a];  // kept for the stamp
             const double p = in.pos[3 * size_t(i) + a];
-            const double l = p - e.half[a], u = p + e.half[a];
+            float hf = reachEstimate(col, rf, a);
+            if (!isfinite(p)) hf = CUDART_NAN_F;
+            frames[3 * size_t(i) + a] = make_float4(col[3 * a], col[3 * a + 1], col[3 * a + 2], hf);
+            double l, u;
+            if (isnan(hf)) {
+                const double half = hypotV8(e.col[a] * e.radius[0], e.col[3 + a] * e.radius[1], e.col[6 + a] * e.radius[2]);
+                l = p - half;
+                u = p + half;
+            } else {
+                l = p - double(hf) * (1.0 - kReachSlack);  // >= position - reach
+                u = p + double(hf) * (1.0 - kReachSlack);  // <= position + reach
+            }
             sawNan |= isnan(l) || isnan(u);
             lo[a] = min(lo[a], orderedKey(l));
             hi[a] = max(hi[a], orderedKey(u));
@@ -185,6 +241,48 @@ __global__ void cloudBoundsKernel(CloudInput in, unsigned long long* __restrict_
             atomicMax(keys + 3 + a, hi[a]);
         }
         if (sawNan) atomicOr(nan, 1u);
+    }
+}
+
+// The exact reach along axis a (cloudVolume.js:201-209).
+__device__ double exactReach(const CloudInput& in, uint32_t i, int a) {
+    Ellipsoid e;
+    frameOf(in, i, e);
+    return hypotV8(e.col[a] * e.radius[0], e.col[3 + a] * e.radius[1], e.col[6 + a] * e.radius[2]);
+}
+
+// Second pass: the exact extremes. Only a Gaussian whose position - reach can
+// lie at or below the first pass's smallest upper bound can hold the minimum
+// (every other one's exceeds it), and likewise for the maximum; those few get
+// the exact reach and their exact bound into exact[0..5].
+__global__ void cloudExtremesKernel(CloudInput in, const unsigned long long* __restrict__ keys,
+                                    const float4* __restrict__ frames, unsigned long long* __restrict__ exact) {
+    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < in.count; i += gridDim.x * blockDim.x) {
+        for (int a = 0; a < 3; a++) {
+            const double p = in.pos[3 * size_t(i) + a];
+            const float hf = frames[3 * size_t(i) + a].w;
+            bool low = true, high = true;
+            if (!isnan(hf)) {
+                const double wide = double(hf) * (1.0 + kReachSlack);
+                low = orderedKey(p - wide) <= keys[a];
+                high = orderedKey(p + wide) >= keys[3 + a];
+            }
+            if (!(low || high)) continue;
+            const double half = exactReach(in, i, a);
+            if (low) lo[a] = min(lo[a], orderedKey(p - half));
+            if (high) hi[a] = max(hi[a], orderedKey(p + half));
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        lo[a] = warpMin64(lo[a]);
+        hi[a] = warpMax64(hi[a]);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int a = 0; a < 3; a++) {
+            if (lo[a] != ~0ull) atomicMin(exact + a, lo[a]);
+            if (hi[a] != 0) atomicMax(exact + 3 + a, hi[a]);
+        }
     }
 }
 
@@ -282,6 +380,61 @@ __device__ bool floatTestOf(const GridView& g, const Box& b, const double c[3], 
     return true;
 }
 
+// floatTestOf with the bound's terms summed in float instead of double, from
+// the frame rows the bounds pass kept (f.col, exactly floatTestOf's), the
+// position as float (exact) and the radius as float(sigma) * scale (within
+// 2^-23 of float(r), so its reciprocal stays inside the 2^-21 |t|
+// allowance). All terms are sums and products of magnitudes, so each float
+// rounding (2^-24 relative, about a dozen along any chain) lowers them by
+// under 2^-20 in all, which the final (1 + 2^-16) more than restores;
+// magnitudes under 2^-100 are counted as 2^-100. Only the base offsets are
+// formed in double, as floatTestOf forms them. Inside the ranges checked
+// here (and g.floatBound's: h in [2^-30, 2^30], |origin| <= 2^40) no term is
+// a subnormal float or overflows (the smallest, 2^-50 h, is above 2^-80; the
+// error after the reciprocal above 2^-113); elsewhere floatTestOf decides.
+// Conversions from double cost FP64-pipe time on this part: there are four
+// a Gaussian.
+__device__ bool floatTestInFloat(const CloudInput& in, uint32_t i, const GridView& g, const Box& b,
+                                 const double c[3], const float cf[3], const float col[9], FloatTest& f) {
+    float rf[3];
+    bool ok = g.floatBound;
+    for (int a = 0; a < 3; a++) {
+        rf[a] = in.sigmaF * in.scale[3 * size_t(i) + a];
+        ok = ok && fabsf(cf[a]) <= 0x1p40f && b.extent(a) <= (1 << 20) && rf[a] >= 0x1p-30f && rf[a] <= 0x1p30f;
+    }
+    for (int q = 0; q < 9; q++) {
+        const float m = fabsf(col[q]);
+        ok = ok && (m == 0.0f || (m >= 0x1p-30f && m <= 0x1p30f));
+    }
+    if (!ok) {
+        Ellipsoid e;
+        for (int q = 0; q < 9; q++) e.col[q] = col[q];
+        for (int a = 0; a < 3; a++) e.radius[a] = in.sigma * double(in.scale[3 * size_t(i) + a]);
+        return floatTestOf(g, b, c, e, f);
+    }
+    const float h = g.hF;
+    float X[3], ex[3];
+    for (int a = 0; a < 3; a++) {
+        const double base = (g.origin[a] + double(b.lo[a]) * g.h) - c[a];
+        f.base[a] = float(base);
+        const float span = float(int32_t(b.extent(a) + 1)) * h;
+        X[a] = fmaxf(fabsf(f.base[a]), 0x1p-100f) + span;
+        const float lo = float(int32_t(b.lo[a]));
+        ex[a] = 0x1p-22f * X[a] + 0x1p-50f * (g.originMag[a] + fmaxf(fabsf(cf[a]), 0x1p-100f) + fabsf(lo) * h + span);
+    }
+    f.h = h;
+    for (int q = 0; q < 9; q++) f.col[q] = col[q];
+    for (int a = 0; a < 3; a++) {
+        f.inv[a] = __frcp_rn(rf[a]);
+        float dotErr = 0.0f;
+        for (int k = 0; k < 3; k++) dotErr += fabsf(f.col[3 * a + k]) * (ex[k] + 0x1p-22f * X[k]);
+        const float err = 4.0f * dotErr * f.inv[a] * (1.0f + 0x1p-16f);
+        if (!(err < 1e-3f)) return false;
+        f.err[a] = err;
+    }
+    return true;
+}
+
 // 1 inside, 0 outside, -1 too close to call in float.
 __device__ __forceinline__ int floatSample(const FloatTest& f, float ox, float oy, float oz) {
     const float dx = f.base[0] + ox * f.h, dy = f.base[1] + oy * f.h, dz = f.base[2] + oz * f.h;
@@ -304,19 +457,25 @@ __device__ __forceinline__ int floatSample(const FloatTest& f, float ox, float o
 // padding is under two cells) coordinates, and like a typed array the grid
 // ignores an index outside it. The double frame is rebuilt only for a sample
 // the float test cannot call.
+//
+// The float path converts nothing from double or 64-bit integers: on this
+// part such conversions run on the FP64 pipe, and nine samples a cell made
+// them the stamp's bottleneck. The cell's place in its box (under 2^20, so
+// exact) is an int32 turned float once; the sample offsets are float
+// constants.
 __device__ void stampCell(const CloudInput& in, uint32_t gaussian, const GridView& g, uint8_t* occ, const Box& b,
                           int64_t i, int64_t j, int64_t k, const double c[3], const FloatTest* f) {
     const int64_t cell = i + int64_t(g.dims[0]) * (j + int64_t(g.dims[1]) * k);
     if (cell < 0 || cell >= int64_t(g.cells) || occ[cell] != 0) return;
     Ellipsoid e;
     bool haveFrame = false;
+    const float fi = float(int32_t(i - b.lo[0])), fj = float(int32_t(j - b.lo[1])), fk = float(int32_t(k - b.lo[2]));
+#pragma unroll
     for (int s = 0; s < 9; s++) {
-        double ox, oy, oz;
-        sampleOffset(s, ox, oy, oz);
+        const float ox = s == 8 ? 0.5f : float(s & 1), oy = s == 8 ? 0.5f : float((s >> 1) & 1);
+        const float oz = s == 8 ? 0.5f : float((s >> 2) & 1);
         int inside = -1;
-        if (f)
-            inside = floatSample(*f, float(i - b.lo[0]) + float(ox), float(j - b.lo[1]) + float(oy),
-                                 float(k - b.lo[2]) + float(oz));
+        if (f) inside = floatSample(*f, fi + ox, fj + oy, fk + oz);
         if (inside < 0) {
             if (!haveFrame) {
                 frameOf(in, gaussian, e);
@@ -331,40 +490,98 @@ __device__ void stampCell(const CloudInput& in, uint32_t gaussian, const GridVie
     }
 }
 
-__device__ Box boxOf(const GridView& g, const double c[3], const double* half) {
+// floor(RN(RN(x - origin) / h)) (cloudVolume.js:384-386) shared by every
+// double x in [xl, xu], found without the double division; false when the
+// ends do not floor to one cell or leave the estimate's range. For an end q
+// = RN(x - origin) the float quotient e = float(q) * invH is within 3 2^-24
+// of q / h and so within 2^-22.2 |e| of RN(q / h); e - 2^-21 |e| and e +
+// 2^-21 |e|, each rounded once more, still bracket it. RN is monotone, so
+// the quotients of the ends bracket every x's, and one floor for both
+// brackets is the floor of all. (q zero gives the exact quotient 0; a q that
+// float cannot hold to 2^-24 is refused.)
+__device__ bool sharedCell(double xl, double xu, double origin, float invH, int64_t& cell) {
+    const double ql = xl - origin, qu = xu - origin;
+    const float fl = float(ql), fu = float(qu);
+    const bool okl = ql == 0.0 || (fabsf(fl) >= 0x1p-60f && fabsf(fl) <= 0x1p60f);
+    const bool oku = qu == 0.0 || (fabsf(fu) >= 0x1p-60f && fabsf(fu) <= 0x1p60f);
+    if (!(okl && oku && invH > 0.0f)) return false;
+    const float el = fl * invH, eu = fu * invH;
+    if (!(fabsf(el) < 0x1p22f && fabsf(eu) < 0x1p22f)) return false;
+    const float a = floorf(el - fabsf(el) * 0x1p-21f), b = floorf(eu + fabsf(eu) * 0x1p-21f);
+    if (a != b) return false;
+    cell = int64_t(a);
+    return true;
+}
+
+__device__ __forceinline__ int64_t clampCell(int64_t v, int64_t lo, int64_t hi) { return v < lo ? lo : v > hi ? hi : v; }
+
+// cloudVolume.js:384-386 for the centre: the float estimate, else exact.
+__device__ int64_t centreCell(const GridView& g, double c, int a) {
+    int64_t cell;
+    if (sharedCell(c, c, g.origin[a], g.invH, cell)) return clampCell(cell, 0, int64_t(g.dims[a]) - 1);
+    return clampedCell(c, g.origin[a], g.h, 0, int64_t(g.dims[a]) - 1);
+}
+
+// cloudVolume.js:147-160: the cells from position - reach to position +
+// reach, within one cell of the faces. With a reach estimate hf the exact
+// reach lies in [hf (1 - kReachSlack), hf (1 + kReachSlack)] (both products
+// exact in double), so each edge is the shared cell of that interval's
+// ends; only an edge within the slack of a cell boundary (or a Gaussian
+// without an estimate) takes the exact reach and the double division.
+__device__ Box boxOf(const CloudInput& in, uint32_t i, const GridView& g, const double c[3], const float hf[3]) {
     Box b;
     for (int a = 0; a < 3; a++) {
-        b.lo[a] = clampedCell(c[a] - half[a], g.origin[a], g.h, 1, int64_t(g.dims[a]) - 2);
-        b.hi[a] = clampedCell(c[a] + half[a], g.origin[a], g.h, 1, int64_t(g.dims[a]) - 2);
+        const int64_t lo = 1, hi = int64_t(g.dims[a]) - 2;
+        if (!isnan(hf[a])) {
+            const double narrow = double(hf[a]) * (1.0 - kReachSlack), wide = double(hf[a]) * (1.0 + kReachSlack);
+            int64_t l, u;
+            if (sharedCell(c[a] - wide, c[a] - narrow, g.origin[a], g.invH, l) &&
+                sharedCell(c[a] + narrow, c[a] + wide, g.origin[a], g.invH, u)) {
+                b.lo[a] = clampCell(l, lo, hi);
+                b.hi[a] = clampCell(u, lo, hi);
+                continue;
+            }
+        }
+        const double half = exactReach(in, i, a);
+        b.lo[a] = clampedCell(c[a] - half, g.origin[a], g.h, lo, hi);
+        b.hi[a] = clampedCell(c[a] + half, g.origin[a], g.h, lo, hi);
     }
     return b;
 }
 
-// The Gaussian's box and its float test (false: test in double).
-__device__ bool prepareStamp(const CloudInput& in, uint32_t i, const GridView& g, const double* __restrict__ reach,
+// The Gaussian's box and its float test (false: test in double), from the
+// frame rows and reach estimates the bounds pass kept; the frame's double
+// values are the float rows widened, exactly frameOf's.
+__device__ bool prepareStamp(const CloudInput& in, uint32_t i, const GridView& g, const float4* __restrict__ frames,
                              const double c[3], Box& b, FloatTest& f) {
-    const double half[3] = {reach[3 * size_t(i)], reach[3 * size_t(i) + 1], reach[3 * size_t(i) + 2]};
-    b = boxOf(g, c, half);
-    Ellipsoid e;
-    frameOf(in, i, e);
-    return floatTestOf(g, b, c, e, f);
+    float col[9], hf[3], cf[3];
+    for (int a = 0; a < 3; a++) {
+        const float4 row = frames[3 * size_t(i) + a];
+        col[3 * a] = row.x;
+        col[3 * a + 1] = row.y;
+        col[3 * a + 2] = row.z;
+        hf[a] = row.w;
+        cf[a] = in.pos[3 * size_t(i) + a];
+    }
+    b = boxOf(in, i, g, c, hf);
+    return floatTestInFloat(in, i, g, b, c, cf, col, f);
 }
 
 // cloudVolume.js:147-177 for one Gaussian per thread: the centre's cell
 // unconditionally, then the box; a box of more than kInlineBoxCells cells is
 // listed for cloudStampBoxKernel.
-__global__ void cloudStampKernel(CloudInput in, GridView g, const double* __restrict__ reach,
+__global__ void cloudStampKernel(CloudInput in, GridView g, const float4* __restrict__ frames,
                                  uint8_t* __restrict__ occ, uint32_t* __restrict__ big,
                                  uint32_t* __restrict__ bigCount) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= in.count) return;
     const double c[3] = {in.pos[3 * size_t(i)], in.pos[3 * size_t(i) + 1], in.pos[3 * size_t(i) + 2]};
     int64_t at[3];
-    for (int a = 0; a < 3; a++) at[a] = clampedCell(c[a], g.origin[a], g.h, 0, int64_t(g.dims[a]) - 1);
+    for (int a = 0; a < 3; a++) at[a] = centreCell(g, c[a], a);
     occ[at[0] + int64_t(g.dims[0]) * (at[1] + int64_t(g.dims[1]) * at[2])] = 1;
     Box b;
     FloatTest f;
-    const bool fast = prepareStamp(in, i, g, reach, c, b, f);
+    const bool fast = prepareStamp(in, i, g, frames, c, b, f);
     if (b.cells() > kInlineBoxCells) {
         big[atomicAdd(bigCount, 1u)] = i;  // at most one slot per Gaussian: `big` holds count
         return;
@@ -375,7 +592,7 @@ __global__ void cloudStampKernel(CloudInput in, GridView g, const double* __rest
 }
 
 // The listed large boxes, a block each, its threads over the box's cells.
-__global__ void cloudStampBoxKernel(CloudInput in, GridView g, const double* __restrict__ reach,
+__global__ void cloudStampBoxKernel(CloudInput in, GridView g, const float4* __restrict__ frames,
                                     uint8_t* __restrict__ occ, const uint32_t* __restrict__ big,
                                     const uint32_t* __restrict__ bigCount) {
     const uint32_t listed = *bigCount;
@@ -384,7 +601,7 @@ __global__ void cloudStampBoxKernel(CloudInput in, GridView g, const double* __r
         const double c[3] = {in.pos[3 * size_t(i)], in.pos[3 * size_t(i) + 1], in.pos[3 * size_t(i) + 2]};
         Box b;
         FloatTest f;
-        const bool fast = prepareStamp(in, i, g, reach, c, b, f);
+        const bool fast = prepareStamp(in, i, g, frames, c, b, f);
         const int64_t ex = b.extent(0), exy = ex * b.extent(1), total = b.cells();
         for (int64_t t = threadIdx.x; t < total; t += blockDim.x) {
             const int64_t k = b.lo[2] + t / exy, r = t % exy;
@@ -554,7 +771,8 @@ __global__ void countKernel(const uint8_t* __restrict__ occ, uint32_t cells, uns
 
 // Small device words of one run.
 struct CloudScalars {
-    unsigned long long keys[6];
+    unsigned long long keys[6];   // the bounds' first pass
+    unsigned long long exact[6];  // the exact extremes
     unsigned long long filled;
     unsigned long long occupied;
     uint32_t nan;
@@ -617,12 +835,13 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     POOL_ALLOC(scalarsBuf, sizeof(CloudScalars), pool, st, "cloud scratch");
     auto* sc = static_cast<CloudScalars*>(scalarsBuf.p);
     CloudScalars init{};
-    for (int a = 0; a < 3; a++) init.keys[a] = ~0ull;
+    for (int a = 0; a < 3; a++) init.keys[a] = init.exact[a] = ~0ull;
     CK(cudaMemcpyAsync(sc, &init, sizeof init, cudaMemcpyHostToDevice, st), "cloud scratch");
-    DeviceBuffer reachBuf;
-    POOL_ALLOC(reachBuf, size_t(in.count) * 3 * sizeof(double), pool, st, "cloud scratch");
-    auto* reach = static_cast<double*>(reachBuf.p);
-    cloudBoundsKernel<<<streamGrid(in.count, sms), kCloudBlock, 0, st>>>(in, sc->keys, &sc->nan, reach);
+    DeviceBuffer framesBuf;
+    POOL_ALLOC(framesBuf, size_t(in.count) * 3 * sizeof(float4), pool, st, "cloud scratch");
+    auto* frames = static_cast<float4*>(framesBuf.p);
+    cloudBoundsKernel<<<streamGrid(in.count, sms), kCloudBlock, 0, st>>>(in, sc->keys, &sc->nan, frames);
+    cloudExtremesKernel<<<streamGrid(in.count, sms), kCloudBlock, 0, st>>>(in, sc->keys, frames, sc->exact);
     CK(cudaGetLastError(), "cloud bounds");
     CloudScalars got{};
     CK(cudaMemcpyAsync(&got, sc, sizeof got, cudaMemcpyDeviceToHost, st), "cloud bounds");
@@ -632,8 +851,8 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     double lo[3], hi[3], extent[3];
     bool nan = got.nan != 0;
     for (int a = 0; a < 3; a++) {
-        lo[a] = fromOrderedKey(got.keys[a]);
-        hi[a] = fromOrderedKey(got.keys[3 + a]);
+        lo[a] = fromOrderedKey(got.exact[a]);
+        hi[a] = fromOrderedKey(got.exact[3 + a]);
         extent[a] = hi[a] - lo[a];
         nan |= std::isnan(extent[a]);
     }
@@ -661,6 +880,16 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
         g.origin[a] = v->origin[a];
     }
     g.h = h;
+    // float(1 / h) for the float cell estimate, which wants every quotient
+    // it forms a normal float (quotients from 2^-60 / 2^40 up)
+    const float invH = float(1.0 / h);
+    g.invH = invH >= 0x1p-40f && invH <= 0x1p40f ? invH : 0.0f;
+    g.hF = float(h);
+    g.floatBound = h >= 0x1p-30 && h <= 0x1p30;
+    for (int a = 0; a < 3; a++) {
+        g.originMag[a] = std::max(std::fabs(float(g.origin[a])), 0x1p-100f);
+        g.floatBound = g.floatBound && std::fabs(g.origin[a]) <= 0x1p40;
+    }
     g.cells = n;
 
     CK(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&v->occupancy), n, pool, st), "cloud occupancy");
@@ -670,9 +899,9 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     DeviceBuffer bigBuf;
     POOL_ALLOC(bigBuf, size_t(in.count) * 4, pool, st, "cloud scratch");
     cloudStampKernel<<<(in.count + kCloudBlock - 1) / kCloudBlock, kCloudBlock, 0, st>>>(
-        in, g, reach, v->occupancy, static_cast<uint32_t*>(bigBuf.p), &sc->bigCount);
+        in, g, frames, v->occupancy, static_cast<uint32_t*>(bigBuf.p), &sc->bigCount);
     cloudStampBoxKernel<<<uint32_t(sms) * 4, kCloudBlock, 0, st>>>(
-        in, g, reach, v->occupancy, static_cast<const uint32_t*>(bigBuf.p), &sc->bigCount);
+        in, g, frames, v->occupancy, static_cast<const uint32_t*>(bigBuf.p), &sc->bigCount);
     CK(cudaGetLastError(), "cloud stamp");
 
     // 4. seal and fill
@@ -765,7 +994,7 @@ int vsim_voxelize_cloud_device(const float* d_positions, const float* d_rotation
     // the caller's work on the inputs finishes first
     cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
     int rc = e == cudaSuccess ? VSIM_OK : cudaFail(e, "caller stream");
-    if (!rc) rc = voxelizeCloud(v, CloudInput{d_positions, d_rotations, d_scales, uint32_t(count), options->sigma},
+    if (!rc) rc = voxelizeCloud(v, CloudInput{d_positions, d_rotations, d_scales, uint32_t(count), options->sigma, float(options->sigma)},
                                 *options);
     if (rc) {
         cudaStreamSynchronize(v->stream);
@@ -791,7 +1020,7 @@ int voxelizeHostCloud(vsim_cloud_volume* v, const float* positions, const float*
     CK(cudaMemcpyAsync(dPos, positions, n * 12, cudaMemcpyHostToDevice, v->stream), "cloud inputs");
     CK(cudaMemcpyAsync(dRot, rotations, n * 16, cudaMemcpyHostToDevice, v->stream), "cloud inputs");
     CK(cudaMemcpyAsync(dScale, scales, n * 12, cudaMemcpyHostToDevice, v->stream), "cloud inputs");
-    return voxelizeCloud(v, CloudInput{dPos, dRot, dScale, uint32_t(n), o.sigma}, o);
+    return voxelizeCloud(v, CloudInput{dPos, dRot, dScale, uint32_t(n), o.sigma, float(o.sigma)}, o);
 }
 
 }  // namespace

@@ -463,13 +463,13 @@ __device__ __forceinline__ int floatSample(const FloatTest& f, float ox, float o
 // them the stamp's bottleneck. The cell's place in its box (under 2^20, so
 // exact) is an int32 turned float once; the sample offsets are float
 // constants.
-__device__ void stampCell(const CloudInput& in, uint32_t gaussian, const GridView& g, uint8_t* occ, const Box& b,
+__device__ void stampCell(const CloudInput& in, uint32_t gaussian, const GridView& g, uint8_t* occ, const int64_t lo[3],
                           int64_t i, int64_t j, int64_t k, const double c[3], const FloatTest* f) {
     const int64_t cell = i + int64_t(g.dims[0]) * (j + int64_t(g.dims[1]) * k);
     if (cell < 0 || cell >= int64_t(g.cells) || occ[cell] != 0) return;
     Ellipsoid e;
     bool haveFrame = false;
-    const float fi = float(int32_t(i - b.lo[0])), fj = float(int32_t(j - b.lo[1])), fk = float(int32_t(k - b.lo[2]));
+    const float fi = float(int32_t(i - lo[0])), fj = float(int32_t(j - lo[1])), fk = float(int32_t(k - lo[2]));
 #pragma unroll
     for (int s = 0; s < 9; s++) {
         const float ox = s == 8 ? 0.5f : float(s & 1), oy = s == 8 ? 0.5f : float((s >> 1) & 1);
@@ -567,28 +567,83 @@ __device__ bool prepareStamp(const CloudInput& in, uint32_t i, const GridView& g
     return floatTestInFloat(in, i, g, b, c, cf, col, f);
 }
 
-// cloudVolume.js:147-177 for one Gaussian per thread: the centre's cell
-// unconditionally, then the box; a box of more than kInlineBoxCells cells is
-// listed for cloudStampBoxKernel.
-__global__ void cloudStampKernel(CloudInput in, GridView g, const float4* __restrict__ frames,
-                                 uint8_t* __restrict__ occ, uint32_t* __restrict__ big,
-                                 uint32_t* __restrict__ bigCount) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= in.count) return;
-    const double c[3] = {in.pos[3 * size_t(i)], in.pos[3 * size_t(i) + 1], in.pos[3 * size_t(i) + 2]};
-    int64_t at[3];
-    for (int a = 0; a < 3; a++) at[a] = centreCell(g, c[a], a);
-    occ[at[0] + int64_t(g.dims[0]) * (at[1] + int64_t(g.dims[1]) * at[2])] = 1;
-    Box b;
+// One Gaussian's stamp as the walk below needs it, in shared memory.
+struct StampEntry {
     FloatTest f;
-    const bool fast = prepareStamp(in, i, g, frames, c, b, f);
-    if (b.cells() > kInlineBoxCells) {
-        big[atomicAdd(bigCount, 1u)] = i;  // at most one slot per Gaussian: `big` holds count
-        return;
+    int64_t lo[3];
+    uint32_t ex, exy;  // the box's extent along x, and x times y
+    uint32_t gaussian;
+    uint32_t fast;
+};
+
+constexpr uint32_t kStampBlock = 128;
+
+// cloudVolume.js:147-177. Each thread sets up one Gaussian: its centre's cell
+// unconditionally, its box and float test; a box of more than
+// kInlineBoxCells cells is listed for cloudStampBoxKernel. Then each warp
+// walks its 32 Gaussians' boxes as one list of cells dealt to its lanes 32
+// at a time (a lane finds the Gaussian owning its cell by a binary search
+// over the warp's running offsets), so lanes are not idle while one
+// Gaussian's box is longer than its neighbours'. Marking is an OR: which
+// lane tests a cell, and when, changes nothing.
+__global__ void __launch_bounds__(kStampBlock) cloudStampKernel(CloudInput in, GridView g,
+                                                                const float4* __restrict__ frames,
+                                                                uint8_t* __restrict__ occ, uint32_t* __restrict__ big,
+                                                                uint32_t* __restrict__ bigCount) {
+    constexpr unsigned kAll = 0xffffffffu;
+    __shared__ StampEntry entries[kStampBlock];
+    const uint32_t lane = threadIdx.x & 31;
+    const StampEntry* warpEntries = entries + (threadIdx.x & ~31u);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t n = 0;
+    if (i < in.count) {
+        const double c[3] = {in.pos[3 * size_t(i)], in.pos[3 * size_t(i) + 1], in.pos[3 * size_t(i) + 2]};
+        int64_t at[3];
+        for (int a = 0; a < 3; a++) at[a] = centreCell(g, c[a], a);
+        occ[at[0] + int64_t(g.dims[0]) * (at[1] + int64_t(g.dims[1]) * at[2])] = 1;
+        Box b;
+        StampEntry& mine = entries[threadIdx.x];
+        const bool fast = prepareStamp(in, i, g, frames, c, b, mine.f);
+        if (b.cells() > kInlineBoxCells) {
+            big[atomicAdd(bigCount, 1u)] = i;  // at most one slot per Gaussian: `big` holds count
+        } else {
+            n = uint32_t(b.cells());
+            for (int a = 0; a < 3; a++) mine.lo[a] = b.lo[a];
+            mine.ex = uint32_t(b.extent(0));
+            mine.exy = mine.ex * uint32_t(b.extent(1));
+            mine.gaussian = i;
+            mine.fast = fast ? 1u : 0u;
+        }
     }
-    for (int64_t k = b.lo[2]; k <= b.hi[2]; k++)
-        for (int64_t j = b.lo[1]; j <= b.hi[1]; j++)
-            for (int64_t i2 = b.lo[0]; i2 <= b.hi[0]; i2++) stampCell(in, i, g, occ, b, i2, j, k, c, fast ? &f : nullptr);
+    // The warp's running offsets: lane l's cells are [off, off + n).
+    uint32_t incl = n;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(kAll, incl, d);
+        if (lane >= uint32_t(d)) incl += v;
+    }
+    const uint32_t off = incl - n;
+    const uint32_t total = __shfl_sync(kAll, incl, 31);
+    __syncwarp();
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t t = base + lane;
+        // the last lane whose offset is at or below t (offsets never fall)
+        uint32_t owner = 0;
+#pragma unroll
+        for (uint32_t step = 16; step >= 1; step >>= 1) {
+            const uint32_t probe = __shfl_sync(kAll, off, owner + step);
+            if (probe <= t) owner += step;
+        }
+        const uint32_t first = __shfl_sync(kAll, off, owner);
+        if (t >= total) continue;
+        const StampEntry& e = warpEntries[owner];
+        const uint32_t r = t - first, ex = e.ex, exy = e.exy;
+        const uint32_t k = r / exy, rem = r - k * exy, j = rem / ex, i2 = rem - j * ex;
+        const uint32_t gi = e.gaussian;
+        const double c[3] = {in.pos[3 * size_t(gi)], in.pos[3 * size_t(gi) + 1], in.pos[3 * size_t(gi) + 2]};
+        const int64_t lo[3] = {e.lo[0], e.lo[1], e.lo[2]};
+        stampCell(in, gi, g, occ, lo, lo[0] + i2, lo[1] + j, lo[2] + k, c, e.fast ? &e.f : nullptr);
+    }
 }
 
 // The listed large boxes, a block each, its threads over the box's cells.
@@ -605,7 +660,7 @@ __global__ void cloudStampBoxKernel(CloudInput in, GridView g, const float4* __r
         const int64_t ex = b.extent(0), exy = ex * b.extent(1), total = b.cells();
         for (int64_t t = threadIdx.x; t < total; t += blockDim.x) {
             const int64_t k = b.lo[2] + t / exy, r = t % exy;
-            stampCell(in, i, g, occ, b, b.lo[0] + r % ex, b.lo[1] + r / ex, k, c, fast ? &f : nullptr);
+            stampCell(in, i, g, occ, b.lo, b.lo[0] + r % ex, b.lo[1] + r / ex, k, c, fast ? &f : nullptr);
         }
     }
 }
@@ -898,7 +953,7 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     // 3. stamp
     DeviceBuffer bigBuf;
     POOL_ALLOC(bigBuf, size_t(in.count) * 4, pool, st, "cloud scratch");
-    cloudStampKernel<<<(in.count + kCloudBlock - 1) / kCloudBlock, kCloudBlock, 0, st>>>(
+    cloudStampKernel<<<(in.count + kStampBlock - 1) / kStampBlock, kStampBlock, 0, st>>>(
         in, g, frames, v->occupancy, static_cast<uint32_t*>(bigBuf.p), &sc->bigCount);
     cloudStampBoxKernel<<<uint32_t(sms) * 4, kCloudBlock, 0, st>>>(
         in, g, frames, v->occupancy, static_cast<const uint32_t*>(bigBuf.p), &sc->bigCount);

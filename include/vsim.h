@@ -582,6 +582,12 @@ int vsim_cloud_volume_grid(const vsim_cloud_volume* volume, vsim_cloud_grid* out
 int vsim_cloud_volume_read(vsim_cloud_volume* volume, uint8_t* occupancy, size_t cells);
 /* Frees the volume; NULL is accepted. */
 int vsim_cloud_volume_destroy(vsim_cloud_volume* volume);
+/* The fill finds what the outside reaches by rounds of sweeps over the grid
+ * until a round adds nothing, and past a cap of rounds by a union-find over
+ * the empty cells instead; both give the flood's set. Sets the cap for the
+ * whole process (default 24; 0: always the union-find) and returns the
+ * previous one. For tests of both paths; no reference counterpart. */
+uint32_t vsim_cloud_set_flood_rounds(uint32_t rounds);
 
 /* ---- material arithmetic (material.js:101-140, compliance.js:30-109) -- */
 

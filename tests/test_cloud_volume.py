@@ -4,6 +4,11 @@ csrc/cloud_volume.cu) against the host restatement of cloudVolume.js
 (tests/test_host_pins.py): the same grid (dims, origin, h) and the same
 occupancy byte for byte, and the same occupied and filled counts.
 
+The fill's flood runs by rounds of sweeps and, past a cap of rounds, by a
+union-find; the fill cases run both ways (`flood`), and nested shells whose
+inner cavity is reached only by a winding path take several rounds, or the
+union-find when the cap is lower.
+
 Cases: the reference tests' sphere shell at its element sizes, with and
 without the fill; an open capture; anisotropic randomly rotated Gaussians;
 boxes large enough to go to the block-per-Gaussian stamp; degenerate
@@ -25,6 +30,13 @@ def vz(vsimlib, gpu):
     from vsim import voxelize
 
     return voxelize
+
+
+@pytest.fixture(params=["sweeps", "union-find"])
+def flood(request, vz):
+    before = vz.set_flood_rounds(24 if request.param == "sweeps" else 0)
+    yield request.param
+    vz.set_flood_rounds(before)
 
 
 def _cloud_at(points, radius):
@@ -57,17 +69,17 @@ def _same(vz, cloud, element, **kw):
 
 
 @pytest.mark.parametrize("element", [0.013, 0.0086, 0.0065, 0.0043, 0.0032])
-def test_sphere_shell_filled(vz, element):
+def test_sphere_shell_filled(vz, flood, element):
     _same(vz, _cloud_at(_shell(0.05, 6000), 0.0008), element)
 
 
-def test_sphere_shell_unfilled_and_open(vz):
+def test_sphere_shell_unfilled_and_open(vz, flood):
     _same(vz, _cloud_at(_shell(0.05, 6000), 0.0008), 0.005, fill=False)
     g = _same(vz, _cloud_at(_shell(0.05, 6000, 0.75), 0.0008), 0.005)
     assert vz.count_occupied(g) > 0
 
 
-def test_rotated_anisotropic_capture(vz):
+def test_rotated_anisotropic_capture(vz, flood):
     import vsim.scenes as sc
 
     cloud = sc.capture_cloud(60_000, 0.08, seed=11)
@@ -112,7 +124,7 @@ def test_degenerate_gaussians(vz):
 
 
 @pytest.mark.parametrize("padding", [0, 1, 3])
-def test_padding_edges(vz, padding):
+def test_padding_edges(vz, flood, padding):
     # under two cells of padding the stamp's box can leave the grid, and the
     # reference's typed array ignores those indices
     rng = np.random.default_rng(9)
@@ -165,3 +177,47 @@ def test_samples_on_the_surface(vz):
     _same(vz, below, 0.25, fill=False)
     mixed = (pos, exact[1], np.where(rng.random((300, 1)) < 0.5, exact[2], below[2]).astype(np.float32))
     _same(vz, mixed, 0.25)
+
+
+def _cube_shell(half, spacing, hole_axis_sign, hole_half):
+    """Points on the faces of a cube of half-size `half`, `spacing` apart,
+    leaving a square hole of half-width `hole_half` in the middle of the
+    face on x = hole_axis_sign * half."""
+    t = np.arange(-half, half + spacing / 2, spacing)
+    u, v = np.meshgrid(t, t, indexing="ij")
+    u, v = u.ravel(), v.ravel()
+    faces = []
+    for axis in range(3):
+        for sign in (-1.0, 1.0):
+            p = np.zeros((u.size, 3))
+            p[:, axis] = sign * half
+            p[:, (axis + 1) % 3] = u
+            p[:, (axis + 2) % 3] = v
+            if axis == 0 and sign == hole_axis_sign:
+                keep = ~((np.abs(u) < hole_half) & (np.abs(v) < hole_half))
+                p = p[keep]
+            faces.append(p)
+    return np.unique(np.round(np.concatenate(faces), 9), axis=0)
+
+
+@pytest.mark.parametrize("rounds", [24, 2, 1, 0])
+def test_nested_shells_winding_path(vz, rounds):
+    # An outer cube open on +x around an inner cube open on -x: the inner
+    # cavity is outside only by a path that enters the gap, turns round the
+    # inner cube and enters it from the far side, which the sweeps follow
+    # over several rounds; with fewer rounds the union-find decides. A
+    # closed third cube inside stays enclosed and is filled.
+    pts = np.concatenate([_cube_shell(0.12, 0.003, 1.0, 0.02), _cube_shell(0.07, 0.003, -1.0, 0.02),
+                          _cube_shell(0.025, 0.003, 1.0, 0.0)])
+    cloud = _cloud_at(pts, 0.0016)
+    before = vz.set_flood_rounds(rounds)
+    try:
+        g = _same(vz, cloud, 0.004)
+    finally:
+        vz.set_flood_rounds(before)
+    # the innermost cube is filled; the cavity between it and the middle one is not
+    cell, _ = vz.locate(g.origin, g.h, g.dims, 0.0, 0.0, 0.0)
+    assert g.occupancy[cell[0] + g.dims[0] * (cell[1] + g.dims[1] * cell[2])] == 1
+    for probe in ((0.0, 0.05, 0.0), (0.095, 0.0, 0.0), (-0.095, 0.0, 0.0)):
+        cell, _ = vz.locate(g.origin, g.h, g.dims, *probe)
+        assert g.occupancy[cell[0] + g.dims[0] * (cell[1] + g.dims[1] * cell[2])] == 0, probe

@@ -29,6 +29,7 @@
 // components of a graph do not depend on the order edges are merged, so no
 // step's result depends on thread timing.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -61,6 +62,11 @@ constexpr uint32_t kInlineBoxCells = 64;    // larger boxes are stamped by a blo
 constexpr uint32_t kFindLimit = 1u << 22;
 constexpr uint32_t kUniteLimit = 1u << 16;
 constexpr uint32_t kPollEvery = 1024;
+// Rounds of flood sweeps before the union-find takes over (a round that
+// adds nothing ends the flood; each turn of a path the sweeps' axes cannot
+// follow in one round costs a round).
+constexpr uint32_t kFloodRounds = 24;
+std::atomic<uint32_t> floodRounds{kFloodRounds};
 
 struct CloudInput {
     const float* pos;    // xyz per Gaussian
@@ -825,6 +831,200 @@ __global__ void countKernel(const uint8_t* __restrict__ occ, uint32_t cells, uns
 }
 
 // Small device words of one run.
+// ---------------------------------------------------------------- flood --
+// The same set fillEnclosed's flood reaches (cloudVolume.js:321-375): the
+// empty cells joined to an empty face cell by a path of face-adjacent empty
+// cells. The grid's empty cells are packed 32 to a word along x (rows of
+// nw words; bits past nx are clear, so never entered), the face cells seed
+// `reached`, and sweeps spread it: along x within each row (an occluded
+// fill, words carried into their neighbours, up then down), along y and z
+// 32 columns at a time (a word takes its neighbour's reached bits where it
+// is empty, then fills along x within itself). Every step only adds empty
+// cells adjacent to reached ones, and a round of the three sweeps that adds
+// nothing leaves a set closed under adjacency: the flood's set exactly. The
+// rounds are capped; past the cap the union-find below decides instead.
+
+struct Words {
+    uint32_t nw;    // words per row
+    uint32_t rows;  // ny * nz
+    uint32_t ny, nz;
+};
+
+// Seeds g spread through the set bits of p towards higher (Up) or lower
+// (Down) bit positions: Kogge-Stone occluded fill.
+__device__ __forceinline__ uint32_t fillUp(uint32_t g, uint32_t p) {
+    g |= p & (g << 1);
+    p &= p << 1;
+    g |= p & (g << 2);
+    p &= p << 2;
+    g |= p & (g << 4);
+    p &= p << 4;
+    g |= p & (g << 8);
+    p &= p << 8;
+    return g | (p & (g << 16));
+}
+
+__device__ __forceinline__ uint32_t fillDown(uint32_t g, uint32_t p) {
+    g |= p & (g >> 1);
+    p &= p >> 1;
+    g |= p & (g >> 2);
+    p &= p >> 2;
+    g |= p & (g >> 4);
+    p &= p >> 4;
+    g |= p & (g >> 8);
+    p &= p >> 8;
+    return g | (p & (g >> 16));
+}
+
+// A thread per word: its 32 cells' emptiness, and as reached those on a face
+// of the grid.
+__global__ void packEmptyKernel(const uint8_t* __restrict__ occ, Dims d, Words w, uint32_t* __restrict__ empty,
+                                uint32_t* __restrict__ reached) {
+    const uint32_t total = w.rows * w.nw;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const uint32_t row = t / w.nw, word = t - row * w.nw;
+        const uint32_t j = row % d.ny, k = row / d.ny;
+        const uint32_t first = word * 32, count = min(32u, d.nx - first);
+        const uint8_t* cells = occ + size_t(row) * d.nx + first;
+        uint32_t e = 0;
+        for (uint32_t b = 0; b < count; b++) e |= uint32_t(cells[b] == 0) << b;
+        uint32_t face = (j == 0 || k == 0 || j == d.ny - 1 || k == d.nz - 1) ? 0xffffffffu : 0u;
+        if (word == 0) face |= 1u;
+        if (word == w.nw - 1) face |= 1u << ((d.nx - 1) % 32);
+        empty[t] = e;
+        reached[t] = e & face;
+    }
+}
+
+// Along x: a thread per row, up then down, the edge bit carried between
+// neighbouring words.
+__global__ void sweepXKernel(Words w, const uint32_t* __restrict__ empty, uint32_t* __restrict__ reached,
+                             uint32_t* __restrict__ changed) {
+    bool grew = false;
+    for (uint32_t row = blockIdx.x * blockDim.x + threadIdx.x; row < w.rows; row += gridDim.x * blockDim.x) {
+        uint32_t* r = reached + size_t(row) * w.nw;
+        const uint32_t* e = empty + size_t(row) * w.nw;
+        uint32_t carry = 0;
+        for (uint32_t q = 0; q < w.nw; q++) {
+            const uint32_t was = r[q], p = e[q];
+            const uint32_t g = fillUp(was | (carry & p & 1u), p);
+            carry = g >> 31;
+            if (g != was) {
+                r[q] = g;
+                grew = true;
+            }
+        }
+        carry = 0;
+        for (uint32_t q = w.nw; q-- > 0;) {
+            const uint32_t was = r[q], p = e[q];
+            const uint32_t g = fillDown(was | ((carry << 31) & p), p);
+            carry = g & 1u;
+            if (g != was) {
+                r[q] = g;
+                grew = true;
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, grew) && (threadIdx.x & 31) == 0) atomicOr(changed, 1u);
+}
+
+// Along y (a line per word column of an xz plane: stride nw, lines nz) or
+// z (a line per word column of an xy row: stride nw ny, lines ny), a warp per
+// line. Along a line a word takes its predecessor's reached bits where it
+// is empty, x -> r | (e & x): maps of that form compose associatively,
+// (a2, b2) after (a1, b1) = (a2 | (b2 & a1), b2 & b1), so each lane folds its
+// segment of the line into one map, a warp scan gives every lane the
+// reached bits entering its segment, and a second walk applies them, each
+// word also filled along x within itself. Up the line, then down.
+__device__ void sweepLineWay(bool up, uint32_t lane, uint32_t length, uint32_t seg, size_t base, uint32_t stride,
+                             const uint32_t* __restrict__ empty, uint32_t* __restrict__ reached, bool& grew) {
+    constexpr unsigned kAll = 0xffffffffu;
+    // lane l holds steps [l seg, (l + 1) seg), walked upwards or downwards;
+    // the lanes come in lane order up, in reverse lane order down
+    const uint32_t s0 = min(lane * seg, length), s1 = min(s0 + seg, length);
+    auto at = [&](uint32_t s) { return base + size_t(s) * stride; };
+    uint32_t a = 0, b = ~0u;
+    if (up) {
+        for (uint32_t s = s0; s < s1; s++) {
+            const uint32_t e = empty[at(s)];
+            a = reached[at(s)] | (e & a);
+            b &= e;
+        }
+    } else {
+        for (uint32_t s = s1; s-- > s0;) {
+            const uint32_t e = empty[at(s)];
+            a = reached[at(s)] | (e & a);
+            b &= e;
+        }
+    }
+    // inclusive scan in walk order (lane order up, reverse lane order down)
+#pragma unroll
+    for (uint32_t d = 1; d < 32; d <<= 1) {
+        const uint32_t pa = up ? __shfl_up_sync(kAll, a, d) : __shfl_down_sync(kAll, a, d);
+        const uint32_t pb = up ? __shfl_up_sync(kAll, b, d) : __shfl_down_sync(kAll, b, d);
+        if (up ? lane >= d : lane + d < 32) {
+            a |= b & pa;
+            b &= pb;
+        }
+    }
+    const uint32_t before = up ? __shfl_up_sync(kAll, a, 1) : __shfl_down_sync(kAll, a, 1);
+    uint32_t carry = (up ? lane > 0 : lane < 31) ? before : 0u;
+    auto apply = [&](uint32_t s) {
+        const uint32_t was = reached[at(s)], e = empty[at(s)];
+        const uint32_t g = fillDown(fillUp(was | (e & carry), e), e);
+        carry = g;
+        if (g != was) {
+            reached[at(s)] = g;
+            grew = true;
+        }
+    };
+    if (up) {
+        for (uint32_t s = s0; s < s1; s++) apply(s);
+    } else {
+        for (uint32_t s = s1; s-- > s0;) apply(s);
+    }
+}
+
+__global__ void sweepLineKernel(Words w, uint32_t lines, uint32_t length, uint32_t stride, uint32_t lineStride,
+                                const uint32_t* __restrict__ empty, uint32_t* __restrict__ reached,
+                                uint32_t* __restrict__ changed) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t seg = (length + 31) / 32;
+    bool grew = false;
+    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < lines * w.nw; t += warps) {
+        const uint32_t line = t / w.nw, word = t - line * w.nw;
+        const size_t base = size_t(line) * lineStride + word;
+        sweepLineWay(true, lane, length, seg, base, stride, empty, reached, grew);
+        __syncwarp();
+        sweepLineWay(false, lane, length, seg, base, stride, empty, reached, grew);
+        __syncwarp();
+    }
+    if (__any_sync(0xffffffffu, grew) && lane == 0) atomicOr(changed, 1u);
+}
+
+// cloudVolume.js:367-374 from the words: every empty cell not reached
+// becomes material; *filled counts them. A thread per word.
+__global__ void fillFromWordsKernel(uint8_t* __restrict__ occ, Dims d, Words w, const uint32_t* __restrict__ empty,
+                                    const uint32_t* __restrict__ reached, unsigned long long* __restrict__ filled) {
+    unsigned long long mine = 0;
+    const uint32_t total = w.rows * w.nw;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        uint32_t enclosed = empty[t] & ~reached[t];
+        if (!enclosed) continue;
+        mine += __popc(enclosed);
+        const uint32_t row = t / w.nw, word = t - row * w.nw;
+        uint8_t* cells = occ + size_t(row) * d.nx + word * 32;
+        while (enclosed) {
+            const int b = __ffs(enclosed) - 1;
+            enclosed &= enclosed - 1;
+            cells[b] = 1;
+        }
+    }
+    const unsigned long long total2 = blockSum(mine);
+    if (threadIdx.x == 0 && total2) atomicAdd(filled, total2);
+}
+
 struct CloudScalars {
     unsigned long long keys[6];   // the bounds' first pass
     unsigned long long exact[6];  // the exact extremes
@@ -833,7 +1033,7 @@ struct CloudScalars {
     uint32_t nan;
     uint32_t err;
     uint32_t bigCount;
-    uint32_t pad;
+    uint32_t changed;  // a flood round added cells
 };
 
 // Scratch comes from a stream-ordered memory pool of this library's own, one
@@ -975,11 +1175,42 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
             neighbourhoodKernel<true><<<grid, kCloudBlock, 0, st>>>(cur, other, d);
             std::swap(cur, other);
         }
-        CK(cudaMemsetAsync(reached, 0, n, st), "cloud fill");
-        labelRunsKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, d);
-        labelMergeKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, d, &sc->err);
-        markFaceRootsKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, reached, d, &sc->err);
-        fillEnclosedKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, reached, n, &sc->filled, &sc->err);
+        // The flood by sweeps over packed words, to a round that adds
+        // nothing; past the cap of rounds the union-find decides.
+        const Words W{(d.nx + 31) / 32, d.ny * d.nz, d.ny, d.nz};
+        const size_t words = size_t(W.rows) * W.nw;
+        DeviceBuffer wordsBuf;
+        POOL_ALLOC(wordsBuf, words * 8, pool, st, "cloud fill scratch");
+        auto* emptyW = static_cast<uint32_t*>(wordsBuf.p);
+        uint32_t* reachedW = emptyW + words;
+        packEmptyKernel<<<streamGrid(words, sms), kCloudBlock, 0, st>>>(cur, d, W, emptyW, reachedW);
+        // a warp per line, four to a block
+        auto lineBlocks = [](uint64_t lines) { return uint32_t(std::max<uint64_t>(1, (lines + 3) / 4)); };
+        bool converged = false;
+        const uint32_t rounds = floodRounds.load();
+        for (uint32_t round = 0; round < rounds && !converged; round++) {
+            CK(cudaMemsetAsync(&sc->changed, 0, sizeof(uint32_t), st), "cloud flood");
+            sweepXKernel<<<uint32_t((W.rows + 127) / 128), 128, 0, st>>>(W, emptyW, reachedW, &sc->changed);
+            sweepLineKernel<<<lineBlocks(uint64_t(d.nz) * W.nw), 128, 0, st>>>(W, d.nz, d.ny, W.nw, W.nw * d.ny,
+                                                                                emptyW, reachedW, &sc->changed);
+            sweepLineKernel<<<lineBlocks(uint64_t(d.ny) * W.nw), 128, 0, st>>>(W, d.ny, d.nz, W.nw * d.ny, W.nw,
+                                                                                emptyW, reachedW, &sc->changed);
+            CK(cudaGetLastError(), "cloud flood");
+            uint32_t changed = 1;
+            CK(cudaMemcpyAsync(&changed, &sc->changed, sizeof changed, cudaMemcpyDeviceToHost, st), "cloud flood");
+            CK(cudaStreamSynchronize(st), "cloud flood");
+            converged = changed == 0;
+        }
+        if (converged) {
+            fillFromWordsKernel<<<streamGrid(words, sms), kCloudBlock, 0, st>>>(cur, d, W, emptyW, reachedW,
+                                                                                &sc->filled);
+        } else {
+            CK(cudaMemsetAsync(reached, 0, n, st), "cloud fill");
+            labelRunsKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, d);
+            labelMergeKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, d, &sc->err);
+            markFaceRootsKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, reached, d, &sc->err);
+            fillEnclosedKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, reached, n, &sc->filled, &sc->err);
+        }
         for (uint32_t p = 0; p < o.seal; p++) {
             neighbourhoodKernel<false><<<grid, kCloudBlock, 0, st>>>(cur, other, d);
             std::swap(cur, other);
@@ -1128,5 +1359,7 @@ int vsim_cloud_volume_destroy(vsim_cloud_volume* volume) {
     destroyVolume(volume);
     return VSIM_OK;
 }
+
+uint32_t vsim_cloud_set_flood_rounds(uint32_t rounds) { return floodRounds.exchange(rounds); }
 
 }  // extern "C"

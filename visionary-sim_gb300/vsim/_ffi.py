@@ -230,6 +230,7 @@ SIGNATURES = {
     "vsim_cloud_volume_grid": (C.c_int, [_P, C.POINTER(CloudGrid)]),
     "vsim_cloud_volume_read": (C.c_int, [_P, C.POINTER(C.c_uint8), _SZ]),
     "vsim_cloud_volume_destroy": (C.c_int, [_P]),
+    "vsim_cloud_set_flood_rounds": (C.c_uint32, [C.c_uint32]),
     "vsim_radix_sort_u32_noalloc": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P]),
     "vsim_profile_frame": (C.c_int, [_P, C.c_uint32, C.c_int, _F, C.POINTER(Profile)]),
     "vsim_color_counts": (C.c_int, [_P, _U]),

@@ -340,6 +340,16 @@ def voxelize_cloud(positions, rotations, scales, element_size: float, padding: i
     return grid
 
 
+def set_flood_rounds(rounds: int) -> int:
+    """Caps the rounds of flood sweeps `voxelize_cloud_on_device`'s fill runs
+    before its union-find decides (vsim_cloud_set_flood_rounds; 0: always the
+    union-find), process-wide; returns the previous cap. Both paths give the
+    flood's set; this is for testing each."""
+    from . import _ffi
+
+    return int(_ffi.lib().vsim_cloud_set_flood_rounds(int(rounds)))
+
+
 def voxelize_cloud_on_device(positions, rotations, scales, element_size: float, padding: int = DEFAULT_PADDING,
                              sigma: float = CLOUD_SIGMA, seal: int = CLOUD_SEAL, fill: bool = True,
                              stats: dict | None = None) -> OccupancyGrid:

@@ -18,13 +18,16 @@
 //      cells of its box against the ellipsoid (stampCloud, :138-178), box
 //      edges and samples decided in float unless too close to call; a box
 //      of more than kInlineBoxCells cells is handed to a block instead;
-//   4. seal and fill (:291-306): 6-neighbourhood dilations, the fill, as
-//      many erosions, the stamp put back. The reference fills by flooding
-//      the empty cells from the grid's faces (fillEnclosed, :321-375); the
-//      cells a flood reaches are exactly the face-connected components of
-//      empty cells that touch a face, found here by a concurrent union-find
-//      (x runs seeded by warp ballots, links by atomicMin on roots, path
-//      halving by plain stores) instead of a serial flood.
+//   4. seal and fill (:291-306) on the cells packed 32 to a word along x:
+//      6-neighbourhood dilations, the fill, as many erosions, the stamp put
+//      back, the words written out as bytes once. The reference fills by
+//      flooding the empty cells from the grid's faces (fillEnclosed,
+//      :321-375); here the flood's set is reached by rounds of sweeps over
+//      the words (an occluded fill along x, warp scans along y and z) to a
+//      round that adds nothing, or, past a cap of rounds, found as the
+//      face-connected components of empty cells that touch a face by a
+//      concurrent union-find (x runs seeded by warp ballots, links by
+//      atomicMin on roots, path halving by plain stores).
 // Marking is an OR (a cell is set by any Gaussian that reaches it), and the
 // components of a graph do not depend on the order edges are merged, so no
 // step's result depends on thread timing.
@@ -675,31 +678,6 @@ struct Dims {
     uint32_t nx, ny, nz, cells;
 };
 
-// voxelize.js:402-435 (neighbourhoodPass): a clear cell with a set face
-// neighbour becomes set (dilate), a set cell with a clear one becomes clear
-// (erode); outside the grid counts as clear.
-template <bool DILATE>
-__global__ void neighbourhoodKernel(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, Dims d) {
-    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < d.cells; idx += gridDim.x * blockDim.x) {
-        const uint32_t i = idx % d.nx, j = (idx / d.nx) % d.ny, k = idx / (d.nx * d.ny);
-        bool result = src[idx] == 1;
-        if (result != DILATE) {
-            const uint32_t plane = d.nx * d.ny;
-            const uint8_t n[6] = {i + 1 < d.nx ? src[idx + 1] : uint8_t(0), i > 0 ? src[idx - 1] : uint8_t(0),
-                                  j + 1 < d.ny ? src[idx + d.nx] : uint8_t(0), j > 0 ? src[idx - d.nx] : uint8_t(0),
-                                  k + 1 < d.nz ? src[idx + plane] : uint8_t(0), k > 0 ? src[idx - plane] : uint8_t(0)};
-            for (int q = 0; q < 6; q++)
-                if (DILATE ? n[q] == 1 : n[q] == 0) result = DILATE;
-        }
-        dst[idx] = result ? 1 : 0;
-    }
-}
-
-// cloudVolume.js:302-304: the stamp put back on top.
-__global__ void orKernel(uint8_t* __restrict__ occ, const uint8_t* __restrict__ stamp, uint32_t cells) {
-    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < cells; idx += gridDim.x * blockDim.x)
-        occ[idx] |= stamp[idx];
-}
 
 // The root of a's tree. Labels only decrease along a path, so the walk ends;
 // each step points a at its grandparent (path halving). A plain store is
@@ -876,18 +854,56 @@ __device__ __forceinline__ uint32_t fillDown(uint32_t g, uint32_t p) {
     return g | (p & (g >> 16));
 }
 
-// A thread per word: its 32 cells' emptiness, and as reached those on a face
-// of the grid.
-__global__ void packEmptyKernel(const uint8_t* __restrict__ occ, Dims d, Words w, uint32_t* __restrict__ empty,
+// The valid bits of word `word` of a row (cells past nx are clear).
+__device__ __forceinline__ uint32_t validBits(const Dims& d, uint32_t word) {
+    const uint32_t count = min(32u, d.nx - word * 32);
+    return count == 32 ? 0xffffffffu : (1u << count) - 1u;
+}
+
+// A thread per word: bit b of word w of a row set where cell 32 w + b is.
+__global__ void packCellsKernel(const uint8_t* __restrict__ occ, Dims d, Words w, uint32_t* __restrict__ bits) {
+    const uint32_t total = w.rows * w.nw;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const uint32_t row = t / w.nw, word = t - row * w.nw;
+        const uint32_t first = word * 32, count = min(32u, d.nx - first);
+        const uint8_t* cells = occ + size_t(row) * d.nx + first;
+        uint32_t m = 0;
+        for (uint32_t b = 0; b < count; b++) m |= uint32_t(cells[b] != 0) << b;
+        bits[t] = m;
+    }
+}
+
+// voxelize.js:402-435 (neighbourhoodPass) on packed words, a thread per
+// word: a clear cell with a set face neighbour becomes set (dilate), a set
+// cell with a clear one becomes clear (erode); outside the grid counts as
+// clear. The x neighbours are the word shifted by one, the edge bits taken
+// from the neighbouring words of the row.
+template <bool DILATE>
+__global__ void neighbourhoodWordsKernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, Dims d, Words w) {
+    const uint32_t total = w.rows * w.nw, plane = w.nw * d.ny;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const uint32_t row = t / w.nw, word = t - row * w.nw;
+        const uint32_t j = row % d.ny, k = row / d.ny;
+        const uint32_t c = src[t];
+        const uint32_t left = word > 0 ? src[t - 1] : 0u, right = word + 1 < w.nw ? src[t + 1] : 0u;
+        const uint32_t n[6] = {(c << 1) | (left >> 31), (c >> 1) | (right << 31), j > 0 ? src[t - w.nw] : 0u,
+                               j + 1 < d.ny ? src[t + w.nw] : 0u, k > 0 ? src[t - plane] : 0u,
+                               k + 1 < d.nz ? src[t + plane] : 0u};
+        uint32_t out = c;
+        for (int q = 0; q < 6; q++) out = DILATE ? (out | n[q]) : (out & n[q]);
+        dst[t] = out & validBits(d, word);
+    }
+}
+
+// A thread per word: the empty cells of the sealed grid, and as reached
+// those on a face of the grid (the flood's seeds, cloudVolume.js:344-352).
+__global__ void seedFloodKernel(const uint32_t* __restrict__ cur, Dims d, Words w, uint32_t* __restrict__ empty,
                                 uint32_t* __restrict__ reached) {
     const uint32_t total = w.rows * w.nw;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         const uint32_t row = t / w.nw, word = t - row * w.nw;
         const uint32_t j = row % d.ny, k = row / d.ny;
-        const uint32_t first = word * 32, count = min(32u, d.nx - first);
-        const uint8_t* cells = occ + size_t(row) * d.nx + first;
-        uint32_t e = 0;
-        for (uint32_t b = 0; b < count; b++) e |= uint32_t(cells[b] == 0) << b;
+        const uint32_t e = ~cur[t] & validBits(d, word);
         uint32_t face = (j == 0 || k == 0 || j == d.ny - 1 || k == d.nz - 1) ? 0xffffffffu : 0u;
         if (word == 0) face |= 1u;
         if (word == w.nw - 1) face |= 1u << ((d.nx - 1) % 32);
@@ -1003,26 +1019,61 @@ __global__ void sweepLineKernel(Words w, uint32_t lines, uint32_t length, uint32
     if (__any_sync(0xffffffffu, grew) && lane == 0) atomicOr(changed, 1u);
 }
 
-// cloudVolume.js:367-374 from the words: every empty cell not reached
-// becomes material; *filled counts them. A thread per word.
-__global__ void fillFromWordsKernel(uint8_t* __restrict__ occ, Dims d, Words w, const uint32_t* __restrict__ empty,
-                                    const uint32_t* __restrict__ reached, unsigned long long* __restrict__ filled) {
+// cloudVolume.js:367-374 on the words: every empty cell not reached becomes
+// material; *filled counts them. A thread per word.
+__global__ void encloseWordsKernel(uint32_t* __restrict__ cur, Words w, const uint32_t* __restrict__ empty,
+                                   const uint32_t* __restrict__ reached, unsigned long long* __restrict__ filled) {
     unsigned long long mine = 0;
     const uint32_t total = w.rows * w.nw;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-        uint32_t enclosed = empty[t] & ~reached[t];
+        const uint32_t enclosed = empty[t] & ~reached[t];
         if (!enclosed) continue;
         mine += __popc(enclosed);
-        const uint32_t row = t / w.nw, word = t - row * w.nw;
-        uint8_t* cells = occ + size_t(row) * d.nx + word * 32;
-        while (enclosed) {
-            const int b = __ffs(enclosed) - 1;
-            enclosed &= enclosed - 1;
-            cells[b] = 1;
+        cur[t] |= enclosed;
+    }
+    const unsigned long long sum = blockSum(mine);
+    if (threadIdx.x == 0 && sum) atomicAdd(filled, sum);
+}
+
+// The cells of a | b as bytes (0 or 1) into occ, a thread per 16 cells of
+// the byte grid (one 16-byte store where occ is 16-byte aligned, bytes
+// otherwise); *occupied counts them when given.
+__global__ void unpackCellsKernel(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, Dims d, Words w,
+                                  uint8_t* __restrict__ occ, unsigned long long* __restrict__ occupied) {
+    unsigned long long mine = 0;
+    const uint32_t chunks = (d.cells + 15) / 16;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < chunks; q += gridDim.x * blockDim.x) {
+        const uint32_t first = q * 16, count = min(16u, d.cells - first);
+        uint32_t row = first / d.nx, i = first - row * d.nx;
+        uint32_t at = ~0u, m = 0;
+        uint32_t packed[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (uint32_t c = 0; c < 16; c++) {
+            if (c < count) {
+                const uint32_t word = row * w.nw + (i >> 5);
+                if (word != at) {
+                    at = word;
+                    m = a[word] | (b ? b[word] : 0u);
+                }
+                const uint32_t bit = (m >> (i & 31)) & 1u;
+                packed[c >> 2] |= bit << (8 * (c & 3));
+                mine += bit;
+                if (++i == d.nx) {
+                    i = 0;
+                    row++;
+                }
+            }
+        }
+        if (count == 16 && (reinterpret_cast<uintptr_t>(occ) & 15u) == 0) {
+            *reinterpret_cast<uint4*>(occ + first) = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        } else {
+            for (uint32_t c = 0; c < count; c++) occ[first + c] = uint8_t((packed[c >> 2] >> (8 * (c & 3))) & 1u);
         }
     }
-    const unsigned long long total2 = blockSum(mine);
-    if (threadIdx.x == 0 && total2) atomicAdd(filled, total2);
+    if (occupied) {
+        const unsigned long long sum = blockSum(mine);
+        if (threadIdx.x == 0 && sum) atomicAdd(occupied, sum);
+    }
 }
 
 struct CloudScalars {
@@ -1162,28 +1213,32 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     // 4. seal and fill
     const uint32_t grid = streamGrid(n, sms);
     if (o.fill) {
-        // stamp copy, a ping-pong buffer, labels, reached flags
-        DeviceBuffer work;
-        POOL_ALLOC(work, size_t(n) * 7 + 64, pool, st, "cloud fill scratch");
-        auto* labels = static_cast<uint32_t*>(work.p);
-        uint8_t* stamp = reinterpret_cast<uint8_t*>(labels + n);
-        uint8_t* other = stamp + n;
-        uint8_t* reached = other + n;
-        CK(cudaMemcpyAsync(stamp, v->occupancy, n, cudaMemcpyDeviceToDevice, st), "cloud fill");
-        uint8_t* cur = v->occupancy;
-        for (uint32_t p = 0; p < o.seal; p++) {
-            neighbourhoodKernel<true><<<grid, kCloudBlock, 0, st>>>(cur, other, d);
-            std::swap(cur, other);
-        }
-        // The flood by sweeps over packed words, to a round that adds
-        // nothing; past the cap of rounds the union-find decides.
+        // The seal and fill on the cells packed 32 to a word along x: the
+        // stamp packed once, `seal` dilations, the flood, the enclosed cells
+        // set, `seal` erosions, the stamp put back as the words are written
+        // out as bytes once.
         const Words W{(d.nx + 31) / 32, d.ny * d.nz, d.ny, d.nz};
         const size_t words = size_t(W.rows) * W.nw;
         DeviceBuffer wordsBuf;
-        POOL_ALLOC(wordsBuf, words * 8, pool, st, "cloud fill scratch");
-        auto* emptyW = static_cast<uint32_t*>(wordsBuf.p);
+        POOL_ALLOC(wordsBuf, words * 5 * sizeof(uint32_t), pool, st, "cloud fill scratch");
+        uint32_t* stampW = static_cast<uint32_t*>(wordsBuf.p);
+        uint32_t* cur = stampW + words;
+        uint32_t* other = cur + words;
+        uint32_t* emptyW = other + words;
         uint32_t* reachedW = emptyW + words;
-        packEmptyKernel<<<streamGrid(words, sms), kCloudBlock, 0, st>>>(cur, d, W, emptyW, reachedW);
+        const uint32_t wordGrid = streamGrid(words, sms);
+        packCellsKernel<<<wordGrid, kCloudBlock, 0, st>>>(v->occupancy, d, W, stampW);
+        const uint32_t* src = stampW;
+        for (uint32_t p = 0; p < o.seal; p++) {
+            neighbourhoodWordsKernel<true><<<wordGrid, kCloudBlock, 0, st>>>(src, cur, d, W);
+            src = cur;
+            std::swap(cur, other);
+        }
+        if (src != stampW) std::swap(cur, other);  // cur: the sealed grid
+        else CK(cudaMemcpyAsync(cur, stampW, words * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st), "cloud fill");
+        // The flood by sweeps, to a round that adds nothing; past the cap of
+        // rounds the union-find decides.
+        seedFloodKernel<<<wordGrid, kCloudBlock, 0, st>>>(cur, d, W, emptyW, reachedW);
         // a warp per line, four to a block
         auto lineBlocks = [](uint64_t lines) { return uint32_t(std::max<uint64_t>(1, (lines + 3) / 4)); };
         bool converged = false;
@@ -1202,26 +1257,34 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
             converged = changed == 0;
         }
         if (converged) {
-            fillFromWordsKernel<<<streamGrid(words, sms), kCloudBlock, 0, st>>>(cur, d, W, emptyW, reachedW,
-                                                                                &sc->filled);
+            encloseWordsKernel<<<wordGrid, kCloudBlock, 0, st>>>(cur, W, emptyW, reachedW, &sc->filled);
         } else {
+            // the sealed grid as bytes, filled by the union-find, packed back
+            DeviceBuffer work;
+            const size_t sealedAt = (size_t(n) * 4 + 15) / 16 * 16;
+            POOL_ALLOC(work, sealedAt + size_t(n) * 2 + 64, pool, st, "cloud fill scratch");
+            auto* labels = static_cast<uint32_t*>(work.p);
+            uint8_t* sealed = static_cast<uint8_t*>(work.p) + sealedAt;
+            uint8_t* reached = sealed + n;
+            unpackCellsKernel<<<streamGrid((n + 15) / 16, sms), kCloudBlock, 0, st>>>(cur, nullptr, d, W, sealed,
+                                                                                       nullptr);
             CK(cudaMemsetAsync(reached, 0, n, st), "cloud fill");
-            labelRunsKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, d);
-            labelMergeKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, d, &sc->err);
-            markFaceRootsKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, reached, d, &sc->err);
-            fillEnclosedKernel<<<grid, kCloudBlock, 0, st>>>(cur, labels, reached, n, &sc->filled, &sc->err);
+            labelRunsKernel<<<grid, kCloudBlock, 0, st>>>(sealed, labels, d);
+            labelMergeKernel<<<grid, kCloudBlock, 0, st>>>(sealed, labels, d, &sc->err);
+            markFaceRootsKernel<<<grid, kCloudBlock, 0, st>>>(sealed, labels, reached, d, &sc->err);
+            fillEnclosedKernel<<<grid, kCloudBlock, 0, st>>>(sealed, labels, reached, n, &sc->filled, &sc->err);
+            packCellsKernel<<<wordGrid, kCloudBlock, 0, st>>>(sealed, d, W, cur);
+            CK(cudaStreamSynchronize(st), "cloud fill");  // before `work` is freed
         }
         for (uint32_t p = 0; p < o.seal; p++) {
-            neighbourhoodKernel<false><<<grid, kCloudBlock, 0, st>>>(cur, other, d);
+            neighbourhoodWordsKernel<false><<<wordGrid, kCloudBlock, 0, st>>>(cur, other, d, W);
             std::swap(cur, other);
         }
-        if (cur != v->occupancy)
-            CK(cudaMemcpyAsync(v->occupancy, cur, n, cudaMemcpyDeviceToDevice, st), "cloud fill");
-        orKernel<<<grid, kCloudBlock, 0, st>>>(v->occupancy, stamp, n);
+        unpackCellsKernel<<<streamGrid((n + 15) / 16, sms), kCloudBlock, 0, st>>>(cur, stampW, d, W, v->occupancy,
+                                                                                   &sc->occupied);
         CK(cudaGetLastError(), "cloud fill");
-        countKernel<<<grid, kCloudBlock, 0, st>>>(v->occupancy, n, &sc->occupied);
         CK(cudaMemcpyAsync(&got, sc, sizeof got, cudaMemcpyDeviceToHost, st), "cloud fill");
-        CK(cudaStreamSynchronize(st), "cloud fill");  // before `work` is freed
+        CK(cudaStreamSynchronize(st), "cloud fill");  // before the words are freed
     } else {
         countKernel<<<grid, kCloudBlock, 0, st>>>(v->occupancy, n, &sc->occupied);
         CK(cudaMemcpyAsync(&got, sc, sizeof got, cudaMemcpyDeviceToHost, st), "cloud stamp");

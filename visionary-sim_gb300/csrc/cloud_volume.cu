@@ -86,6 +86,7 @@ struct GridView {
     double h;
     float invH;  // float(1 / h), 0 outside [2^-40, 2^40]
     float hF;    // float(h)
+    float originF[3];    // float(origin)
     float originMag[3];  // max(|float(origin)|, 2^-100)
     bool floatBound;     // h in [2^-30, 2^30] and |origin| <= 2^40 on every axis
     uint32_t cells;
@@ -174,10 +175,10 @@ __device__ __forceinline__ unsigned long long warpMax64(unsigned long long v) {
 //
 // The estimate, sqrtf of the float sum of the float products' squares, is
 // within 2^-21 of V8's hypot of the double products (relative): the float
-// products are within 2^-22.9 of the double ones (the radius and the product
-// each rounded once), their squares and two sums add under 2^-22, the square
-// root halves that, and V8's own evaluation is within 2^-50 of the exact
-// hypot. kReachSlack, 8 times that, brackets the exact reach:
+// products are within 2^-22.4 of the double ones (float(sigma), the radius
+// and the product each rounded once), their squares and two sums add under
+// 2^-21, the square root halves that, and V8's own evaluation is within
+// 2^-50 of the exact hypot. kReachSlack, 8 times that, brackets the exact reach:
 //   hf (1 - kReachSlack) <= reach <= hf (1 + kReachSlack),
 // both products rounded in double well inside the slack. It holds while
 // every nonzero product lies in [2^-60, 2^60] (squares and sums stay normal
@@ -195,53 +196,69 @@ __device__ float reachEstimate(const float col[9], const float r[3], int a) {
     return sqrtf(sum);
 }
 
-// The radii sigma * scale in double, as cloudVolume.js:196-199 computes them,
-// and as floats for the estimate (NaN where out of its range).
-__device__ void radiiOf(const CloudInput& in, uint32_t i, double r[3], float rf[3]) {
+// The radii float(sigma) * scale for the estimate (within 2^-23 of the
+// double sigma * scale of cloudVolume.js:196-199), NaN where out of its
+// range.
+__device__ void radiiOf(const CloudInput& in, uint32_t i, float rf[3]) {
     for (int a = 0; a < 3; a++) {
-        r[a] = in.sigma * double(in.scale[3 * size_t(i) + a]);
-        const double m = fabs(r[a]);
-        rf[a] = (r[a] == 0.0 || (m >= 0x1p-100 && m <= 0x1p100)) ? float(r[a]) : CUDART_NAN_F;
+        const float r = in.sigmaF * in.scale[3 * size_t(i) + a];
+        const float m = fabsf(r);
+        rf[a] = (r == 0.0f || (m >= 0x1p-100f && m <= 0x1p100f)) ? r : CUDART_NAN_F;
     }
 }
 
+// Floats ordered as unsigned integers (as orderedKey for doubles).
+__device__ __forceinline__ uint32_t orderedKey32(float v) {
+    const uint32_t u = __float_as_uint(v);
+    return (u >> 31) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ float fromOrderedKey32(uint32_t k) {
+    return __uint_as_float((k >> 31) ? (k & 0x7fffffffu) : ~k);
+}
+
 // cloudVolume.js:219-234 (materialBounds), first pass: per axis the smallest
-// upper bound on position - reach (keys[0..2]) and the largest lower bound on
-// position + reach (keys[3..5]) over all Gaussians, from the reach estimates;
-// exact values where a Gaussian has no estimate. A NaN anywhere raises *nan
-// (Math.min and Math.max then give NaN). Fills `frames`.
-__global__ void cloudBoundsKernel(CloudInput in, unsigned long long* __restrict__ keys, uint32_t* __restrict__ nan,
+// float upper bound on position - reach (keys[0..2]) and the largest float
+// lower bound on position + reach (keys[3..5]) over all Gaussians, from the
+// reach estimates with directed roundings (the exact value rounded outwards
+// where a Gaussian has no estimate). A NaN anywhere raises *nan (Math.min
+// and Math.max then give NaN). Fills `frames`.
+__global__ void cloudBoundsKernel(CloudInput in, uint32_t* __restrict__ keys, uint32_t* __restrict__ nan,
                                   float4* __restrict__ frames) {
-    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
+    uint32_t lo[3] = {~0u, ~0u, ~0u}, hi[3] = {0, 0, 0};
     bool sawNan = false;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < in.count; i += gridDim.x * blockDim.x) {
         Ellipsoid e;
         frameOf(in, i, e);
         float col[9], rf[3];
         for (int q = 0; q < 9; q++) col[q] = float(e.col[q]);
-        radiiOf(in, i, e.radius, rf);
+        radiiOf(in, i, rf);
         for (int a = 0; a < 3; a++) {
-            const double p = in.pos[3 * size_t(i) + a];
+            const float p = in.pos[3 * size_t(i) + a];
             float hf = reachEstimate(col, rf, a);
             if (!isfinite(p)) hf = CUDART_NAN_F;
             frames[3 * size_t(i) + a] = make_float4(col[3 * a], col[3 * a + 1], col[3 * a + 2], hf);
-            double l, u;
+            float l, u;
             if (isnan(hf)) {
                 const double half = hypotV8(e.col[a] * e.radius[0], e.col[3 + a] * e.radius[1], e.col[6 + a] * e.radius[2]);
-                l = p - half;
-                u = p + half;
+                const double ld = double(p) - half, ud = double(p) + half;
+                sawNan |= isnan(ld) || isnan(ud);
+                l = __double2float_ru(ld);
+                u = __double2float_rd(ud);
             } else {
-                l = p - double(hf) * (1.0 - kReachSlack);  // >= position - reach
-                u = p + double(hf) * (1.0 - kReachSlack);  // <= position + reach
+                const float narrow = __fmul_rd(hf, float(1.0 - kReachSlack));  // <= reach
+                l = __fsub_ru(p, narrow);                                     // >= position - reach
+                u = __fadd_rd(p, narrow);                                     // <= position + reach
             }
-            sawNan |= isnan(l) || isnan(u);
-            lo[a] = min(lo[a], orderedKey(l));
-            hi[a] = max(hi[a], orderedKey(u));
+            lo[a] = min(lo[a], orderedKey32(l));
+            hi[a] = max(hi[a], orderedKey32(u));
         }
     }
     for (int a = 0; a < 3; a++) {
-        lo[a] = warpMin64(lo[a]);
-        hi[a] = warpMax64(hi[a]);
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = min(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = max(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
     }
     sawNan = __any_sync(0xffffffffu, sawNan);
     if ((threadIdx.x & 31) == 0) {
@@ -263,24 +280,28 @@ __device__ double exactReach(const CloudInput& in, uint32_t i, int a) {
 // Second pass: the exact extremes. Only a Gaussian whose position - reach can
 // lie at or below the first pass's smallest upper bound can hold the minimum
 // (every other one's exceeds it), and likewise for the maximum; those few get
-// the exact reach and their exact bound into exact[0..5].
-__global__ void cloudExtremesKernel(CloudInput in, const unsigned long long* __restrict__ keys,
+// the exact reach and their exact bound into exact[0..5]. The test is in
+// float, rounded outwards: position - reach >= RD(position - RU(hf (1 +
+// slack))).
+__global__ void cloudExtremesKernel(CloudInput in, const uint32_t* __restrict__ keys,
                                     const float4* __restrict__ frames, unsigned long long* __restrict__ exact) {
     unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
+    float bound[6];
+    for (int q = 0; q < 6; q++) bound[q] = fromOrderedKey32(keys[q]);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < in.count; i += gridDim.x * blockDim.x) {
         for (int a = 0; a < 3; a++) {
-            const double p = in.pos[3 * size_t(i) + a];
+            const float p = in.pos[3 * size_t(i) + a];
             const float hf = frames[3 * size_t(i) + a].w;
             bool low = true, high = true;
             if (!isnan(hf)) {
-                const double wide = double(hf) * (1.0 + kReachSlack);
-                low = orderedKey(p - wide) <= keys[a];
-                high = orderedKey(p + wide) >= keys[3 + a];
+                const float wide = __fmul_ru(hf, float(1.0 + kReachSlack));  // >= reach
+                low = __fsub_rd(p, wide) <= bound[a];
+                high = __fadd_ru(p, wide) >= bound[3 + a];
             }
             if (!(low || high)) continue;
             const double half = exactReach(in, i, a);
-            if (low) lo[a] = min(lo[a], orderedKey(p - half));
-            if (high) hi[a] = max(hi[a], orderedKey(p + half));
+            if (low) lo[a] = min(lo[a], orderedKey(double(p) - half));
+            if (high) hi[a] = max(hi[a], orderedKey(double(p) + half));
         }
     }
     for (int a = 0; a < 3; a++) {
@@ -499,53 +520,63 @@ __device__ void stampCell(const CloudInput& in, uint32_t gaussian, const GridVie
     }
 }
 
-// floor(RN(RN(x - origin) / h)) (cloudVolume.js:384-386) shared by every
-// double x in [xl, xu], found without the double division; false when the
-// ends do not floor to one cell or leave the estimate's range. For an end q
-// = RN(x - origin) the float quotient e = float(q) * invH is within 3 2^-24
-// of q / h and so within 2^-22.2 |e| of RN(q / h); e - 2^-21 |e| and e +
-// 2^-21 |e|, each rounded once more, still bracket it. RN is monotone, so
-// the quotients of the ends bracket every x's, and one floor for both
-// brackets is the floor of all. (q zero gives the exact quotient 0; a q that
-// float cannot hold to 2^-24 is refused.)
-__device__ bool sharedCell(double xl, double xu, double origin, float invH, int64_t& cell) {
-    const double ql = xl - origin, qu = xu - origin;
-    const float fl = float(ql), fu = float(qu);
-    const bool okl = ql == 0.0 || (fabsf(fl) >= 0x1p-60f && fabsf(fl) <= 0x1p60f);
-    const bool oku = qu == 0.0 || (fabsf(fu) >= 0x1p-60f && fabsf(fu) <= 0x1p60f);
-    if (!(okl && oku && invH > 0.0f)) return false;
-    const float el = fl * invH, eu = fu * invH;
-    if (!(fabsf(el) < 0x1p22f && fabsf(eu) < 0x1p22f)) return false;
-    const float a = floorf(el - fabsf(el) * 0x1p-21f), b = floorf(eu + fabsf(eu) * 0x1p-21f);
-    if (a != b) return false;
+// The cell floor(RN(RN(x - origin) / h)) of cloudVolume.js:384-386, for x =
+// RN(c + s) with s anywhere in [s1, s2] (c the position, s a signed
+// half-reach or 0), decided in float when every such x shares one cell.
+// With co = float(c - float(origin)), e(s) = (co + s) * invH: the float
+// origin, the two sums and the product each round within 2^-24 of their
+// magnitude, invH within 2^-24 of 1 / h, so e is within 5 2^-24 M of (c +
+// s - origin) / h, M = (|origin| + |c| + |co| + |s|) / h bounding every
+// magnitude in cells; the double path's quotient is within 3 2^-53 M of it
+// too. delta = 2^-20 M (plus 2^-100 for subnormal roundings) covers both,
+// and e and the double quotient are monotone in s, so one floor of e(s1) -
+// delta and e(s2) + delta is the floor of every x's quotient. False when
+// they differ or leave float's exact integers.
+__device__ __forceinline__ bool floatCell(float co, float s1, float s2, float invH, float delta, int64_t& cell) {
+    const float a = floorf((co + s1) * invH - delta), b = floorf((co + s2) * invH + delta);
+    if (a != b || !(fabsf(a) < 0x1p22f)) return false;
     cell = int64_t(a);
     return true;
 }
 
+// Whether the float cells hold for a position on axis a (ranges that keep
+// every term above a normal float's floor and below overflow).
+__device__ __forceinline__ bool floatCellsHold(const GridView& g, float c, float reach) {
+    return g.floatBound && g.invH > 0.0f && fabsf(c) <= 0x1p40f && reach <= 0x1p40f;
+}
+
 __device__ __forceinline__ int64_t clampCell(int64_t v, int64_t lo, int64_t hi) { return v < lo ? lo : v > hi ? hi : v; }
 
-// cloudVolume.js:384-386 for the centre: the float estimate, else exact.
+// cloudVolume.js:384-386 for the centre: in float, else exact.
 __device__ int64_t centreCell(const GridView& g, double c, int a) {
+    const float cf = float(c);  // exact: c is a float position
     int64_t cell;
-    if (sharedCell(c, c, g.origin[a], g.invH, cell)) return clampCell(cell, 0, int64_t(g.dims[a]) - 1);
+    if (floatCellsHold(g, cf, 0.0f)) {
+        const float co = cf - g.originF[a];
+        const float delta = 0x1p-20f * (g.originMag[a] + fabsf(cf) + fabsf(co)) * g.invH + 0x1p-100f;
+        if (floatCell(co, 0.0f, 0.0f, g.invH, delta, cell)) return clampCell(cell, 0, int64_t(g.dims[a]) - 1);
+    }
     return clampedCell(c, g.origin[a], g.h, 0, int64_t(g.dims[a]) - 1);
 }
 
 // cloudVolume.js:147-160: the cells from position - reach to position +
 // reach, within one cell of the faces. With a reach estimate hf the exact
-// reach lies in [hf (1 - kReachSlack), hf (1 + kReachSlack)] (both products
-// exact in double), so each edge is the shared cell of that interval's
-// ends; only an edge within the slack of a cell boundary (or a Gaussian
-// without an estimate) takes the exact reach and the double division.
+// reach lies in [hf (1 - kReachSlack), hf (1 + kReachSlack)], also after
+// those bounds are rounded to float (slack 2^-18 against the estimate's
+// 2^-21), so each edge is the float cell of that interval; only an edge
+// within delta of a cell boundary (or a Gaussian without an estimate)
+// takes the exact reach and the double division.
 __device__ Box boxOf(const CloudInput& in, uint32_t i, const GridView& g, const double c[3], const float hf[3]) {
     Box b;
     for (int a = 0; a < 3; a++) {
         const int64_t lo = 1, hi = int64_t(g.dims[a]) - 2;
-        if (!isnan(hf[a])) {
-            const double narrow = double(hf[a]) * (1.0 - kReachSlack), wide = double(hf[a]) * (1.0 + kReachSlack);
+        const float cf = float(c[a]);  // exact: c is a float position
+        if (!isnan(hf[a]) && floatCellsHold(g, cf, hf[a])) {
+            const float narrow = hf[a] * float(1.0 - kReachSlack), wide = hf[a] * float(1.0 + kReachSlack);
+            const float co = cf - g.originF[a];
+            const float delta = 0x1p-20f * (g.originMag[a] + fabsf(cf) + fabsf(co) + wide) * g.invH + 0x1p-100f;
             int64_t l, u;
-            if (sharedCell(c[a] - wide, c[a] - narrow, g.origin[a], g.invH, l) &&
-                sharedCell(c[a] + narrow, c[a] + wide, g.origin[a], g.invH, u)) {
+            if (floatCell(co, -wide, -narrow, g.invH, delta, l) && floatCell(co, narrow, wide, g.invH, delta, u)) {
                 b.lo[a] = clampCell(l, lo, hi);
                 b.hi[a] = clampCell(u, lo, hi);
                 continue;
@@ -1077,8 +1108,8 @@ __global__ void unpackCellsKernel(const uint32_t* __restrict__ a, const uint32_t
 }
 
 struct CloudScalars {
-    unsigned long long keys[6];   // the bounds' first pass
     unsigned long long exact[6];  // the exact extremes
+    uint32_t keys[6];             // the bounds' first pass, float keys
     unsigned long long filled;
     unsigned long long occupied;
     uint32_t nan;
@@ -1141,7 +1172,10 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     POOL_ALLOC(scalarsBuf, sizeof(CloudScalars), pool, st, "cloud scratch");
     auto* sc = static_cast<CloudScalars*>(scalarsBuf.p);
     CloudScalars init{};
-    for (int a = 0; a < 3; a++) init.keys[a] = init.exact[a] = ~0ull;
+    for (int a = 0; a < 3; a++) {
+        init.keys[a] = ~0u;
+        init.exact[a] = ~0ull;
+    }
     CK(cudaMemcpyAsync(sc, &init, sizeof init, cudaMemcpyHostToDevice, st), "cloud scratch");
     DeviceBuffer framesBuf;
     POOL_ALLOC(framesBuf, size_t(in.count) * 3 * sizeof(float4), pool, st, "cloud scratch");
@@ -1193,7 +1227,8 @@ int voxelizeCloud(vsim_cloud_volume* v, const CloudInput& in, const vsim_cloud_o
     g.hF = float(h);
     g.floatBound = h >= 0x1p-30 && h <= 0x1p30;
     for (int a = 0; a < 3; a++) {
-        g.originMag[a] = std::max(std::fabs(float(g.origin[a])), 0x1p-100f);
+        g.originF[a] = float(g.origin[a]);
+        g.originMag[a] = std::max(std::fabs(g.originF[a]), 0x1p-100f);
         g.floatBound = g.floatBound && std::fabs(g.origin[a]) <= 0x1p40;
     }
     g.cells = n;

@@ -2,8 +2,8 @@
  * vsim_oracle.h -- TEST INFRASTRUCTURE ONLY.
  *
  * A CPU restatement of the visionary-sim reference's solver step (its WGSL
- * compute shaders and the JS that feeds them), used as the checker for the
- * GPU library and as the timed CPU baseline. Nothing in the product links,
+ * compute shaders and the JS that feeds them), the oracle the GPU library's
+ * results are compared against and the timed CPU baseline. Nothing in the product links,
  * loads or calls this; only tests/, __graft_entry__.smoke() and bench.py's
  * CPU legs do.
  *

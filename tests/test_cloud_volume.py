@@ -7,7 +7,9 @@ occupancy byte for byte, and the same occupied and filled counts.
 The fill's flood runs by rounds of sweeps and, past a cap of rounds, by a
 union-find; the fill cases run both ways (`flood`), and nested shells whose
 inner cavity is reached only by a winding path take several rounds, or the
-union-find when the cap is lower.
+union-find when the cap is lower. The seal and flood pack 32 cells to a word
+along x; box shells with rows of 8, 31, 32, 33, 64 and 65 cells take the
+word edges.
 
 Cases: the reference tests' sphere shell at its element sizes, with and
 without the fill; an open capture; anisotropic randomly rotated Gaussians;
@@ -221,3 +223,30 @@ def test_nested_shells_winding_path(vz, rounds):
     for probe in ((0.0, 0.05, 0.0), (0.095, 0.0, 0.0), (-0.095, 0.0, 0.0)):
         cell, _ = vz.locate(g.origin, g.h, g.dims, *probe)
         assert g.occupancy[cell[0] + g.dims[0] * (cell[1] + g.dims[1] * cell[2])] == 0, probe
+
+
+def _box_shell(half, spacing):
+    """Points on the faces of an axis-aligned box of half-extents `half`."""
+    axes = [np.arange(-h, h + spacing / 2, spacing) for h in half]
+    pts = []
+    for axis in range(3):
+        u, v = np.meshgrid(axes[(axis + 1) % 3], axes[(axis + 2) % 3], indexing="ij")
+        for sign in (-1.0, 1.0):
+            p = np.zeros((u.size, 3))
+            p[:, axis] = sign * half[axis]
+            p[:, (axis + 1) % 3] = u.ravel()
+            p[:, (axis + 2) % 3] = v.ravel()
+            pts.append(p)
+    return np.unique(np.round(np.concatenate(pts), 9), axis=0)
+
+
+@pytest.mark.parametrize("nx", [8, 31, 32, 33, 64, 65])
+def test_word_edges(vz, flood, nx):
+    # The seal and the flood pack 32 cells to a word along x: rows one cell
+    # short of, on and past a word's end, and shorter than a word.
+    h, reach = 0.004, 0.0016
+    extent = (nx - 4 - 0.5) * h  # padding 2 on both sides
+    cloud = _cloud_at(_box_shell((extent / 2 - reach, 0.03, 0.02), 0.002), reach / 2)
+    g = _same(vz, cloud, h)
+    assert g.dims[0] == nx
+    assert vz.count_occupied(g) > 0

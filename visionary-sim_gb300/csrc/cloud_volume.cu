@@ -39,6 +39,7 @@
 
 #include <math_constants.h>
 
+#include "frame_rows.cuh"
 #include "sim_internal.cuh"
 
 struct vsim_cloud_volume {
@@ -228,10 +229,20 @@ __global__ void cloudBoundsKernel(CloudInput in, uint32_t* __restrict__ keys, ui
     uint32_t lo[3] = {~0u, ~0u, ~0u}, hi[3] = {0, 0, 0};
     bool sawNan = false;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < in.count; i += gridDim.x * blockDim.x) {
-        Ellipsoid e;
-        frameOf(in, i, e);
+        // The frame in float where every entry is certified to equal the
+        // double path's float32 rounding (frame_rows.cuh), else in double.
         float col[9], rf[3];
-        for (int q = 0; q < 9; q++) col[q] = float(e.col[q]);
+        const float* q4 = in.rot + 4 * size_t(i);
+        if (!frame::rowsInFloat(q4[0], q4[1], q4[2], q4[3], col)) {
+            Ellipsoid full;
+            frameOf(in, i, full);
+            for (int q = 0; q < 9; q++) col[q] = float(full.col[q]);
+        }
+        // the double frame, when an exact reach is wanted: the float32
+        // entries widened, exactly frameOf's
+        Ellipsoid e;
+        for (int q = 0; q < 9; q++) e.col[q] = col[q];
+        for (int a = 0; a < 3; a++) e.radius[a] = in.sigma * double(in.scale[3 * size_t(i) + a]);
         radiiOf(in, i, rf);
         for (int a = 0; a < 3; a++) {
             const float p = in.pos[3 * size_t(i) + a];

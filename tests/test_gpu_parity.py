@@ -453,9 +453,10 @@ def test_captured_cloud_body(lib):
     assert np.array_equal(order, pyoracle.stable_sort(keys))
 
 
-# 2^20 keys fill exactly 256 tiles of the histogram; 1.1M keys go past it
+# 2^20 keys fill exactly 256 tiles of the histogram, 1.1M keys go past it;
+# past ~4.2M keys (64 scan chunks) the scan takes three launches a pass
 @pytest.mark.parametrize("n,bits", [(1, 32), (4095, 32), (4097, 8), (1_000_003, 32), (300_000, 20), (1 << 20, 32),
-                                    (1_100_000, 32)])
+                                    (1_100_000, 32), (4_500_000, 32)])
 def test_radix_sort_matches_stable_sort(lib, gpu, n, bits):
     import torch
     import pyoracle

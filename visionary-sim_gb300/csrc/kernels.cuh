@@ -212,6 +212,8 @@ cudaError_t launchSplatDeform(cudaStream_t st, const SplatState& s, const float4
 // ---- radix sort -------------------------------------------------------------
 
 size_t radixSortTempBytes(uint32_t n);
+// Kernels one radixSortU32 call launches.
+uint32_t radixSortLaunches(uint32_t n, uint32_t keyBits);
 cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint32_t keyBits, void* temp,
                          size_t tempBytes, cudaStream_t st);
 

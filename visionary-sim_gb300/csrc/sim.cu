@@ -1173,7 +1173,7 @@ uint32_t vsim_frame_launches(const vsim_sim* s, uint32_t steps) {
 
 uint32_t vsim_splat_launches(const vsim_sim* s) {
     if (!s || s->splatCount == 0) return 0;
-    return 1 + 5 * 4;  // deformation, then four 8-bit passes of five kernels
+    return 1 + radixSortLaunches(s->splatCount, 32);  // deformation, then the depth sort
 }
 
 int vsim_time_colour_passes(vsim_sim* s, uint32_t sweeps, float* ms) {

@@ -179,6 +179,7 @@ constexpr uint32_t kSortTile = kSortThreads * kSortItems;  // 4096 keys
 constexpr uint32_t kWarps = kSortThreads / 32;
 constexpr uint32_t kScanChunk = 4096;  // elements per block of the scan
 constexpr uint32_t kScanMaxChunks = 4096;
+constexpr uint32_t kFoldChunks = 64;  // chunks a down-sweep block sums itself
 
 namespace {
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -189,6 +190,12 @@ constexpr size_t sortTempBytes(uint32_t n) {
 }  // namespace
 
 size_t radixSortTempBytes(uint32_t n) { return sortTempBytes(n); }
+
+uint32_t radixSortLaunches(uint32_t n, uint32_t keyBits) {
+    if (n == 0) return 0;
+    const uint32_t chunks = (256 * tilesOf(n) + kScanChunk - 1) / kScanChunk;
+    return (keyBits + 7) / 8 * (chunks <= kFoldChunks ? 4u : 5u);  // the scan's middle level folded in
+}
 
 __global__ void __launch_bounds__(kSortThreads) sortHistKernel(const uint32_t* __restrict__ keys, uint32_t n,
                                                                uint32_t shift, uint32_t mask, uint32_t tiles,
@@ -296,6 +303,35 @@ __global__ void __launch_bounds__(kSortThreads) scanDownKernel(uint32_t* __restr
     }
     uint32_t total;
     uint32_t run = blockExclusiveScan(sum, warpSums, total) + partial[blockIdx.x];
+#pragma unroll
+    for (uint32_t i = 0; i < per; i++) {
+        if (base + i < n) data[base + i] = run;
+        run += v[i];
+    }
+}
+
+// Scan, levels 2 and 3 in one launch when the chunks are few (at most
+// kFoldChunks): each block sums the chunk totals before its own (one per
+// thread at most) instead of reading them scanned by scanPartialKernel.
+
+__global__ void __launch_bounds__(kSortThreads) scanDownFoldKernel(uint32_t* __restrict__ data, uint32_t n,
+                                                                   const uint32_t* __restrict__ partial) {
+    pdlWait();  // the counts and chunk totals come from the kernels before
+    pdlLaunchNext();
+    __shared__ uint32_t warpSums[kWarps + 1];
+    uint32_t before;
+    blockExclusiveScan(threadIdx.x < blockIdx.x ? partial[threadIdx.x] : 0u, warpSums, before);
+    constexpr uint32_t per = kScanChunk / kSortThreads;
+    const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * per;
+    uint32_t v[per];
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < per; i++) {
+        v[i] = base + i < n ? data[base + i] : 0;
+        sum += v[i];
+    }
+    uint32_t total;
+    uint32_t run = blockExclusiveScan(sum, warpSums, total) + before;
 #pragma unroll
     for (uint32_t i = 0; i < per; i++) {
         if (base + i < n) data[base + i] = run;
@@ -422,8 +458,12 @@ cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint
         uint32_t* vout = last ? order : (pass % 2 == 0 ? valsA : valsB);
         pdl(sortHistKernel, tiles, st, kin, n, shift, mask, tiles, hist);
         pdl(scanReduceKernel, chunks, st, (const uint32_t*)hist, histCount, partial);
-        pdl(scanPartialKernel, 1u, st, partial, chunks);
-        pdl(scanDownKernel, chunks, st, hist, histCount, (const uint32_t*)partial);
+        if (chunks <= kFoldChunks) {
+            pdl(scanDownFoldKernel, chunks, st, hist, histCount, (const uint32_t*)partial);
+        } else {
+            pdl(scanPartialKernel, 1u, st, partial, chunks);
+            pdl(scanDownKernel, chunks, st, hist, histCount, (const uint32_t*)partial);
+        }
         pdl(sortScatterKernel, tiles, st, kin, vin, n, shift, mask, tiles, (const uint32_t*)hist, kout, vout);
         kin = kout;
         vin = vout;

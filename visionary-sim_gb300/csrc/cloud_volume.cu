@@ -39,6 +39,7 @@
 
 #include <math_constants.h>
 
+#include "float_bounds.cuh"
 #include "frame_rows.cuh"
 #include "sim_internal.cuh"
 
@@ -56,6 +57,11 @@ struct vsim_cloud_volume {
 
 namespace vsim {
 namespace {
+
+using bounds::floatCell;
+using bounds::hypotV8;
+using bounds::kReachSlack;
+using bounds::reachEstimate;
 
 constexpr uint32_t kCloudBlock = 256;
 constexpr uint32_t kInlineBoxCells = 64;    // larger boxes are stamped by a block each
@@ -101,30 +107,6 @@ struct Ellipsoid {
     double radius[3];
 };
 
-// JavaScript's Math.hypot as V8 evaluates it (its published math builtin):
-// infinity if any argument is infinite, else NaN if any is NaN, else 0 when
-// all are 0; otherwise the magnitudes over the largest, squared and summed in
-// argument order with Kahan compensation, square root times the largest.
-__device__ double hypotV8(double a, double b, double c) {
-    a = fabs(a);
-    b = fabs(b);
-    c = fabs(c);
-    if (isinf(a) || isinf(b) || isinf(c)) return CUDART_INF;
-    if (isnan(a) || isnan(b) || isnan(c)) return CUDART_NAN;
-    const double top = fmax(a, fmax(b, c));
-    if (top == 0.0) return 0.0;
-    const double v[3] = {a, b, c};
-    double total = 0.0, compensation = 0.0;
-    for (int r = 0; r < 3; r++) {
-        // x / x is exactly 1 and 0 / x exactly 0: those divisions are skipped
-        const double n = v[r] == top ? 1.0 : v[r] == 0.0 ? 0.0 : v[r] / top;
-        const double summand = n * n - compensation;
-        const double preliminary = total + summand;
-        compensation = (preliminary - total) - summand;
-        total = preliminary;
-    }
-    return sqrt(total) * top;
-}
 
 // mat3.js:71-87 (mat3FromQuat), each entry rounded to float32 as its output
 // array does, and the half-axes sigma * scale (cloudVolume.js:196-199).
@@ -174,38 +156,12 @@ __device__ __forceinline__ unsigned long long warpMax64(unsigned long long v) {
 // hypot evaluated in double (FP64 runs at a small fraction of the float rate
 // on this part: a double division costs about a hundred float operations).
 //
-// The estimate, sqrtf of the float sum of the float products' squares, is
-// within 2^-21 of V8's hypot of the double products (relative): the float
-// products are within 2^-22.4 of the double ones (float(sigma), the radius
-// and the product each rounded once), their squares and two sums add under
-// 2^-21, the square root halves that, and V8's own evaluation is within
-// 2^-50 of the exact hypot. kReachSlack, 8 times that, brackets the exact reach:
-//   hf (1 - kReachSlack) <= reach <= hf (1 + kReachSlack),
-// both products rounded in double well inside the slack. It holds while
-// every nonzero product lies in [2^-60, 2^60] (squares and sums stay normal
-// floats) and the radii are 0 or in [2^-100, 2^100].
-constexpr double kReachSlack = 0x1p-18;
-
-__device__ float reachEstimate(const float col[9], const float r[3], int a) {
-    float sum = 0.0f;
-    for (int k = 0; k < 3; k++) {
-        const float c = col[3 * k + a];
-        const float v = c * r[k];
-        if (c != 0.0f && r[k] != 0.0f && !(fabsf(v) >= 0x1p-60f && fabsf(v) <= 0x1p60f)) return CUDART_NAN_F;
-        sum += v * v;
-    }
-    return sqrtf(sum);
-}
 
 // The radii float(sigma) * scale for the estimate (within 2^-23 of the
 // double sigma * scale of cloudVolume.js:196-199), NaN where out of its
 // range.
 __device__ void radiiOf(const CloudInput& in, uint32_t i, float rf[3]) {
-    for (int a = 0; a < 3; a++) {
-        const float r = in.sigmaF * in.scale[3 * size_t(i) + a];
-        const float m = fabsf(r);
-        rf[a] = (r == 0.0f || (m >= 0x1p-100f && m <= 0x1p100f)) ? r : CUDART_NAN_F;
-    }
+    for (int a = 0; a < 3; a++) rf[a] = bounds::radiusEstimate(in.sigmaF, in.scale[3 * size_t(i) + a]);
 }
 
 // Floats ordered as unsigned integers (as orderedKey for doubles).
@@ -531,24 +487,6 @@ __device__ void stampCell(const CloudInput& in, uint32_t gaussian, const GridVie
     }
 }
 
-// The cell floor(RN(RN(x - origin) / h)) of cloudVolume.js:384-386, for x =
-// RN(c + s) with s anywhere in [s1, s2] (c the position, s a signed
-// half-reach or 0), decided in float when every such x shares one cell.
-// With co = float(c - float(origin)), e(s) = (co + s) * invH: the float
-// origin, the two sums and the product each round within 2^-24 of their
-// magnitude, invH within 2^-24 of 1 / h, so e is within 5 2^-24 M of (c +
-// s - origin) / h, M = (|origin| + |c| + |co| + |s|) / h bounding every
-// magnitude in cells; the double path's quotient is within 3 2^-53 M of it
-// too. delta = 2^-20 M (plus 2^-100 for subnormal roundings) covers both,
-// and e and the double quotient are monotone in s, so one floor of e(s1) -
-// delta and e(s2) + delta is the floor of every x's quotient. False when
-// they differ or leave float's exact integers.
-__device__ __forceinline__ bool floatCell(float co, float s1, float s2, float invH, float delta, int64_t& cell) {
-    const float a = floorf((co + s1) * invH - delta), b = floorf((co + s2) * invH + delta);
-    if (a != b || !(fabsf(a) < 0x1p22f)) return false;
-    cell = int64_t(a);
-    return true;
-}
 
 // Whether the float cells hold for a position on axis a (ranges that keep
 // every term above a normal float's floor and below overflow).
@@ -564,7 +502,7 @@ __device__ int64_t centreCell(const GridView& g, double c, int a) {
     int64_t cell;
     if (floatCellsHold(g, cf, 0.0f)) {
         const float co = cf - g.originF[a];
-        const float delta = 0x1p-20f * (g.originMag[a] + fabsf(cf) + fabsf(co)) * g.invH + 0x1p-100f;
+        const float delta = bounds::cellDelta(g.originMag[a], cf, co, 0.0f, g.invH);
         if (floatCell(co, 0.0f, 0.0f, g.invH, delta, cell)) return clampCell(cell, 0, int64_t(g.dims[a]) - 1);
     }
     return clampedCell(c, g.origin[a], g.h, 0, int64_t(g.dims[a]) - 1);
@@ -585,7 +523,7 @@ __device__ Box boxOf(const CloudInput& in, uint32_t i, const GridView& g, const 
         if (!isnan(hf[a]) && floatCellsHold(g, cf, hf[a])) {
             const float narrow = hf[a] * float(1.0 - kReachSlack), wide = hf[a] * float(1.0 + kReachSlack);
             const float co = cf - g.originF[a];
-            const float delta = 0x1p-20f * (g.originMag[a] + fabsf(cf) + fabsf(co) + wide) * g.invH + 0x1p-100f;
+            const float delta = bounds::cellDelta(g.originMag[a], cf, co, wide, g.invH);
             int64_t l, u;
             if (floatCell(co, -wide, -narrow, g.invH, delta, l) && floatCell(co, narrow, wide, g.invH, delta, u)) {
                 b.lo[a] = clampCell(l, lo, hi);

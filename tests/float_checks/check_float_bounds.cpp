@@ -6,7 +6,11 @@
 //   cells: wherever floatCell decides a cell for position c and signed
 //     half-reach s in [s1, s2], floor(RN(RN(RN(c + s) - origin) / h)) in
 //     double is that cell for s1, s2 and points between them, including
-//     positions placed within a few ulps of cell boundaries.
+//     positions placed within a few ulps of cell boundaries;
+//   samples: wherever the float sample test decides, the double evaluation
+//     of the sample decides the same, with ellipsoids scaled so their
+//     surface passes within a few ulps of a sample, and with grids small
+//     enough that the bound is summed in double (floatTestOf).
 // Prints the counts; exits 1 on any disagreement.
 #include <cstdint>
 #include <cstdio>
@@ -114,7 +118,103 @@ int main(int argc, char** argv) {
             }
         }
     }
-    std::printf("reach checked %ld bad %ld; cells tried %ld decided %ld bad %ld\n", reachChecked, reachBad, cellTried,
-                cellDecided, cellBad);
-    return reachBad || cellBad ? 1 : 0;
+    // samples: the float test of a box against the double evaluation
+    long samples = 0, sampleDecided = 0, sampleBad = 0;
+    const long gaussians = cases / 20 + 1;
+    for (long n = 0; n < gaussians; n++) {
+        double v[4], len = 0;
+        for (int k = 0; k < 4; k++) {
+            v[k] = uniform() * 2 - 1;
+            len += v[k] * v[k];
+        }
+        len = std::sqrt(len);
+        float q[4];
+        for (int k = 0; k < 4; k++) q[k] = float(v[k] / len);
+        float col[9];
+        frameInDouble(q[0], q[1], q[2], q[3], col);
+        // a grid: h, origin; tiny h now and then takes the double-summed bound
+        const double h = (next() % 16 == 0) ? 1e-10 * (1 + uniform()) : std::exp(std::log(1e-4) + uniform() * std::log(1e2));
+        bounds::GridView g{};
+        for (int a = 0; a < 3; a++) {
+            g.dims[a] = 400;
+            g.origin[a] = (uniform() * 2 - 1) * 0.5;
+        }
+        g.h = h;
+        const float invH = float(1.0 / h);
+        g.invH = invH >= 0x1p-40f && invH <= 0x1p40f ? invH : 0.0f;
+        g.hF = float(h);
+        g.floatBound = h >= 0x1p-30 && h <= 0x1p30;
+        for (int a = 0; a < 3; a++) {
+            g.originF[a] = float(g.origin[a]);
+            g.originMag[a] = std::fmax(std::fabs(g.originF[a]), 0x1p-100f);
+            g.floatBound = g.floatBound && std::fabs(g.origin[a]) <= 0x1p40;
+        }
+        g.cells = 400u * 400u * 400u;
+        // the centre at a random place; the radii chosen so the surface
+        // passes within a few ulps of a sample point half the time
+        float cf[3];
+        double c[3];
+        for (int a = 0; a < 3; a++) {
+            cf[a] = float(g.origin[a] + (50 + uniform() * 300) * h);
+            c[a] = cf[a];
+        }
+        const double sigma = 2.0;
+        float scale[3];
+        for (int a = 0; a < 3; a++) scale[a] = float(h * (0.3 + uniform() * 1.5) / sigma);
+        bounds::Ellipsoid e;
+        for (int qq = 0; qq < 9; qq++) e.col[qq] = col[qq];
+        for (int a = 0; a < 3; a++) e.radius[a] = sigma * double(scale[a]);
+        bounds::Box b;
+        for (int a = 0; a < 3; a++) {
+            const double half = bounds::hypotV8(e.col[a] * e.radius[0], e.col[3 + a] * e.radius[1], e.col[6 + a] * e.radius[2]);
+            b.lo[a] = int64_t(std::floor(((c[a] - half) - g.origin[a]) / h));
+            b.hi[a] = int64_t(std::floor(((c[a] + half) - g.origin[a]) / h));
+        }
+        if (next() % 2) {
+            // scale the ellipsoid so its surface meets one sample exactly
+            // (the sum there 1 up to rounding), then nudge by a few ulps
+            const int64_t i = b.lo[0] + int64_t(next() % uint64_t(b.extent(0)));
+            const int64_t j = b.lo[1] + int64_t(next() % uint64_t(b.extent(1)));
+            const int64_t k = b.lo[2] + int64_t(next() % uint64_t(b.extent(2)));
+            double ox, oy, oz;
+            bounds::sampleOffset(int(next() % 9), ox, oy, oz);
+            const double d[3] = {g.origin[0] + (double(i) + ox) * h - c[0], g.origin[1] + (double(j) + oy) * h - c[1],
+                                 g.origin[2] + (double(k) + oz) * h - c[2]};
+            double sum = 0;
+            for (int a = 0; a < 3; a++) {
+                const double t = (e.col[3 * a] * d[0] + e.col[3 * a + 1] * d[1] + e.col[3 * a + 2] * d[2]) / e.radius[a];
+                sum += t * t;
+            }
+            if (sum > 0) {
+                const double f = std::sqrt(sum) * (1 + (uniform() * 2 - 1) * 1e-7);
+                for (int a = 0; a < 3; a++) {
+                    scale[a] = float(scale[a] * f);
+                    e.radius[a] = sigma * double(scale[a]);
+                }
+            }
+        }
+        bounds::FloatTest f;
+        const bool fast = bounds::floatTestInFloat(g, b, c, cf, col, sigma, float(sigma), scale, f);
+        if (!fast) continue;
+        for (int64_t k = b.lo[2]; k <= b.hi[2]; k++)
+            for (int64_t j = b.lo[1]; j <= b.hi[1]; j++)
+                for (int64_t i = b.lo[0]; i <= b.hi[0]; i++)
+                    for (int sIdx = 0; sIdx < 9; sIdx++) {
+                        double ox, oy, oz;
+                        bounds::sampleOffset(sIdx, ox, oy, oz);
+                        const int got = bounds::floatSample(f, float(i - b.lo[0]) + float(ox), float(j - b.lo[1]) + float(oy),
+                                                            float(k - b.lo[2]) + float(oz));
+                        samples++;
+                        if (got < 0) continue;
+                        sampleDecided++;
+                        const bool want = bounds::sampleInside(g, i, j, k, sIdx, c, e);
+                        if ((got == 1) != want) {
+                            if (sampleBad < 5) std::printf("sample mismatch: float %d double %d\n", got, int(want));
+                            sampleBad++;
+                        }
+                    }
+    }
+    std::printf("reach checked %ld bad %ld; cells tried %ld decided %ld bad %ld; samples %ld decided %ld bad %ld\n",
+                reachChecked, reachBad, cellTried, cellDecided, cellBad, samples, sampleDecided, sampleBad);
+    return reachBad || cellBad || sampleBad ? 1 : 0;
 }

@@ -53,13 +53,17 @@ def bounds_harness(tmp_path_factory):
     return out
 
 
-def test_reach_bracket_and_float_cells(bounds_harness):
+def test_reach_bracket_float_cells_and_samples(bounds_harness):
     """csrc/float_bounds.cuh: V8's hypot of the double products lies inside
-    the float reach estimate's bracket (and its float-rounded bounds), and
-    every box-edge cell the float test decides is the double division's,
-    positions within a few ulps of a cell boundary included."""
+    the float reach estimate's bracket (and its float-rounded bounds); every
+    box-edge cell the float test decides is the double division's,
+    positions within a few ulps of a cell boundary included; and every
+    sample the float sample test decides is decided the same by the double
+    evaluation, surfaces within a few ulps of a sample included."""
     run = subprocess.run([str(bounds_harness), "1500000"], capture_output=True, text=True)
     assert run.returncode == 0, run.stdout + run.stderr
-    m = re.search(r"reach checked (\d+) bad (\d+); cells tried (\d+) decided (\d+) bad (\d+)", run.stdout)
-    assert m and int(m.group(2)) == 0 and int(m.group(5)) == 0
+    m = re.search(r"reach checked (\d+) bad (\d+); cells tried (\d+) decided (\d+) bad (\d+); "
+                  r"samples (\d+) decided (\d+) bad (\d+)", run.stdout)
+    assert m and int(m.group(2)) == 0 and int(m.group(5)) == 0 and int(m.group(8)) == 0
     assert int(m.group(4)) > 0.6 * int(m.group(3))
+    assert int(m.group(7)) > 0.9 * int(m.group(6))

@@ -58,7 +58,14 @@ struct vsim_cloud_volume {
 namespace vsim {
 namespace {
 
+using bounds::Box;
+using bounds::Ellipsoid;
 using bounds::floatCell;
+using bounds::floatSample;
+using bounds::floatTestOf;
+using bounds::FloatTest;
+using bounds::GridView;
+using bounds::sampleInside;
 using bounds::hypotV8;
 using bounds::kReachSlack;
 using bounds::reachEstimate;
@@ -87,25 +94,7 @@ struct CloudInput {
     float sigmaF;        // float(sigma)
 };
 
-struct GridView {
-    uint32_t dims[3];
-    double origin[3];
-    double h;
-    float invH;  // float(1 / h), 0 outside [2^-40, 2^40]
-    float hF;    // float(h)
-    float originF[3];    // float(origin)
-    float originMag[3];  // max(|float(origin)|, 2^-100)
-    bool floatBound;     // h in [2^-30, 2^30] and |origin| <= 2^40 on every axis
-    uint32_t cells;
-};
 
-// One Gaussian as an ellipsoid (cloudVolume.js:195-210): the column-major
-// rotation as the reference's Float32Array holds it, the half-axes in the
-// Gaussian's frame.
-struct Ellipsoid {
-    double col[9];
-    double radius[3];
-};
 
 
 // mat3.js:71-87 (mat3FromQuat), each entry rounded to float32 as its output
@@ -289,164 +278,12 @@ __device__ __forceinline__ int64_t clampedCell(double v, double origin, double h
     return static_cast<int64_t>(fmin(fmax(f, double(lo)), double(hi)));
 }
 
-// One of a cell's nine sample points (its eight corners in corners.js:12-21
-// order, then its centre) tested against the ellipsoid in the reference's
-// double arithmetic and order (cloudVolume.js:255-273).
-__device__ __forceinline__ void sampleOffset(int s, double& ox, double& oy, double& oz) {
-    ox = s == 8 ? 0.5 : double(s & 1);
-    oy = s == 8 ? 0.5 : double((s >> 1) & 1);
-    oz = s == 8 ? 0.5 : double((s >> 2) & 1);
-}
-
-__device__ bool sampleInside(const GridView& g, int64_t i, int64_t j, int64_t k, int s, const double c[3],
-                             const Ellipsoid& e) {
-    double ox, oy, oz;
-    sampleOffset(s, ox, oy, oz);
-    const double dx = g.origin[0] + (double(i) + ox) * g.h - c[0];
-    const double dy = g.origin[1] + (double(j) + oy) * g.h - c[1];
-    const double dz = g.origin[2] + (double(k) + oz) * g.h - c[2];
-    double sum = 0.0;
-    for (int a = 0; a < 3; a++) {
-        const double t = (e.col[3 * a] * dx + e.col[3 * a + 1] * dy + e.col[3 * a + 2] * dz) / e.radius[a];
-        sum += t * t;
-    }
-    return sum <= 1.0;
-}
-
-struct Box {
-    int64_t lo[3], hi[3];
-    __device__ int64_t extent(int a) const { return hi[a] - lo[a] + 1; }
-    __device__ int64_t cells() const { return extent(0) * extent(1) * extent(2); }
-};
-
-// The sample test in float, with a bound on how far its sum of squares can
-// be from the double evaluation's; a sample whose float sum is further than
-// the bound from 1 is decided by it, every other one is evaluated in double.
-// Same answers, far fewer double operations (a double division costs tens
-// of float operations on this part). The bound, per Gaussian and box:
-//   offset: float(base) + off * float(h), with base = origin + lo h - c (in
-//     double) and off = i - lo + ox exact, against the double sequence
-//     origin + (i + ox) h - c: within 2^-22 X + A, where X = |base| +
-//     (extent + 1) h bounds |base|, off h and the offset, and A = 2^-50
-//     (|origin| + |c| + (|lo| + extent + 1) h) the double sequence's own
-//     rounding;
-//   dot with column a (float entries, exact): the propagated offset errors
-//     plus 2^-22 sum_k |col| X_k for its own three roundings;
-//   t = dot / r: that over r (held x4 in `err`, a factor of 4 to spare),
-//     plus 2^-23 |t| for the float reciprocal and product (taken x4);
-//   sum of squares: sum_a (2|t_a| + e_a) e_a, plus 2^-21 s for its roundings,
-//     plus a floor of 2^-20 so that 1 +- the bound is never rounded away.
-// A Gaussian whose bound is not small (err >= 1e-3), whose half-axes or cell
-// are outside [1e-30, 1e30], or whose box is wider than 2^20 cells is tested
-// in double throughout.
-struct FloatTest {
-    float base[3];
-    float h;
-    float col[9];
-    float inv[3];
-    float err[3];
-};
-
-__device__ bool floatTestOf(const GridView& g, const Box& b, const double c[3], const Ellipsoid& e, FloatTest& f) {
-    if (!(g.h > 1e-30 && g.h < 1e30)) return false;
-    double X[3], ex[3];
-    for (int a = 0; a < 3; a++) {
-        if (b.extent(a) > (1 << 20)) return false;
-        const double base = (g.origin[a] + double(b.lo[a]) * g.h) - c[a];
-        const double span = double(b.extent(a) + 1) * g.h;
-        X[a] = fabs(base) + span;
-        ex[a] = 0x1p-22 * X[a] + 0x1p-50 * (fabs(g.origin[a]) + fabs(c[a]) + fabs(double(b.lo[a])) * g.h + span);
-        f.base[a] = float(base);
-    }
-    f.h = float(g.h);
-    for (int q = 0; q < 9; q++) f.col[q] = float(e.col[q]);
-    for (int a = 0; a < 3; a++) {
-        const double r = e.radius[a];
-        if (!(r > 1e-30 && r < 1e30)) return false;
-        // the float reciprocal of float(r): within 2^-23 of 1 / r, inside the
-        // 2^-21 |t| allowance
-        f.inv[a] = __frcp_rn(float(r));
-        double dotErr = 0.0;
-        for (int k = 0; k < 3; k++) dotErr += fabs(e.col[3 * a + k]) * (ex[k] + 0x1p-22 * X[k]);
-        // above 4 dotErr / r: the reciprocal's error and every rounding of
-        // this product are covered by the (1 + 2^-20)
-        const double err = 4.0 * dotErr * double(f.inv[a]) * (1.0 + 0x1p-20);
-        if (!(err < 1e-3)) return false;
-        f.err[a] = float(err);
-    }
-    return true;
-}
-
-// floatTestOf with the bound's terms summed in float instead of double, from
-// the frame rows the bounds pass kept (f.col, exactly floatTestOf's), the
-// position as float (exact) and the radius as float(sigma) * scale (within
-// 2^-23 of float(r), so its reciprocal stays inside the 2^-21 |t|
-// allowance). All terms are sums and products of magnitudes, so each float
-// rounding (2^-24 relative, about a dozen along any chain) lowers them by
-// under 2^-20 in all, which the final (1 + 2^-16) more than restores;
-// magnitudes under 2^-100 are counted as 2^-100. Only the base offsets are
-// formed in double, as floatTestOf forms them. Inside the ranges checked
-// here (and g.floatBound's: h in [2^-30, 2^30], |origin| <= 2^40) no term is
-// a subnormal float or overflows (the smallest, 2^-50 h, is above 2^-80; the
-// error after the reciprocal above 2^-113); elsewhere floatTestOf decides.
-// Conversions from double cost FP64-pipe time on this part: there are four
-// a Gaussian.
-__device__ bool floatTestInFloat(const CloudInput& in, uint32_t i, const GridView& g, const Box& b,
-                                 const double c[3], const float cf[3], const float col[9], FloatTest& f) {
-    float rf[3];
-    bool ok = g.floatBound;
-    for (int a = 0; a < 3; a++) {
-        rf[a] = in.sigmaF * in.scale[3 * size_t(i) + a];
-        ok = ok && fabsf(cf[a]) <= 0x1p40f && b.extent(a) <= (1 << 20) && rf[a] >= 0x1p-30f && rf[a] <= 0x1p30f;
-    }
-    for (int q = 0; q < 9; q++) {
-        const float m = fabsf(col[q]);
-        ok = ok && (m == 0.0f || (m >= 0x1p-30f && m <= 0x1p30f));
-    }
-    if (!ok) {
-        Ellipsoid e;
-        for (int q = 0; q < 9; q++) e.col[q] = col[q];
-        for (int a = 0; a < 3; a++) e.radius[a] = in.sigma * double(in.scale[3 * size_t(i) + a]);
-        return floatTestOf(g, b, c, e, f);
-    }
-    const float h = g.hF;
-    float X[3], ex[3];
-    for (int a = 0; a < 3; a++) {
-        const double base = (g.origin[a] + double(b.lo[a]) * g.h) - c[a];
-        f.base[a] = float(base);
-        const float span = float(int32_t(b.extent(a) + 1)) * h;
-        X[a] = fmaxf(fabsf(f.base[a]), 0x1p-100f) + span;
-        const float lo = float(int32_t(b.lo[a]));
-        ex[a] = 0x1p-22f * X[a] + 0x1p-50f * (g.originMag[a] + fmaxf(fabsf(cf[a]), 0x1p-100f) + fabsf(lo) * h + span);
-    }
-    f.h = h;
-    for (int q = 0; q < 9; q++) f.col[q] = col[q];
-    for (int a = 0; a < 3; a++) {
-        f.inv[a] = __frcp_rn(rf[a]);
-        float dotErr = 0.0f;
-        for (int k = 0; k < 3; k++) dotErr += fabsf(f.col[3 * a + k]) * (ex[k] + 0x1p-22f * X[k]);
-        const float err = 4.0f * dotErr * f.inv[a] * (1.0f + 0x1p-16f);
-        if (!(err < 1e-3f)) return false;
-        f.err[a] = err;
-    }
-    return true;
-}
-
-// 1 inside, 0 outside, -1 too close to call in float.
-__device__ __forceinline__ int floatSample(const FloatTest& f, float ox, float oy, float oz) {
-    const float dx = f.base[0] + ox * f.h, dy = f.base[1] + oy * f.h, dz = f.base[2] + oz * f.h;
-    float sum = 0.0f, bound = 0.0f;
-    for (int a = 0; a < 3; a++) {
-        const float t = (f.col[3 * a] * dx + f.col[3 * a + 1] * dy + f.col[3 * a + 2] * dz) * f.inv[a];
-        const float at = fabsf(t);
-        const float et = f.err[a] + 0x1p-21f * at;
-        sum += t * t;
-        bound += (2.0f * at + et) * et;
-    }
-    bound += 0x1p-20f * sum + 0x1p-20f;
-    if (sum > 1.0f + bound) return 0;
-    if (sum < 1.0f - bound) return 1;
-    return -1;
+// The float test of Gaussian i's box (bounds::floatTestInFloat), from the
+// cloud's scales.
+__device__ bool floatTestInFloat(const CloudInput& in, uint32_t i, const GridView& g, const Box& b, const double c[3],
+                                 const float cf[3], const float col[9], FloatTest& f) {
+    const float scale[3] = {in.scale[3 * size_t(i)], in.scale[3 * size_t(i) + 1], in.scale[3 * size_t(i) + 2]};
+    return bounds::floatTestInFloat(g, b, c, cf, col, in.sigma, in.sigmaF, scale, f);
 }
 
 // cloudVolume.js:170-173 for one cell of a box: any sample inside. The index

@@ -6,7 +6,7 @@
  * of the reference's ES class `Simulator`
  * (packages/visionary-sim/src/sim/simulator.js:35-518) or of the seams under
  * it; the citation beside each names the exact method. A Node N-API shim (or
- * any other FFI) binds these 1:1; see INTEGRATION.md for the bindings.
+ * any other FFI) binds these 1:1.
  *
  * Conventions
  *   - Opaque handles, `int` status codes (VSIM_OK == 0), caller-owned output
@@ -388,6 +388,7 @@ int vsim_splats_read(vsim_sim* sim, float* means, float* cov6, uint32_t* order, 
  * apps/simulator/src/scene/app.js:71-75). Writes to `d_order` the
  * permutation that sorts `d_keys` ascending, ties in index order; `d_keys`
  * is not modified. Only the low `key_bits` bits take part (1..32).
+ * `d_keys` and `d_order` must not overlap (VSIM_ERR_INVALID if they do).
  * Scratch: call once with d_temp == NULL to receive the size in *temp_bytes.
  */
 int vsim_radix_sort_u32(const uint32_t* d_keys, uint32_t* d_order, uint32_t n, uint32_t key_bits,
@@ -402,8 +403,12 @@ int vsim_radix_sort_u32(const uint32_t* d_keys, uint32_t* d_order, uint32_t n, u
  * that loads the library until the process exits, and it sorts at most
  * 1048576 keys (more fails with VSIM_ERR_CAPACITY). The first call on each
  * device looks up the array's device address; make that first call before
- * any stream capture. All calls share the array: calls that overlap on the
- * GPU race, so serialise them. Same results as vsim_radix_sort_u32.
+ * any stream capture. The address is remembered per device and context: after
+ * a device reset (cudaDeviceReset, or the primary context made again) the
+ * next call looks it up once more, so make that call outside a capture too.
+ * All calls share the array: calls that overlap on the GPU race, so
+ * serialise them. `d_keys` and `d_order` must not overlap. Same results as
+ * vsim_radix_sort_u32.
  */
 int vsim_radix_sort_u32_noalloc(const uint32_t* d_keys, uint32_t* d_order, uint32_t n,
                                 uint32_t key_bits, void* stream);

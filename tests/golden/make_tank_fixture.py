@@ -5,9 +5,9 @@ node positions the reference recorded for it on its own GPU path
 (apps/simulator/test/motion-reference/recorded/tank.json, with the script
 of apps/simulator/test/motion-reference/scenarios.js:32-35).
 
-Run from the repository root with the reference at /root/reference:
+Run from the repository root, naming the reference checkout's root:
 
-    python tests/golden/make_tank_fixture.py [/root/reference]
+    python tests/golden/make_tank_fixture.py REFERENCE_ROOT
 
 The OBJ meshes and tank.json are read only here; the tests read the npz.
 """
@@ -23,7 +23,9 @@ sys.path.insert(0, str(ROOT / "visionary-sim_gb300"))
 
 from vsim import voxelize as vz  # noqa: E402
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_tank_fixture.py REFERENCE_ROOT")
+REF = Path(sys.argv[1])
 APP = REF / "apps" / "simulator"
 
 # tank.js:33-36 (JELLY, RUBBER) over material.js:69-77 (DEFAULT_MATERIAL).

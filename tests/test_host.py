@@ -5,6 +5,7 @@ import ctypes as C
 import math
 
 import numpy as np
+import pytest
 
 
 def test_exports_every_header_symbol(vsimlib):
@@ -212,3 +213,42 @@ def test_material_wave_speed(vsimlib):
     assert speed(1e7, 1000.0) > speed(1e5, 1000.0)
     assert speed(1e5, 4000.0) < speed(1e5, 1000.0)
     assert 5 < speed(1e5, 1000.0, 0.35) < 30
+
+
+def _cuda_present():
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+# The argument checks return before any device work; with a GPU present a
+# broken check would launch on the made-up addresses below, so this runs only
+# where there is none.
+@pytest.mark.skipif(_cuda_present(), reason="made-up device addresses; argument checks are tested without a GPU")
+def test_sort_entry_points_reject_bad_arguments(vsimlib):
+    lib = vsimlib.lib()
+    ok, rng_err, inv = vsimlib.VSIM_OK, vsimlib.VSIM_ERR_RANGE, vsimlib.VSIM_ERR_INVALID
+    keys, order = 0x10000, 0x20000  # never dereferenced
+    # the sort without allocation
+    noalloc = lib.vsim_radix_sort_u32_noalloc
+    assert noalloc(None, None, 0, 32, None) == ok  # nothing to sort
+    assert noalloc(keys, order, 10, 0, None) == rng_err
+    assert noalloc(keys, order, 10, 33, None) == rng_err
+    assert noalloc(None, order, 10, 32, None) == inv
+    assert noalloc(keys, None, 10, 32, None) == inv
+    assert noalloc(keys, keys, 10, 32, None) == inv  # in place
+    assert noalloc(keys, keys + 36, 10, 32, None) == inv  # order starts inside keys
+    assert noalloc(keys + 36, keys, 10, 32, None) == inv  # keys start inside order
+    assert b"overlap" in lib.vsim_last_error()
+    # the allocating sort, past its size query
+    need = C.c_size_t()
+    assert lib.vsim_radix_sort_u32(None, None, 10, 32, None, C.byref(need), None) == ok
+    temp = 0x30000
+    sort = lib.vsim_radix_sort_u32
+    assert sort(keys, order, 10, 0, temp, C.byref(need), None) == rng_err
+    assert sort(None, order, 10, 32, temp, C.byref(need), None) == inv
+    assert sort(keys, keys + 4, 10, 32, temp, C.byref(need), None) == inv
+    assert b"overlap" in lib.vsim_last_error()

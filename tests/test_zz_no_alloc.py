@@ -35,9 +35,11 @@ def test_no_alloc_sort_matches_allocating_sort(vsimlib, gpu):
 
     lib = vsimlib.lib()
     rng = np.random.default_rng(20261203)
-    cases = [(MAX_KEYS, 32), (300_001, 24)]
+    # two multi-pass sorts in a row, then a single 8-bit pass (keys straight
+    # to the order, no ping-pong through the scratch's key buffers)
+    cases = [(MAX_KEYS, 32), (300_001, 24), (4097, 8)]
     for call, (n, bits) in enumerate(cases):
-        keys = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+        keys = rng.integers(0, 2 ** bits, n, dtype=np.uint64).astype(np.uint32)
         keys[: n // 4] = keys[n // 2]  # a long run of equal keys: stability matters
         keys_dev = torch.from_numpy(keys.view(np.int32)).to(gpu)
         expected = allocating_sort(lib, torch, keys_dev, n, bits)

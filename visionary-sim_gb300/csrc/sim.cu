@@ -1015,41 +1015,61 @@ int vsim_tune(vsim_sim* s, uint32_t frames, uint32_t* block, uint32_t* brick) {
     CK(cudaMemcpyAsync(saved.data() + 8 * N, s->d.vel, N * 16, cudaMemcpyDeviceToHost, s->stream), "tune");
     CK(cudaStreamSynchronize(s->stream), "tune");
     const uint32_t steps = std::max<uint32_t>(1, uint32_t(std::lround(1.0 / 60.0 / s->clock.stepDuration)));
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0), "tune");
-    CK(cudaEventCreate(&e1), "tune");
+    // Events are released, and the state and launch shape put back, on every
+    // way out; a failed sweep leaves the shape the caller had.
+    struct Events {
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~Events() {
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+        }
+    } ev;
+    const uint32_t callerBlock = s->block, callerBrick = s->brick;
+    auto restore = [&](uint32_t bl, uint32_t br) {
+        int rc = vsim_set_launch_shape(s, bl, br);
+        cudaError_t e = cudaMemcpyAsync(s->d.pos, saved.data(), N * 16, cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->d.prev, saved.data() + 4 * N, N * 16, cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->d.vel, saved.data() + 8 * N, N * 16, cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess && rc == VSIM_OK) rc = cudaFail(e, "tune: restore state");
+        return rc;
+    };
+    // A failure inside the sweep: its error stays the reported one.
+    auto abandon = [&](int rc) {
+        const std::string why = vsim_last_error();
+        restore(callerBlock, callerBrick);
+        return fail(rc, why);
+    };
+    cudaError_t e;
+    if ((e = cudaEventCreate(&ev.a)) || (e = cudaEventCreate(&ev.b))) return cudaFail(e, "tune");
     float best = INFINITY;
-    uint32_t bestBlock = s->block, bestBrick = s->brick;
+    uint32_t bestBlock = callerBlock, bestBrick = callerBrick;
     const uint32_t bricks[3] = {0, 4, 8}, blocksz[3] = {128, 256, 512};
     for (uint32_t br : bricks)
         for (uint32_t bl : blocksz) {
             int rc = vsim_set_launch_shape(s, bl, br);
-            if (rc) return rc;
+            if (rc) return abandon(rc);
             rc = runFrame(s, steps);  // warm-up and graph capture
-            if (rc) return rc;
-            CK(cudaEventRecord(e0, s->stream), "tune");
+            if (rc) return abandon(rc);
+            if ((e = cudaEventRecord(ev.a, s->stream))) return abandon(cudaFail(e, "tune"));
             for (uint32_t f = 0; f < frames; f++) {
                 rc = runFrame(s, steps);
-                if (rc) return rc;
+                if (rc) return abandon(rc);
             }
-            CK(cudaEventRecord(e1, s->stream), "tune");
-            CK(cudaEventSynchronize(e1), "tune");
+            if ((e = cudaEventRecord(ev.b, s->stream)) || (e = cudaEventSynchronize(ev.b)))
+                return abandon(cudaFail(e, "tune"));
             float ms = 0;
-            CK(cudaEventElapsedTime(&ms, e0, e1), "tune");
+            if ((e = cudaEventElapsedTime(&ms, ev.a, ev.b))) return abandon(cudaFail(e, "tune"));
             if (ms < best) {
                 best = ms;
                 bestBlock = bl;
                 bestBrick = br;
             }
         }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    int rc = vsim_set_launch_shape(s, bestBlock, bestBrick);
+    const int rc = restore(bestBlock, bestBrick);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(s->d.pos, saved.data(), N * 16, cudaMemcpyHostToDevice, s->stream), "tune");
-    CK(cudaMemcpyAsync(s->d.prev, saved.data() + 4 * N, N * 16, cudaMemcpyHostToDevice, s->stream), "tune");
-    CK(cudaMemcpyAsync(s->d.vel, saved.data() + 8 * N, N * 16, cudaMemcpyHostToDevice, s->stream), "tune");
-    CK(cudaStreamSynchronize(s->stream), "tune");
     if (block) *block = bestBlock;
     if (brick) *brick = bestBrick;
     return VSIM_OK;
@@ -1455,6 +1475,8 @@ int vsim_radix_sort_u32(const uint32_t* d_keys, uint32_t* d_order, uint32_t n, u
     }
     if (*temp_bytes < need) return fail(VSIM_ERR_CAPACITY, "scratch smaller than the size query returned");
     if (n == 0) return VSIM_OK;
+    if (!d_keys || !d_order) return fail(VSIM_ERR_INVALID, "keys or order is NULL");
+    if (wordRangesOverlap(d_keys, d_order, n)) return fail(VSIM_ERR_INVALID, "keys and order overlap");
     CK(radixSortU32(d_keys, d_order, n, key_bits, d_temp, *temp_bytes, static_cast<cudaStream_t>(stream)),
        "radix sort");
     return VSIM_OK;

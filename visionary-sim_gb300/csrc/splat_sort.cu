@@ -499,11 +499,44 @@ constexpr size_t kNoAllocScratchBytes = sortTempBytes(kNoAllocMaxKeys);
 __device__ __align__(256) static unsigned char g_sortScratch[kNoAllocScratchBytes];
 
 // In host code `g_sortScratch` names a host-side stand-in, not device memory:
-// the device address comes from cudaGetSymbolAddress, looked up once per
-// device with that device current and cached here.
+// the device address comes from cudaGetSymbolAddress, looked up with the
+// device current and cached per device together with the identity of the
+// context it was looked up in. A device reset (cudaDeviceReset, or a primary
+// context torn down and made again) reloads the module and may move the
+// array; the next call sees a new context and looks the address up again.
 constexpr int kMaxDevices = 64;
 std::mutex g_scratchLock;
-void* g_scratchAddress[kMaxDevices] = {};
+struct ScratchEntry {
+    void* ptr;
+    unsigned long long context;  // 0: unknown, never trusted
+};
+ScratchEntry g_scratchAddress[kMaxDevices] = {};
+
+// The unique id of the calling thread's current context (cuCtxGetId), 0 when
+// there is none or the driver cannot say. Reached through the runtime's
+// driver entry points, so the library does not link libcuda itself.
+unsigned long long currentContextId() {
+    using GetCurrent = int (*)(void**);
+    using GetId = int (*)(void*, unsigned long long*);
+    static GetCurrent getCurrent = nullptr;
+    static GetId getId = nullptr;
+    static std::once_flag found;
+    std::call_once(found, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            getCurrent = reinterpret_cast<GetCurrent>(fn);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            getId = reinterpret_cast<GetId>(fn);
+    });
+    if (!getCurrent || !getId) return 0;
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (getCurrent(&ctx) != 0 || !ctx || getId(ctx, &id) != 0) return 0;
+    return id;
+}
 
 cudaError_t scratchAddress(void** out) {
     int device = 0;
@@ -511,15 +544,19 @@ cudaError_t scratchAddress(void** out) {
     if (e != cudaSuccess) return e;
     if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> hold(g_scratchLock);
-    if (!g_scratchAddress[device]) {
+    ScratchEntry& entry = g_scratchAddress[device];
+    const unsigned long long context = currentContextId();
+    if (!entry.ptr || context == 0 || entry.context != context) {
         void* ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_sortScratch);
+        e = cudaGetSymbolAddress(&ptr, g_sortScratch);  // makes the device's context current if none was
         if (e != cudaSuccess) return e;
-        g_scratchAddress[device] = ptr;
+        entry.ptr = ptr;
+        entry.context = context ? context : currentContextId();
     }
-    *out = g_scratchAddress[device];
+    *out = entry.ptr;
     return cudaSuccess;
 }
+
 
 }  // namespace
 
@@ -535,6 +572,7 @@ extern "C" int vsim_radix_sort_u32_noalloc(const uint32_t* d_keys, uint32_t* d_o
                                        "vsim_radix_sort_u32 with caller-provided scratch for more");
     if (n == 0) return VSIM_OK;
     if (!d_keys || !d_order) return fail(VSIM_ERR_INVALID, "keys or order is NULL");
+    if (wordRangesOverlap(d_keys, d_order, n)) return fail(VSIM_ERR_INVALID, "keys and order overlap");
     void* scratch = nullptr;
     cudaError_t e = scratchAddress(&scratch);
     if (e != cudaSuccess) return fail(VSIM_ERR_CUDA, std::string("scratch address: ") + cudaGetErrorString(e));

@@ -17,6 +17,13 @@ namespace vsim {
 int fail(int code, const std::string& msg);
 void clearError();
 
+// Whether [a, a + n) and [b, b + n) share a 32-bit word.
+inline bool wordRangesOverlap(const uint32_t* a, const uint32_t* b, uint32_t n) {
+    const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+    const uintptr_t len = uintptr_t(n) * sizeof(uint32_t);
+    return x < y + len && y < x + len;
+}
+
 // ---- constants of the discretisation ------------------------------------
 
 constexpr uint32_t kBucketSlots = 32;          // contacts.wgsl:75, visible entries per bucket

@@ -205,9 +205,51 @@ def roofline(sim, scene, hbm):
         "traffic": traffic,
         "bytes_per_launch": round(per_launch_bytes),
         "avg_launch_us": round(per_launch_s * 1e6, 3),
-        "isolated_launch_us": round(1e3 * ms / launches, 3),
+        "isolated_launch_us": round(1e3 * ms / (scene.substeps * scene.iterations *
+                                                 int(np.count_nonzero(sim.color_counts()))), 3),
         "method": "10 sweeps x 8 colour passes back to back in one graph, CUDA events at its ends",
     }, {k: {"ms": round(v[0], 4), "launches": v[1]} for k, v in prof.items()}, share
+
+
+# Algorithmic bytes of the contact kernels: what each must move once.
+# bin: record 16 + position 16 read, key 4 + rank 4 written, bucket count 8 (r/w)
+# segment: rank 4 + key 4 per record; count 4 + start 4 per occupied bucket
+# scatter: key 4 + rank 4 + start 4 read, entry 4 written
+# order: key, count, start 12 + record 16 + position 16 + substep start 16 + friction 4
+#        read; record 16 + position 16 + motion 16 + index 4 + bucket 4 written
+# gather: own entry 56, 27 neighbour buckets' count + start 8 each, every
+#         visible candidate's record 16 + position 16 + motion 16, correction 16 out
+CONTACT_BYTES = {"bin": (48, 0, 0), "segment": (8, 8, 0), "scatter": (16, 0, 0), "order": (120, 0, 0),
+                 "gather": (56 + 27 * 8 + 16, 0, 48)}  # (per record, per occupied bucket, per candidate)
+
+
+def contact_roofline(sim, hbm):
+    """The contact chain on the current positions (vsim_contact_census, one
+    launch of each kernel bracketed by events): its work counted from the
+    live grid -- records, occupied buckets, visible candidates -- and each
+    kernel's achieved bandwidth over its algorithmic bytes. Also the total by
+    the per-surface-node formula (key 8 B, an 8 B read+write per sort pass --
+    here 4 passes: bin, segment, scatter, order -- the 27 buckets' 8 B, 36 B
+    per candidate, 32 B to apply)."""
+    c = sim.contact_census()
+    r, b, k = c["records"], c["occupied_buckets"], c["candidates"]
+    per = {}
+    for name, (pr, pb, pc) in CONTACT_BYTES.items():
+        nbytes = pr * r + pb * b + pc * k
+        ms = c["ms"][name]
+        gbs = nbytes / (ms / 1e3) / 1e9 if ms > 0 else None
+        per[name] = {"bytes": nbytes, "us": round(ms * 1e3, 2), "achieved_gbs": round(gbs, 1) if gbs else None,
+                     "frac_of_measured_hbm": round(gbs / hbm, 4) if gbs else None}
+    formula = r * (8 + 4 * 16 + 27 * 8 + 32) + 36 * k
+    total_ms = sum(c["ms"].values())
+    return {"records": r, "occupied_buckets": b, "candidates": k,
+            "candidates_per_record": round(k / r, 2) if r else 0,
+            "kernels": per, "chain_us": round(total_ms * 1e3, 2),
+            "formula_bytes": formula,
+            "formula_gbs": round(formula / (total_ms / 1e3) / 1e9, 1) if total_ms else None,
+            "formula_frac_of_measured_hbm": round(formula / (total_ms / 1e3) / 1e9 / hbm, 4) if total_ms else None,
+            "method": "one contact chain on the bench body's current positions, each kernel bracketed by CUDA "
+                      "events (no overlap between kernels), then the grid emptied without moving a node"}
 
 
 def e2e(sim, scene, frames: int):
@@ -234,29 +276,37 @@ def e2e(sim, scene, frames: int):
     return times, 3 * n * 16, n * 16
 
 
-def cpu_baseline(scene, budget_s: float = 12.0):
+def cpu_baseline(scene, budget_s: float = 12.0, single_budget_s: float = 8.0):
+    """The float oracle on the bench workload, whole frames (substeps, splat
+    deformation, sort) for a bounded time: on every host thread (OpenMP over
+    a colour's cells and over nodes), then on one thread."""
     import pyoracle
 
+    def sample(threads, budget):
+        pyoracle.set_threads(threads)
+        orc = pyoracle.Oracle(scene, 32)
+        splats = scene.splats.get(0)
+        frames, t0 = 0, time.perf_counter()
+        while True:
+            orc.dispatch(scene.substeps)
+            if splats is not None:
+                m, q, s, *_ = splats
+                _means, _cov, keys = orc.splat_deform(0, m, q, s, VIEW)
+                pyoracle.stable_sort(keys)
+            frames += 1
+            elapsed = time.perf_counter() - t0
+            if elapsed >= budget or frames >= 50:
+                break
+        desc = (f"{frames} full frames ({scene.substeps} substeps + {len(splats[0]) if splats else 0} "
+                f"splat deformations and sort) of the bench workload, float oracle, {elapsed:.1f} s")
+        return units_per_frame(scene) * frames / elapsed, desc
+
     threads = os.cpu_count() or 1
+    value, desc = sample(threads, budget_s)
+    one, one_desc = sample(1, single_budget_s)
     pyoracle.set_threads(threads)
-    orc = pyoracle.Oracle(scene, 32)
-    splats = scene.splats.get(0)
-    frames, t0 = 0, time.perf_counter()
-    while True:
-        orc.dispatch(scene.substeps)
-        if splats is not None:
-            m, q, s, *_ = splats
-            _means, _cov, keys = orc.splat_deform(0, m, q, s, VIEW)
-            pyoracle.stable_sort(keys)
-        frames += 1
-        elapsed = time.perf_counter() - t0
-        if elapsed >= budget_s or frames >= 50:
-            break
-    value = units_per_frame(scene) * frames / elapsed
-    return {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"{frames} full frames ({scene.substeps} substeps + {len(splats[0]) if splats else 0} "
-                      f"splat deformations and sort) of the bench workload, float oracle, "
-                      f"{elapsed:.1f} s"}
+    return {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc,
+            "single_thread": {"value": one, "unit": METRIC, "cores": 1, "kind": "port", "sample": one_desc}}
 
 
 def reference_arm(scene, steps: int, warmup: int):
@@ -285,49 +335,130 @@ def reference_arm(scene, steps: int, warmup: int):
                       f"{elapsed:.1f} s"}
 
 
-def batched_vs_plain(frames: int, quick: bool):
-    """256 uneven boxes: one simulator stepping all of them with a captured
-    graph, against one simulator per body launched kernel by kernel."""
+def batched_vs_plain(frames: int, quick: bool, cpu: bool = True):
+    """The batching workload: 256 uneven boxes with 20k splats each. One
+    frame = 10 substeps, every splat deformed, the depth keys sorted.
+
+    - batched: one simulator stepping every body in the same launches, its
+      frame a captured graph (programmatic dependent launch), one deformation
+      and one sort over all 5.12M splats;
+    - plain: one simulator per body, each body its own launch sequence, its
+      own 20k splats deformed and sorted, in three forms: on one stream
+      launched kernel by kernel; on one stream with each body's frame a
+      captured graph; and each body on a stream of its own with its graph
+      (bodies overlap on the device).
+
+    Every arm is timed with CUDA events over `frames` frames after two
+    untimed ones: events on a common stream, with per-body streams joined to
+    it by events. `cpu_baseline`: the float oracle on all host cores, a
+    bounded sample of the same frames."""
     import torch
 
     import vsim.scenes as sc
     from vsim import Simulator
 
-    scene = sc.box_batch(32 if quick else 256, seed=2)
+    count = 32 if quick else 256
+    splats = 2_000 if quick else 20_000
+    t0 = time.perf_counter()
+    scene = sc.box_batch(count, seed=2, splats_per_body=splats)
+    gen_s = time.perf_counter() - t0
     units = units_per_frame(scene)
-    batch = Simulator(scene)
-    singles = []
-    for b in scene.bodies:
-        one = sc.Scene([b], scene.tank, step_duration=scene.step_duration, substeps=scene.substeps, contact=False)
-        sim = Simulator(one)
-        sim.set_graph(False)
-        sim.set_pdl(False)
-        singles.append(sim)
-    for _ in range(2):
-        batch.dispatch(scene.substeps)
-        for s in singles:
-            s.dispatch(scene.substeps)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(frames):
-        batch.dispatch(scene.substeps)
-    batch.synchronize()
-    t_batch = (time.perf_counter() - t0) / frames
-    t0 = time.perf_counter()
-    for _ in range(frames):
-        for s in singles:
-            s.dispatch(scene.substeps)
-    for s in singles:
-        s.synchronize()
-    t_plain = (time.perf_counter() - t0) / frames
+    main = torch.cuda.Stream()
+
+    def one_body(b):
+        one = sc.Scene([scene.bodies[b]], scene.tank, step_duration=scene.step_duration, substeps=scene.substeps,
+                       contact=False)
+        one.splats[0] = scene.splats[b]
+        return one
+
+    def timed(run, streams=None):
+        for _ in range(2):
+            run()
+        torch.cuda.synchronize()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(main)
+        for st in streams or []:
+            st.wait_event(start)
+        for _ in range(frames):
+            run()
+        for st in streams or []:
+            done = torch.cuda.Event()
+            done.record(st)
+            main.wait_event(done)
+        end.record(main)
+        end.synchronize()
+        return start.elapsed_time(end) / 1e3 / frames
+
     out = {"workload": f"{len(scene.bodies)} boxes, sides log-uniform 4-48 cells, {scene.cells} cells, "
-                       f"ground contact, 10 substeps/frame",
-           "batched": round(units / t_batch), "plain": round(units / t_plain),
-           "ratio": round(t_plain / t_batch, 2), "unit": METRIC}
+                       f"{splats} splats per body ({splats * len(scene.bodies)} in all), ground contact; one frame = "
+                       f"{scene.substeps} substeps + splat deformation + depth sort",
+           "unit": METRIC, "frames_timed": frames, "timing": "CUDA events on a common stream"}
+    batch = Simulator(scene, stream=main.cuda_stream)
+    t_batch = timed(lambda: run_frame(batch, scene))
+    out["batched"] = round(units / t_batch)
+    out["batched_frame_ms"] = round(t_batch * 1e3, 3)
+    batch.destroy()
+
+    arms = {}
+    bodies = [one_body(b) for b in range(len(scene.bodies))]
+    singles = [Simulator(one, stream=main.cuda_stream) for one in bodies]
+
+    def plain():
+        for sim, one in zip(singles, bodies):
+            run_frame(sim, one)
+
+    for s in singles:
+        s.set_graph(False)
+        s.set_pdl(False)
+    arms["plain_one_stream_no_graph"] = timed(plain)
+    for s in singles:
+        s.set_graph(True)
+        s.set_pdl(True)
+    arms["plain_one_stream_graph"] = timed(plain)
     for s in singles:
         s.destroy()
-    batch.destroy()
+    streams = [torch.cuda.Stream() for _ in bodies]
+    singles = [Simulator(one, stream=st.cuda_stream) for one, st in zip(bodies, streams)]
+    arms["plain_stream_per_body_graph"] = timed(plain, streams)
+    for s in singles:
+        s.destroy()
+    for name, t in arms.items():
+        out[name] = round(units / t)
+        out[name + "_frame_ms"] = round(t * 1e3, 3)
+    best = min(arms, key=arms.get)
+    out["ratio_vs_plain_no_graph"] = round(arms["plain_one_stream_no_graph"] / t_batch, 2)
+    out["ratio_vs_plain_graph"] = round(arms["plain_one_stream_graph"] / t_batch, 2)
+    out["ratio_vs_plain_stream_per_body"] = round(arms["plain_stream_per_body_graph"] / t_batch, 2)
+    out["ratio_vs_fastest_plain"] = round(arms[best] / t_batch, 2)
+    out["fastest_plain"] = best
+    out["scene_generation_s"] = round(gen_s, 1)
+    if cpu:
+        out["cpu_baseline"] = batch_cpu_baseline(scene, budget_s=6.0 if quick else 20.0)
     return out
+
+
+def batch_cpu_baseline(scene, budget_s: float):
+    """The float oracle, all host threads, on the batching workload: whole
+    frames (every body's substeps, every body's splats deformed, the depth
+    keys of all of them sorted together) until `budget_s` has passed."""
+    import pyoracle
+
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    orc = pyoracle.Oracle(scene, 32)
+    frames, t0 = 0, time.perf_counter()
+    while True:
+        orc.dispatch(scene.substeps)
+        keys = [orc.splat_deform(b, m, q, s, VIEW)[2] for b, (m, q, s, *_r) in scene.splats.items()]
+        if keys:
+            pyoracle.stable_sort(np.concatenate(keys))
+        frames += 1
+        elapsed = time.perf_counter() - t0
+        if elapsed >= budget_s or frames >= 20:
+            break
+    return {"value": round(units_per_frame(scene) * frames / elapsed), "unit": METRIC, "cores": threads,
+            "kind": "port", "sample": f"{frames} full frames of the batching workload, float oracle, "
+                                      f"{elapsed:.1f} s"}
 
 
 def single_body_pass(quick: bool, hbm: float):
@@ -772,9 +903,10 @@ def main():
     e2e_value = units_per_frame(scene) / statistics.mean(e2e_times) * world
 
     detail = {"kernel_groups_one_frame": groups, "time_share": share,
+              "contact_roofline": contact_roofline(sim, hbm),
               "frame_ms": {"min": round(min(times) * 1e3, 4), "median": round(statistics.median(times) * 1e3, 4)}}
     if rank == 0 and not args.no_batch:
-        detail["batching"] = batched_vs_plain(3, args.quick)
+        detail["batching"] = batched_vs_plain(10, args.quick, cpu=not args.no_cpu)
     if rank == 0 and not args.no_serve:
         detail["serving"] = serving_sweep(args.quick)
     if rank == 0 and not args.no_stress:

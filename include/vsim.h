@@ -305,6 +305,20 @@ int vsim_cfl_number(vsim_sim* sim, double* out);
  * exceeds `capacity` (then VSIM_ERR_CAPACITY).
  */
 int vsim_contact_pairs(vsim_sim* sim, uint32_t* pairs, size_t capacity, size_t* count);
+/* The contact gather's work on the current positions, for measurement (no
+   reference counterpart): one contact chain is run on the handle's stream
+   with each kernel bracketed by events, its grid is counted, and the grid is
+   emptied again without moving any node. `candidates` sums, over the live
+   records, the visible entries (at most 32 per bucket) of the record's 27
+   neighbour buckets -- what the gather reads. `ms` are the device times of
+   the five kernels: bin, segment, scatter, order, gather. */
+typedef struct vsim_census {
+    uint64_t records;           /* live surface records binned */
+    uint64_t occupied_buckets;
+    uint64_t candidates;
+    double ms[5];
+} vsim_census;
+int vsim_contact_census(vsim_sim* sim, vsim_census* out);
 /* Surface record table (node, body) of the contact constraint
    (bodyContact.js:325-340), `capacity` records at most. */
 int vsim_contact_surface(vsim_sim* sim, uint32_t* nodes, uint32_t* bodies, size_t capacity,

@@ -1,6 +1,7 @@
 """GPU parity at the workloads' full sizes: the bench's single large body
-with its 1M splats, the 256-body batch, and one substep of the stress
-scene, each compared with the float oracle node for node (`==`).
+with its 1M splats, the 256-body batch, and the stress scene (one substep
+from rest, and one whole frame once the sheet has landed on the blob), each
+compared with the float oracle node for node (`==`).
 
 These run the same kernels as tests/test_gpu_parity.py but at the launch
 shapes the bench uses (block sizes, gather mapping, streamed colour passes),
@@ -69,3 +70,26 @@ def test_stress_scene_one_substep(lib):
     sim.dispatch(1)
     orc.dispatch(1)
     assert_same(sim, orc, scene, "substep 1")
+
+
+def test_stress_scene_full_frame_in_contact(lib):
+    """The stress workload once the sheet lies on the blob (30 frames run on
+    the GPU first): the oracle takes that state, and both run one whole frame
+    -- 20 substeps of 2 Gauss-Seidel sweeps (lambda restarting each sweep,
+    xpbdCouple.wgsl:9-13) with dense self and body contact. Positions,
+    previous positions and velocities node for node, then the contact pairs
+    of the state reached."""
+    import vsim.scenes as sc
+
+    scene = sc.blob_and_sheet(192, seed=4, splats=0)
+    sim, orc = make(scene)
+    for _ in range(30):
+        sim.dispatch(scene.substeps)
+    pos, prev, vel = sim.read_state()
+    orc.set_state(pos, prev, vel)
+    sim.dispatch(scene.substeps)
+    orc.dispatch(scene.substeps)
+    assert_same(sim, orc, scene, "frame 31 (20 substeps x 2 sweeps)")
+    pairs = sim.contact_pairs()
+    assert len(pairs) > 10_000, "the sheet and blob are not in contact yet"
+    assert np.array_equal(pairs, orc.contact_pairs())

@@ -165,6 +165,17 @@ cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, const Span& 
 cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drivenCount);
 cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, const Span& span,
                           bool limitOnly, const StretchLengths& lens);
+
+// The streaming colour pass (elasticStreamKernel): blocks of kStreamBlock
+// threads, kStreamBlocksPerSm of them per SM (what the ~127 registers of a
+// cell allow). A dense pass of at least two cells per resident thread
+// streams.
+constexpr uint32_t kStreamBlock = 128;
+constexpr uint32_t kStreamBlocksPerSm = 4;
+inline bool streamsColourPass(uint32_t count, uint32_t sms) {
+    return count >= 2 * kStreamBlocksPerSm * sms * kStreamBlock;
+}
+
 // The substep's closing pass; with `contact` it first applies the contact
 // corrections and empties the grid, with `predictNext` it goes on into the
 // next substep's prediction.
@@ -172,9 +183,15 @@ cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span&
                            bool predictNext);
 // `records` covers the surface records of the stepped bodies; at most
 // `recordItems` of them are binned. `mapping` is a VSIM_GATHER_* value.
+// `marks`, when given, are six events recorded around the five kernels (before
+// bin, between each, after the gather).
 cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& records, uint32_t recordItems,
                           int mapping, ContactMode mode, uint32_t* pairs, uint32_t capacity,
-                          unsigned long long* pairCount);
+                          unsigned long long* pairCount, cudaEvent_t* marks = nullptr);
+// After a Solve-mode contact chain: counts the gather's work on the grid it
+// built (out[0] live records, out[1] visible candidates, out[2] occupied
+// buckets; added to) and empties the grid without applying corrections.
+cudaError_t launchCensus(const LaunchCtx& c, const DeviceState& s, const Span& records, unsigned long long* out);
 cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos);
 cudaError_t launchZeroW(cudaStream_t st, const uint32_t* nodes, uint32_t n, float4* pos);
 cudaError_t launchRefreshW(cudaStream_t st, uint32_t first, uint32_t n, const float* base, float4* pos);

@@ -577,7 +577,7 @@ int createSim(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, v
     CK(allocN(&d.cursor, 1), "allocate contact cursor");
     CK(allocN(&d.driven, VSIM_MAX_DRIVEN), "allocate drive");
     CK(allocN(&d.drivenOffset, VSIM_MAX_DRIVEN), "allocate drive");
-    CK(allocN(&s->pairCount, 1), "allocate pair counter");
+    CK(allocN(&s->pairCount, 4), "allocate pair counter");  // [0] pairs, [1..3] the contact census
     CK(cudaMallocHost(&s->activePinned, s->activeHost.size() * 4), "allocate staging");
     CK(cudaMallocHost(&s->grabsPinned, s->grabsHost.size() * 16), "allocate staging");
 
@@ -1141,6 +1141,42 @@ int vsim_contact_pairs(vsim_sim* s, uint32_t* pairs, size_t capacity, size_t* co
         CK(cudaMemcpy(pairs, s->pairs, copied * 8, cudaMemcpyDeviceToHost), "copy pairs");
     *count = size_t(total);
     return total > capacity ? fail(VSIM_ERR_CAPACITY, "pair buffer too small") : VSIM_OK;
+}
+
+int vsim_contact_census(vsim_sim* s, vsim_census* out) {
+    SIM_GUARD(s);
+    if (!out) return fail(VSIM_ERR_INVALID, "out is NULL");
+    std::memset(out, 0, sizeof *out);
+    if (s->surfaceCount == 0 || !s->contact) return VSIM_OK;
+    int rc = syncParams(s);
+    if (rc) return rc;
+    struct Marks {
+        cudaEvent_t e[6] = {};
+        ~Marks() {
+            for (cudaEvent_t x : e)
+                if (x) cudaEventDestroy(x);
+        }
+    } m;
+    for (cudaEvent_t& x : m.e) CK(cudaEventCreate(&x), "census events");
+    unsigned long long* counts = s->pairCount + 1;
+    CK(cudaMemsetAsync(counts, 0, 3 * sizeof(unsigned long long), s->stream), "census");
+    const LaunchCtx c{s->stream, false, s->sms};
+    CK(launchContact(c, s->d, s->dense.records, s->surfaceCount, s->gatherMapping, ContactMode::Solve, nullptr, 0,
+                     nullptr, m.e),
+       "census contact");
+    CK(launchCensus(c, s->d, s->dense.records, counts), "census");
+    unsigned long long host[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(host, counts, sizeof host, cudaMemcpyDeviceToHost, s->stream), "census");
+    CK(cudaStreamSynchronize(s->stream), "census");
+    out->records = host[0];
+    out->candidates = host[1];
+    out->occupied_buckets = host[2];
+    for (int k = 0; k < 5; k++) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, m.e[k], m.e[k + 1]), "census timing");
+        out->ms[k] = ms;
+    }
+    return VSIM_OK;
 }
 
 int vsim_contact_surface(vsim_sim* s, uint32_t* nodes, uint32_t* bodies, size_t capacity, size_t* count) {

@@ -158,6 +158,65 @@ __device__ __forceinline__ void projectTet(V (&p)[8], const V (&prev)[8], const 
     p[i3] = moved(p[i3], d3, h3, lx, ly, w3);
 }
 
+// The constants of a cell's body that project.wgsl:64-73 derives.
+struct CellConsts {
+    float alphaDev, alphaHyd, gamma, relax, restScale, h, maxStretch;
+};
+
+__device__ __forceinline__ CellConsts cellConsts(const DevBody* b) {
+    return CellConsts{b->alphaDev, b->alphaHyd, b->gamma, b->relax, b->restScale, b->h, b->maxStretch};
+}
+
+// project.wgsl:35-184 on one cell held in registers: the six tetrahedra in
+// Kuhn order (unless LIMIT_ONLY), then, with maxStretch > 1, two sweeps of
+// the unilateral length limit over all 28 corner pairs (project.wgsl:162-179).
+template <bool LIMIT_ONLY>
+__device__ __forceinline__ void solveCell(V (&p)[8], const V (&prev)[8], const float (&w)[8], const CellConsts& k,
+                                          const StretchLengths& lens) {
+    if (!LIMIT_ONLY) {
+        const float s = k.restScale, ns = -s;
+        projectTet<0>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax);
+        projectTet<1>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax);
+        projectTet<2>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax);
+        projectTet<3>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax);
+        projectTet<4>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax);
+        projectTet<5>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax);
+    }
+    if (k.maxStretch > 1.0f) {
+        for (int sweep = 0; sweep < 2; sweep++) {
+#pragma unroll
+            for (int a = 0; a < 8; a++) {
+#pragma unroll
+                for (int bb = a + 1; bb < 8; bb++) {
+                    const V delta = p[bb] - p[a];
+                    const float len = length(delta);
+                    const float maximum = lens.len[__popc(a ^ bb) - 1] * k.h * k.maxStretch;
+                    const float weight = w[a] + w[bb];
+                    if (len > maximum && weight > 0.0f) {
+                        const V correction = delta * ((len - maximum) / (len * weight));
+                        p[a] = p[a] + w[a] * correction;
+                        p[bb] = p[bb] - w[bb] * correction;
+                    }
+                }
+            }
+        }
+    }
+}
+
+// The eight corner nodes of a cell entry (corner-0 node, body, y stride, z
+// stride), in corners.js order.
+__device__ __forceinline__ void cornerNodes(uint4 e, uint32_t (&ids)[8]) {
+    const uint32_t nx = e.z, nxy = e.w, n0 = e.x;
+    ids[0] = n0;
+    ids[1] = n0 + 1;
+    ids[2] = n0 + nx;
+    ids[3] = n0 + nx + 1;
+    ids[4] = n0 + nxy;
+    ids[5] = n0 + nxy + 1;
+    ids[6] = n0 + nxy + nx;
+    ids[7] = n0 + nxy + nx + 1;
+}
+
 // ------------------------------------------------------------- kernels --
 
 // predict.wgsl:19-36 over the active nodes.
@@ -235,22 +294,17 @@ __global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ c
     struct Pre {
         uint4 entry;
         uint32_t live;
-        float maxStretch, alphaDev, alphaHyd, gamma, relax, restScale, h;
+        CellConsts k;
     };
     auto pre = [&](uint32_t slot) {
         const uint4 entry = cells[slot];
-        const DevBody* b = bodies + entry.y;
-        return Pre{entry, bodyActive[entry.y], b->maxStretch, b->alphaDev, b->alphaHyd, b->gamma, b->relax,
-                   b->restScale, b->h};
+        return Pre{entry, bodyActive[entry.y], cellConsts(bodies + entry.y)};
     };
     forEachItemAfterWait(work, pre, [&](uint32_t, const Pre& q) {
         if (!q.live) return;
-        const uint4 entry = q.entry;
-        const float maxStretch = q.maxStretch;
-        if (LIMIT_ONLY && !(maxStretch > 1.0f)) return;
-        const uint32_t nx = entry.z, nxy = entry.w, n0 = entry.x;
-        const uint32_t ids[8] = {n0,       n0 + 1,       n0 + nx,       n0 + nx + 1,
-                                 n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
+        if (LIMIT_ONLY && !(q.k.maxStretch > 1.0f)) return;
+        uint32_t ids[8];
+        cornerNodes(q.entry, ids);
         V p[8], prev[8];
         float w[8];
 #pragma unroll
@@ -261,40 +315,7 @@ __global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ c
         }
 #pragma unroll
         for (int c = 0; c < 8; c++) prev[c] = xyz(prevState[ids[c]]);
-
-        if (!LIMIT_ONLY) {
-            const float alphaDev = q.alphaDev, alphaHyd = q.alphaHyd, gamma = q.gamma, relax = q.relax;
-            const float s = q.restScale, ns = -s;
-            projectTet<0>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            projectTet<1>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            projectTet<2>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            projectTet<3>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            projectTet<4>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            projectTet<5>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-        }
-
-        // project.wgsl:162-179: unilateral length limit over all 28 corner pairs.
-        if (maxStretch > 1.0f) {
-            const float h = q.h;
-            for (int sweep = 0; sweep < 2; sweep++) {
-#pragma unroll
-                for (int a = 0; a < 8; a++) {
-#pragma unroll
-                    for (int bb = a + 1; bb < 8; bb++) {
-                        const V delta = p[bb] - p[a];
-                        const float len = length(delta);
-                        const float maximum = lens.len[__popc(a ^ bb) - 1] * h * maxStretch;
-                        const float weight = w[a] + w[bb];
-                        if (len > maximum && weight > 0.0f) {
-                            const V correction = delta * ((len - maximum) / (len * weight));
-                            p[a] = p[a] + w[a] * correction;
-                            p[bb] = p[bb] - w[bb] * correction;
-                        }
-                    }
-                }
-            }
-        }
-
+        solveCell<LIMIT_ONLY>(p, prev, w, q.k, lens);
 #pragma unroll
         for (int c = 0; c < 8; c++) pos[ids[c]] = withW(p[c], w[c]);
     });
@@ -306,8 +327,6 @@ __global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ c
 // it solves the current one, so the gathers' latency hides behind the
 // arithmetic instead of stalling the warp. Cells of one colour share no
 // node, so reading ahead is safe. Same arithmetic as elasticKernel.
-constexpr uint32_t kStreamBlock = 128;
-constexpr uint32_t kStreamBlocksPerSm = 4;  // what the ~127 registers of a cell allow
 
 __device__ __forceinline__ void copyAsync16(float4* dst, const float4* src) {
     const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
@@ -367,38 +386,9 @@ __global__ void __launch_bounds__(kStreamBlock) elasticStreamKernel(const uint4*
             fetch(entry, zero);
         }
         if (bodyActive[cur.y]) {
-            const DevBody* b = bodies + cur.y;
-            const float alphaDev = b->alphaDev, alphaHyd = b->alphaHyd, gamma = b->gamma, relax = b->relax;
-            const float s = b->restScale, ns = -s, maxStretch = b->maxStretch;
-            projectTet<0>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            projectTet<1>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            projectTet<2>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            projectTet<3>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            projectTet<4>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            projectTet<5>(p, prev, w, s, ns, alphaDev, alphaHyd, gamma, relax);
-            if (maxStretch > 1.0f) {
-                const float h = b->h;
-                for (int sweep = 0; sweep < 2; sweep++) {
-#pragma unroll
-                    for (int a = 0; a < 8; a++) {
-#pragma unroll
-                        for (int bb = a + 1; bb < 8; bb++) {
-                            const V delta = p[bb] - p[a];
-                            const float len = length(delta);
-                            const float maximum = lens.len[__popc(a ^ bb) - 1] * h * maxStretch;
-                            const float weight = w[a] + w[bb];
-                            if (len > maximum && weight > 0.0f) {
-                                const V correction = delta * ((len - maximum) / (len * weight));
-                                p[a] = p[a] + w[a] * correction;
-                                p[bb] = p[bb] - w[bb] * correction;
-                            }
-                        }
-                    }
-                }
-            }
-            const uint32_t nx = cur.z, nxy = cur.w, n0 = cur.x;
-            const uint32_t ids[8] = {n0,       n0 + 1,       n0 + nx,       n0 + nx + 1,
-                                     n0 + nxy, n0 + nxy + 1, n0 + nxy + nx, n0 + nxy + nx + 1};
+            solveCell<false>(p, prev, w, cellConsts(bodies + cur.y), lens);
+            uint32_t ids[8];
+            cornerNodes(cur, ids);
 #pragma unroll
             for (int c = 0; c < 8; c++) pos[ids[c]] = withW(p[c], w[c]);
         }
@@ -948,6 +938,38 @@ __global__ void settleKernel(const FrameParams* __restrict__ fp, Work work, cons
     });
 }
 
+// The gather's work on the current grid, for measurement: per live record,
+// its 27 neighbour buckets' visible entries (min(count, kBucketSlots) each,
+// what collideKernel reads), summed into out[1]; live records into out[0],
+// occupied buckets (their first-arriving records) into out[2]. Runs between
+// the gather and the pass that empties the grid.
+__global__ void censusKernel(Work work, const uint4* __restrict__ surf, const DevBody* __restrict__ bodies,
+                             const uint32_t* __restrict__ key, const uint32_t* __restrict__ rank,
+                             const uint32_t* __restrict__ count, unsigned long long* __restrict__ out) {
+    forEachItem(work, [&](uint32_t r) {
+        const uint32_t b = key[r];
+        if (b == kIdle) return;
+        const DevBody* g = bodies + surf[r].y;
+        const uint32_t linear = b - g->gridBase;
+        const uint32_t z = divBy(linear, g->divXY);
+        const uint32_t rest = linear - z * (g->gridDims[0] * g->gridDims[1]);
+        const uint32_t y = divBy(rest, g->divX);
+        const int c[3] = {int(rest - y * g->gridDims[0]), int(y), int(z)};
+        unsigned long long seen = 0;
+        for (int q = 0; q < 27; q++) {
+            const int x = c[0] + q % 3 - 1, yy = c[1] + (q / 3) % 3 - 1, zz = c[2] + q / 9 - 1;
+            if (x < 0 || yy < 0 || zz < 0 || x >= int(g->gridDims[0]) || yy >= int(g->gridDims[1]) ||
+                zz >= int(g->gridDims[2]))
+                continue;
+            const uint32_t n = count[g->gridBase + uint32_t(x) + g->gridDims[0] * (uint32_t(yy) + g->gridDims[1] * uint32_t(zz))];
+            seen += n < kBucketSlots ? n : kBucketSlots;
+        }
+        atomicAdd(&out[0], 1ull);
+        atomicAdd(&out[1], seen);
+        if (rank[r] == 0) atomicAdd(&out[2], 1ull);
+    });
+}
+
 // ------------------------------------------------------- node utilities --
 
 // pos.w := base[n] for a list of nodes (restoring a released hold).
@@ -1030,9 +1052,7 @@ cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drive
 
 cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, const Span& sp,
                           bool limitOnly, const StretchLengths& lens) {
-    // A dense pass of at least two cells per resident thread streams.
-    const uint32_t resident = kStreamBlocksPerSm * c.sms * kStreamBlock;
-    if (!limitOnly && !sp.work.table && sp.work.count >= 2 * resident)
+    if (!limitOnly && !sp.work.table && streamsColourPass(sp.work.count, c.sms))
         return launch(c, elasticStreamKernel, std::min(blocks(sp.work.count, kStreamBlock), kStreamBlocksPerSm * c.sms),
                       kStreamBlock,
                       cells, sp.work.count, s.bodies, (const uint32_t*)s.bodyActive, s.pos, (const float4*)s.prev,
@@ -1059,24 +1079,30 @@ cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span&
 // the grid itself.
 cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& r, uint32_t recordItems,
                           int mapping, ContactMode mode, uint32_t* pairs, uint32_t capacity,
-                          unsigned long long* pairCount) {
+                          unsigned long long* pairCount, cudaEvent_t* marks) {
     const uint32_t g = r.grid, b = r.block;
     const Work w = r.work;
     cudaError_t e;
+    auto mark = [&](int i) { return marks ? cudaEventRecord(marks[i], c.stream) : cudaSuccess; };
+    if ((e = mark(0))) return e;
     if ((e = launch(c, binKernel, g, b, s.fp, w, s.surf, (const DevBody*)s.bodies, (const uint32_t*)s.bodyActive,
                     (const float4*)s.pos, s.key, s.rank, s.count)))
         return e;
+    if ((e = mark(1))) return e;
     if ((e = launch(c, allocKernel, g, b, s.fp, w, (const uint32_t*)s.key, (const uint32_t*)s.rank,
                     (const uint32_t*)s.count, s.start, s.cursor)))
         return e;
+    if ((e = mark(2))) return e;
     if ((e = launch(c, scatterKernel, g, b, s.fp, w, (const uint32_t*)s.key, (const uint32_t*)s.rank,
                     (const uint32_t*)s.start, s.entries)))
         return e;
+    if ((e = mark(3))) return e;
     if ((e = launch(c, canonKernel, g, b, s.fp, w, (const uint32_t*)s.key, (const uint32_t*)s.rank,
                     (const uint32_t*)s.start, (const uint32_t*)s.count, s.entries, (const uint4*)s.surf,
                     (const float4*)s.pos, (const float4*)s.prev, (const DevBody*)s.bodies, s.sMeta, s.sPos,
                     s.sMoved, s.sRec, s.sKey)))
         return e;
+    if ((e = mark(4))) return e;
     // The gather runs over the bucket-ordered entries (at most recordItems),
     // a warp each while fewer than 2048 per SM, else a thread each.
     const uint32_t cg = std::min(blocks(recordItems, 8), 64 * c.sms);
@@ -1091,10 +1117,22 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& 
     };
     if (mode == ContactMode::Pairs) {
         if ((e = collide(collideKernel<true>, pairs, capacity, pairCount))) return e;
+        if ((e = mark(5))) return e;
         return launch(c, settleKernel, g, b, s.fp, w, s.surf, (const uint32_t*)s.key, (const float4*)s.delta, s.pos,
                       s.count, s.cursor, 0);
     }
-    return collide(collideKernel<false>, (uint32_t*)nullptr, 0u, (unsigned long long*)nullptr);
+    if ((e = collide(collideKernel<false>, (uint32_t*)nullptr, 0u, (unsigned long long*)nullptr))) return e;
+    return mark(5);
+}
+
+cudaError_t launchCensus(const LaunchCtx& c, const DeviceState& s, const Span& r, unsigned long long* out) {
+    cudaError_t e_;
+    if ((e_ = launch(c, censusKernel, r.grid, r.block, r.work, (const uint4*)s.surf, (const DevBody*)s.bodies,
+                     (const uint32_t*)s.key, (const uint32_t*)s.rank, (const uint32_t*)s.count, out)))
+        return e_;
+    // empty the grid without applying the corrections
+    return launch(c, settleKernel, r.grid, r.block, s.fp, r.work, s.surf, (const uint32_t*)s.key,
+                  (const float4*)s.delta, s.pos, s.count, s.cursor, 0);
 }
 
 cudaError_t launchRestoreW(cudaStream_t st, const uint32_t* nodes, uint32_t n, const float* base, float4* pos) {

@@ -87,6 +87,11 @@ class Stats(C.Structure):
     ]
 
 
+class ContactCensus(C.Structure):
+    _fields_ = [("records", C.c_uint64), ("occupied_buckets", C.c_uint64), ("candidates", C.c_uint64),
+                ("ms", C.c_double * 5)]
+
+
 class Profile(C.Structure):
     _fields_ = [("ms", C.c_double * 8), ("launches", C.c_uint32 * 8)]
 
@@ -217,6 +222,7 @@ SIGNATURES = {
     "vsim_cfl_number": (C.c_int, [_P, _D]),
     "vsim_contact_pairs": (C.c_int, [_P, _U, _SZ, C.POINTER(_SZ)]),
     "vsim_contact_surface": (C.c_int, [_P, _U, _U, _SZ, C.POINTER(_SZ)]),
+    "vsim_contact_census": (C.c_int, [_P, C.POINTER(ContactCensus)]),
     "vsim_splats_bind": (C.c_int, [_P, C.c_uint32, _F, _F, _F, C.c_uint32]),
     "vsim_splats_count": (C.c_uint32, [_P]),
     "vsim_splats_deform": (C.c_int, [_P, _F]),

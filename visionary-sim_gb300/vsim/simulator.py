@@ -321,6 +321,16 @@ class Simulator:
         check(lib().vsim_contact_surface(self._h, uptr(nodes), uptr(bodies), n, C.byref(count)))
         return nodes, bodies
 
+    def contact_census(self) -> dict:
+        """The gather's work on the current positions (vsim_contact_census):
+        live records, occupied buckets, visible candidates, and each contact
+        kernel's device time in ms. Moves no node."""
+        c = _ffi.ContactCensus()
+        check(lib().vsim_contact_census(self._h, C.byref(c)))
+        return {"records": int(c.records), "occupied_buckets": int(c.occupied_buckets),
+                "candidates": int(c.candidates),
+                "ms": dict(zip(("bin", "segment", "scatter", "order", "gather"), (float(v) for v in c.ms)))}
+
     # -- profiling --------------------------------------------------------------
     def profile_frame(self, steps: int, splats: bool = False, view_dir=(0.0, 0.0, -1.0)) -> dict:
         """One frame with every kernel group timed by CUDA events:

@@ -677,16 +677,22 @@ def drift(frames: int = 300):
             "final_max_abs_m": float(np.max(np.abs(g - r)))}
 
 
-def serving_sweep(quick: bool, seconds_per_point: float = 3.0, settle_frames: int = 30):
+def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, settle_frames: int = 30,
+                  repeats_at_70: int = 3):
     """Continuous batching under load: a pool of sessions resident on the
     GPU; requests advance a session k ~ U{1..4} frames, half of them dragging
     a random surface node along a seeded Bezier curve at 0.5 m/s. Every
     session first runs `settle_frames` frames (all at once), so that the
     bodies have landed and flattened -- the state they spend their life in,
     with far more self contact than at rest -- before anything is measured.
-    Saturation is then measured closed-loop (every session always has a
-    request), then Poisson arrivals at fractions of it. Frame latency of a
-    request = (completion - arrival) / k."""
+
+    For each tick budget (occupied cells one tick may step, 0 = no cap;
+    vsim_server_set_tick_budget): saturation measured closed-loop (every
+    session always has a request), then Poisson arrivals at 25/50/70/90 % of
+    that saturation, the 70 % point `repeats_at_70` times. Each of these
+    starts from the same settled state (every session checkpointed after the
+    settling frames and written back before the measurement). Frame latency
+    of a request = (completion - arrival) / k."""
     import vsim.scenes as sc
     from vsim.server import Server
 
@@ -709,39 +715,53 @@ def serving_sweep(quick: bool, seconds_per_point: float = 3.0, settle_frames: in
             drag = (node, control, speed)
         return frames, drag
 
+    def drain():
+        while server.stats()["pending"]:
+            server.tick()
+            server.poll()
+
     t0 = time.perf_counter()
+    server.set_tick_budget(0)
     for s in range(admitted):
         server.submit(s, settle_frames)
-    while server.stats()["pending"]:
-        server.tick()
-        server.poll()
+    drain()
     settle_s = time.perf_counter() - t0
+    # Every measurement starts from this settled state: the bodies keep
+    # deforming under the drags, and a saturation measured on one state and
+    # loads applied to a later, costlier one would not be fractions of the
+    # same capacity.
+    checkpoint = [server.read_state(s) for s in range(admitted)]
 
-    # Saturation: keep every session busy.
-    arrival = {}
-    for s in range(admitted):
-        f, d = request(s)
-        arrival[server.submit(s, f, d)] = server.clock()
-    start = server.clock()
-    frames_done, requests_done, ticks = 0, 0, 0
-    while server.clock() - start < seconds_per_point:
-        server.tick()
-        ticks += 1
-        for c in server.poll():
-            requests_done += 1
-            frames_done += c["frames"]
-            f, d = request(c["session"])
-            arrival[server.submit(c["session"], f, d)] = server.clock()
-    sat_elapsed = server.clock() - start
-    sat_rate = requests_done / sat_elapsed
-    stats0 = server.stats()
-    while server.stats()["pending"]:
-        server.tick()
-        server.poll()
-    cells0 = server.stats()["cell_updates"]
+    def restore():
+        for s in range(admitted):
+            server.write_state(s, *checkpoint[s])
 
-    points = []
-    for frac in (0.25, 0.5, 0.7, 0.9):
+    def saturation():
+        restore()
+        arrival = {}
+        for s in range(admitted):
+            f, d = request(s)
+            arrival[server.submit(s, f, d)] = server.clock()
+        start = server.clock()
+        frames_done, requests_done, ticks = 0, 0, 0
+        c0 = server.stats()["cell_updates"]
+        while server.clock() - start < seconds_per_point:
+            server.tick()
+            ticks += 1
+            for c in server.poll():
+                requests_done += 1
+                frames_done += c["frames"]
+                f, d = request(c["session"])
+                arrival[server.submit(c["session"], f, d)] = server.clock()
+        elapsed = server.clock() - start
+        cells = server.stats()["cell_updates"] - c0
+        drain()
+        return {"requests_per_s": round(requests_done / elapsed, 1),
+                "session_frames_per_s": round(frames_done / elapsed, 1), "ticks": ticks,
+                "cell_updates_per_s": round(cells / elapsed)}
+
+    def point(frac, sat_rate):
+        restore()
         lam = frac * sat_rate
         arrival = {}
         lat, req_lat = [], []
@@ -764,7 +784,7 @@ def serving_sweep(quick: bool, seconds_per_point: float = 3.0, settle_frames: in
             elif next_arrival >= end:
                 break
             else:
-                time.sleep(max(0.0, min(next_arrival - server.clock(), 0.001)))
+                time.sleep(max(0.0, min(next_arrival - server.clock(), 0.0001)))
             for c in server.poll():
                 total = c["completed"] - arrival.pop(c["request"])
                 req_lat.append(total)
@@ -774,25 +794,34 @@ def serving_sweep(quick: bool, seconds_per_point: float = 3.0, settle_frames: in
         ticks_run = max(1, st_after["ticks"] - st_before["ticks"])
         tick_ms = {k: round(1e3 * (st_after[f"{k}_seconds"] - st_before[f"{k}_seconds"]) / ticks_run, 3)
                    for k in ("tick", "prepare", "frame")}
-        points.append({"load": frac, "offered_req_per_s": round(lam, 1),
-                       "frame_latency_ms": {"p50": round(1e3 * float(np.percentile(lat, 50)), 3),
-                                            "p99": round(1e3 * float(np.percentile(lat, 99)), 3)},
-                       "request_latency_ms": {"p50": round(1e3 * float(np.percentile(req_lat, 50)), 3),
-                                              "p99": round(1e3 * float(np.percentile(req_lat, 99)), 3)},
-                       "requests": len(lat),
-                       "sessions_per_tick": round(float(np.mean(stepped)), 1) if stepped else 0,
-                       "mean_tick_ms": tick_ms,
-                       "cell_updates_per_s": round((server.stats()["cell_updates"] - c_before) / elapsed)})
+        return {"load": frac, "offered_req_per_s": round(lam, 1),
+                "frame_latency_ms": {"p50": round(1e3 * float(np.percentile(lat, 50)), 3),
+                                     "p99": round(1e3 * float(np.percentile(lat, 99)), 3)},
+                "request_latency_ms": {"p50": round(1e3 * float(np.percentile(req_lat, 50)), 3),
+                                       "p99": round(1e3 * float(np.percentile(req_lat, 99)), 3)},
+                "requests": len(lat),
+                "sessions_per_tick": round(float(np.mean(stepped)), 1) if stepped else 0,
+                "mean_tick_ms": tick_ms,
+                "cell_updates_per_s": round((server.stats()["cell_updates"] - c_before) / elapsed)}
+
+    runs = {}
+    for budget in budgets:
+        server.set_tick_budget(budget)
+        sat = saturation()
+        points = []
+        for frac in (0.25, 0.5, 0.7, 0.9):
+            for _ in range(repeats_at_70 if frac == 0.7 else 1):
+                points.append(point(frac, sat["requests_per_s"]))
+        p99_70 = [p["frame_latency_ms"]["p99"] for p in points if p["load"] == 0.7]
+        runs[str(budget)] = {"tick_cell_budget": budget, "saturation": sat, "sweep": points,
+                             "p99_frame_latency_ms_at_70pct": {"max": max(p99_70), "all": p99_70}}
     st = server.stats()
     server.destroy()
     return {"workload": f"{admitted} sessions ({count} offered), noise blobs on 8^3-64^3 grids, "
                         f"{sum(b.cell_count for b in bodies[:admitted])} cells resident, "
                         f"{st['resident_bytes'] / 1e9:.2f} GB of the 150 GB budget; k ~ U{{1..4}} frames, "
                         f"50% with a Bezier drag at 0.5 m/s",
-            "saturation": {"requests_per_s": round(sat_rate, 1),
-                           "session_frames_per_s": round(frames_done / sat_elapsed, 1),
-                           "ticks": ticks, "cell_updates_per_s": round(stats0["cell_updates"] / sat_elapsed)},
-            "sweep": points, "settle": {"frames": settle_frames, "seconds": round(settle_s, 1)},
+            "by_tick_budget": runs, "settle": {"frames": settle_frames, "seconds": round(settle_s, 1)},
             "pool_generation_s": round(gen_s, 1)}
 
 
@@ -811,6 +840,10 @@ def main():
     ap.add_argument("--stress-only", action="store_true", help="only the stress workload's frames (for captures)")
     ap.add_argument("--cloud-only", action="store_true", help="only the cloud voxeliser section (for captures)")
     ap.add_argument("--tick-sweep", action="store_true", help="only the server's tick time against sessions per tick")
+    ap.add_argument("--serve-only", action="store_true", help="only the serving sweep")
+    ap.add_argument("--batch-only", action="store_true", help="only the batching comparison")
+    ap.add_argument("--tick-budgets", default=None,
+                    help="comma-separated tick cell budgets for the serving sweep (0 = no cap)")
     ap.add_argument("--capture-tick", type=int, default=None, metavar="K",
                     help="profiler capture mode: one server tick of K sessions, for `ncu --profile-from-start off`")
     ap.add_argument("--capture-after", type=int, default=None, metavar="N",
@@ -860,6 +893,13 @@ def main():
     if args.cloud_only:
         print(json.dumps({"cloud_voxelize": cloud_voxelize(args.quick)}))
         return
+    budgets = [int(float(v)) for v in args.tick_budgets.split(",")] if args.tick_budgets else [0]
+    if args.serve_only:
+        print(json.dumps({"serving": serving_sweep(args.quick, budgets)}))
+        return
+    if args.batch_only:
+        print(json.dumps({"batching": batched_vs_plain(10, args.quick, cpu=not args.no_cpu)}))
+        return
     if args.tick_sweep or args.capture_tick is not None:
         print(json.dumps({"tick_sweep": tick_sweep(args.quick, args.capture_tick)}))
         return
@@ -908,7 +948,7 @@ def main():
     if rank == 0 and not args.no_batch:
         detail["batching"] = batched_vs_plain(10, args.quick, cpu=not args.no_cpu)
     if rank == 0 and not args.no_serve:
-        detail["serving"] = serving_sweep(args.quick)
+        detail["serving"] = serving_sweep(args.quick, budgets)
     if rank == 0 and not args.no_stress:
         detail["stress"] = stress(args.quick, hbm)
     if rank == 0 and not args.no_cloud:

@@ -413,7 +413,7 @@ int vsim_radix_sort_u32(const uint32_t* d_keys, uint32_t* d_order, uint32_t n, u
  * that owns the whole GPU through its own pool, a frame loop that may not
  * stall on cudaMalloc, a binding holding only raw device pointers. No
  * counterpart in the reference. It allocates and frees nothing: its scratch
- * is a fixed array of about 16 MiB inside this library, held on every GPU
+ * is a fixed array of about 17 MiB inside this library, held on every GPU
  * that loads the library until the process exits, and it sorts at most
  * 1048576 keys (more fails with VSIM_ERR_CAPACITY). The first call on each
  * device looks up the array's device address; make that first call before
@@ -503,9 +503,18 @@ double vsim_server_clock(const vsim_server* server);
    The session must be resident (else VSIM_ERR_RANGE). */
 int vsim_server_submit(vsim_server* server, uint32_t session, uint32_t frames, const vsim_drag* drag,
                        uint64_t* request);
-/* Run one frame for every session with a pending request and wait for it;
-   *stepped receives how many sessions it advanced (0: nothing to do). */
+/* Run one frame for every session with a pending request (within the tick
+   budget, vsim_server_set_tick_budget) and wait for it; *stepped receives
+   how many sessions it advanced (0: nothing to do). */
 int vsim_server_tick(vsim_server* server, uint32_t* stepped);
+/* Caps the occupied cells one tick steps (0, the default: every session with
+   a pending request runs). Under a cap a tick first takes the sessions whose
+   requests have already started, oldest first, then waiting requests in
+   arrival order, each while its cells still fit; the first always runs. The
+   rest wait for the next tick: admission by slots as they free up, which
+   bounds a tick's length -- and so the frame latency under load -- at some
+   cost in throughput. No reference counterpart. */
+int vsim_server_set_tick_budget(vsim_server* server, uint64_t cells);
 /* Requests completed since the last poll (at most `capacity`). */
 int vsim_server_poll(vsim_server* server, vsim_completion* out, uint32_t capacity, uint32_t* count);
 int vsim_server_get_stats(const vsim_server* server, vsim_server_stats* out);

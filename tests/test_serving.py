@@ -126,6 +126,57 @@ def test_requests_join_at_frame_boundaries(lib):
     assert server.stats()["session_frames"] == 6
 
 
+def test_tick_budget_admits_started_then_oldest(lib):
+    """Under a tick budget a tick runs the sessions whose requests already
+    started (oldest first), then waiting requests in arrival order, while
+    their cells fit; the first always runs. Results do not depend on the
+    budget: each session ends where an unbudgeted server leaves it."""
+    import vsim.scenes as sc
+    from vsim.server import Server
+
+    bodies, tank = small_pool(6, seed=23)
+    cells = [b.cell_count for b in bodies]
+    rng = np.random.default_rng(5)
+    requests = [(0, 3, sc.drag_request(bodies[0], rng)), (1, 1, None), (2, 2, None), (3, 1, None)]
+    server = Server(bodies, tank)
+    server.set_tick_budget(cells[0])  # session 0 alone fills a tick
+    for session, frames, drag in requests:
+        server.submit(session, frames, drag)
+    stepped = []
+    while server.stats()["pending"]:
+        stepped.append(server.tick())
+        server.poll()
+    assert server.stats()["session_frames"] == 7
+    assert len(stepped) > 3  # the free server needs three ticks
+    free, _ = serve(bodies, tank, requests)
+    for s in range(4):
+        assert np.array_equal(server.read_positions(s), free.read_positions(s)), f"session {s}"
+
+
+def test_tick_budget_order(lib):
+    """Started requests keep their place; a later arrival waits while the
+    budget is spent."""
+    from vsim.server import Server
+
+    bodies, tank = small_pool(4, seed=29)
+    cells = [b.cell_count for b in bodies]
+    server = Server(bodies, tank)
+    server.set_tick_budget(max(cells[0], cells[1]))  # one of session 0 or 1 per tick
+    a = server.submit(0, 2)
+    b = server.submit(1, 1)
+    assert server.tick() == 1  # session 0 (earliest)
+    assert server.tick() == 1  # session 0 again: started requests go first
+    done = {c["request"]: c for c in server.poll()}
+    assert a in done and done[a]["first_tick"] == 0 and done[a]["last_tick"] == 1
+    assert server.tick() == 1  # now session 1
+    done = {c["request"]: c for c in server.poll()}
+    assert b in done and done[b]["first_tick"] == 2
+    server.set_tick_budget(0)
+    server.submit(2, 1)
+    server.submit(3, 1)
+    assert server.tick() == 2  # no cap: both together
+
+
 def test_served_session_matches_oracle(lib):
     import pyoracle
     import vsim.scenes as sc

@@ -92,6 +92,7 @@ struct vsim_server {
     uint64_t ticks = 0, nextId = 1, sessionFrames = 0, cellUpdates = 0;
     uint32_t pending = 0;
     double tickSeconds = 0, prepareSeconds = 0, frameSeconds = 0;
+    uint64_t tickCellBudget = 0;  // cells one tick may step; 0: every session with a pending request
     std::chrono::steady_clock::time_point origin = std::chrono::steady_clock::now();
     cudaEvent_t frameStart = nullptr, frameDone = nullptr;
 };
@@ -402,18 +403,53 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
     const double entered = seconds(s);
     const uint32_t bodies = uint32_t(s->resident.size());
 
-    // The sessions this frame runs, and the nodes their drags hold.
+    // The sessions this frame runs: every one with a pending request, or,
+    // under a tick budget, those whose requests already run (oldest first)
+    // and then waiting ones in arrival order while their cells fit.
+    std::vector<uint8_t> runs(bodies, 0);
+    {
+        std::vector<uint32_t> started, waiting;
+        for (uint32_t b = 0; b < bodies; b++) {
+            const auto& q = s->queue[s->resident[b]];
+            if (q.empty()) continue;
+            (q.front().done > 0 ? started : waiting).push_back(b);
+        }
+        if (s->tickCellBudget == 0) {
+            for (uint32_t b : started) runs[b] = 1;
+            for (uint32_t b : waiting) runs[b] = 1;
+        } else {
+            auto front = [&](uint32_t b) -> const Request& { return s->queue[s->resident[b]].front(); };
+            std::sort(started.begin(), started.end(), [&](uint32_t x, uint32_t y) {
+                return front(x).firstTick != front(y).firstTick ? front(x).firstTick < front(y).firstTick
+                                                                : front(x).id < front(y).id;
+            });
+            std::sort(waiting.begin(), waiting.end(), [&](uint32_t x, uint32_t y) { return front(x).id < front(y).id; });
+            uint64_t cells = 0;
+            bool any = false;
+            for (const std::vector<uint32_t>* list : {&started, &waiting})
+                for (uint32_t b : *list) {
+                    const uint64_t c = s->sessions[s->resident[b]].cells;
+                    if (any && cells + c > s->tickCellBudget) continue;
+                    runs[b] = 1;
+                    cells += c;
+                    any = true;
+                }
+        }
+    }
+    // The nodes their drags hold (a session left out keeps what it holds).
     bool holdChanged = false;
     uint32_t active = 0;
     for (uint32_t b = 0; b < bodies; b++) {
         const uint32_t i = s->resident[b];
-        const bool busy = !s->queue[i].empty();
-        const int64_t want = busy && s->queue[i].front().drag ? int64_t(s->queue[i].front().path.node) : int64_t(-1);
+        const bool busy = runs[b] != 0;
+        const int64_t want = !busy                          ? s->held[i]
+                             : s->queue[i].front().drag ? int64_t(s->queue[i].front().path.node)
+                                                        : int64_t(-1);
         if (want != s->held[i]) {
             holdChanged = true;
             s->held[i] = want;
         }
-        if (want >= 0 && s->queue[i].front().done == 0) {
+        if (busy && want >= 0 && s->queue[i].front().done == 0) {
             // A request's drag starts on its curve (the grab's placement),
             // whatever the session held before.
             double p[3], dp[3];
@@ -436,7 +472,7 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
     // velocity is this frame's motion over its duration (simulator.js:309-315).
     for (uint32_t b = 0; b < bodies; b++) {
         const uint32_t i = s->resident[b];
-        if (s->held[i] < 0) continue;
+        if (!runs[b] || s->held[i] < 0) continue;
         Request& r = s->queue[i].front();
         double p[3], dp[3];
         bezier(r.path.control, r.t, p, dp);
@@ -487,6 +523,13 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
     s->ticks++;
     s->tickSeconds += seconds(s) - entered;
     if (stepped) *stepped = active;
+    return VSIM_OK;
+}
+
+int vsim_server_set_tick_budget(vsim_server* s, uint64_t cells) {
+    clearError();
+    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
+    s->tickCellBudget = cells;
     return VSIM_OK;
 }
 

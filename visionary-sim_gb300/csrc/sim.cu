@@ -1311,7 +1311,7 @@ int vsim_profile_frame(vsim_sim* s, uint32_t steps, int with_splats, const float
         prof.begin(VSIM_KIND_SPLAT, 1);
         CK(launchSplatDeform(s->stream, s->sp, s->d.pos, s->splatCount, v[0], v[1], v[2]), "profile splats");
         prof.end();
-        prof.begin(VSIM_KIND_SORT, 20);
+        prof.begin(VSIM_KIND_SORT, radixSortLaunches(s->splatCount, 32));
         CK(radixSortU32(s->sp.keys, s->sp.order, s->splatCount, 32, s->sp.sortTemp, s->sp.sortTempBytes, s->stream),
            "profile sort");
         prof.end();

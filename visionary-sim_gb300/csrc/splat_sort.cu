@@ -1,5 +1,6 @@
 // Gaussian-splat deformation (sample.wgsl:40-80 with covariance.wgsl:18-42)
 // and the stable LSD radix sort behind the depth order.
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -165,54 +166,102 @@ cudaError_t launchSplatDeform(cudaStream_t st, const SplatState& s, const float4
 
 // --------------------------------------------------------- radix sort --
 //
-// Least-significant-digit radix sort, 8-bit digits, reduce-then-scan per
-// pass (no waits between blocks): a per-tile digit histogram, one
-// device-wide exclusive scan of the (digit, tile) counts, then a scatter in
-// which every warp ranks its 512 consecutive keys with __match_any_sync,
-// the block stages the tile in shared memory in digit order, and the tile
-// is written out in runs that are contiguous per digit. Tiles and ranks
-// follow input order, so each pass -- and the sort -- is stable.
+// Least-significant-digit radix sort, 8-bit digits, one sweep of the keys
+// per pass -- the single-pass scan with decoupled look-back (Merrill and
+// Garland, 2016) applied to radix sorting as Adinets and Merrill's
+// "Onesweep" (2022) does:
+//
+// - one launch counts every pass's digits over all the keys at once (a
+//   pass's digit totals do not depend on the order earlier passes leave);
+// - then one launch per pass. Each block takes the next tile from a ticket,
+//   so tiles start in order; it ranks its 4096 keys per digit (every warp
+//   its 512 with __match_any_sync) and publishes the tile's count of each
+//   digit in a status word (count and a flag packed in 32 bits, so one store
+//   carries both). Then each digit's thread walks back over the tiles before
+//   it, adding their counts until it meets a word that already holds an
+//   inclusive prefix, and publishes the tile's own. A tile waits only on
+//   tiles that started before it, which publish their counts without
+//   waiting on anything, so every walk ends. With the digit's global start
+//   (the histogram, scanned) the block writes the tile out in runs that are
+//   contiguous per digit.
+//
+// Tiles and ranks follow input order, so each pass -- and the sort -- is
+// stable. The status words, digit totals and tickets are cleared by one
+// memset at the start of a sort; every other scratch word is written before
+// it is read.
 
 constexpr uint32_t kSortThreads = 256;
 constexpr uint32_t kSortItems = 16;
 constexpr uint32_t kSortTile = kSortThreads * kSortItems;  // 4096 keys
 constexpr uint32_t kWarps = kSortThreads / 32;
-constexpr uint32_t kScanChunk = 4096;  // elements per block of the scan
-constexpr uint32_t kScanMaxChunks = 4096;
-constexpr uint32_t kFoldChunks = 64;  // chunks a down-sweep block sums itself
+constexpr uint32_t kSortMaxPasses = 4;
+constexpr uint32_t kStatusCount = 1u << 30;     // the word holds the tile's own count
+constexpr uint32_t kStatusPrefix = 2u << 30;    // the word holds the inclusive prefix
+constexpr uint32_t kStatusValue = (1u << 30) - 1u;
+constexpr uint32_t kLookbackSpinLimit = 1u << 22;
 
 namespace {
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr uint32_t tilesOf(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
-constexpr size_t sortTempBytes(uint32_t n) {
-    return 4 * align256(size_t(n) * 4) + align256(256 * size_t(tilesOf(n)) * 4) + align256(kScanMaxChunks * 4);
+// Cleared at the start of a sort: per pass, a status word per (tile, digit);
+// the digit totals of every pass; a ticket per pass and the failure word.
+constexpr size_t sortStatusBytes(uint32_t n) { return align256(size_t(kSortMaxPasses) * tilesOf(n) * 256 * 4); }
+constexpr size_t sortClearedBytes(uint32_t n) {
+    return sortStatusBytes(n) + align256(kSortMaxPasses * 256 * 4) + 256;
 }
+constexpr size_t sortTempBytes(uint32_t n) { return 4 * align256(size_t(n) * 4) + sortClearedBytes(n); }
 }  // namespace
 
 size_t radixSortTempBytes(uint32_t n) { return sortTempBytes(n); }
 
 uint32_t radixSortLaunches(uint32_t n, uint32_t keyBits) {
     if (n == 0) return 0;
-    const uint32_t chunks = (256 * tilesOf(n) + kScanChunk - 1) / kScanChunk;
-    return (keyBits + 7) / 8 * (chunks <= kFoldChunks ? 4u : 5u);  // the scan's middle level folded in
+    return 1 + (keyBits + 7) / 8;  // the digit counts, then one launch per pass
 }
 
-__global__ void __launch_bounds__(kSortThreads) sortHistKernel(const uint32_t* __restrict__ keys, uint32_t n,
-                                                               uint32_t shift, uint32_t mask, uint32_t tiles,
-                                                               uint32_t* __restrict__ hist) {
-    pdlWait();  // the keys and counts come from the kernel before
+__device__ __forceinline__ uint32_t loadRelaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void storeRelaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Every pass's digit counts over all keys: per block in shared memory, then
+// added into totals[pass * 256 + digit].
+__global__ void __launch_bounds__(kSortThreads) sortDigitCountKernel(const uint32_t* __restrict__ keys, uint32_t n,
+                                                                     uint32_t keyBits,
+                                                                     uint32_t* __restrict__ totals) {
+    __shared__ uint32_t bins[kSortMaxPasses * 256];
+    for (uint32_t i = threadIdx.x; i < kSortMaxPasses * 256; i += kSortThreads) bins[i] = 0;
+    pdlWait();  // the keys come from the kernel before
     pdlLaunchNext();
-    __shared__ uint32_t bins[256];
-    bins[threadIdx.x] = 0;
     __syncthreads();
-    const uint32_t base = blockIdx.x * kSortTile;
+    const uint32_t passes = (keyBits + 7) / 8;
+    auto count = [&](uint32_t k) {
 #pragma unroll
-    for (uint32_t r = 0; r < kSortItems; r++) {
-        const uint32_t idx = base + r * kSortThreads + threadIdx.x;
-        if (idx < n) atomicAdd(&bins[(keys[idx] >> shift) & mask], 1u);
+        for (uint32_t p = 0; p < kSortMaxPasses; p++) {
+            if (p >= passes) break;
+            const uint32_t bits = keyBits - 8 * p < 8 ? keyBits - 8 * p : 8;
+            atomicAdd(&bins[p * 256 + ((k >> (8 * p)) & ((1u << bits) - 1u))], 1u);
+        }
+    };
+    const uint32_t stride = gridDim.x * kSortThreads;
+    // four keys per load where the keys start on a 16-byte boundary
+    const uint32_t quads = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0 ? n / 4 : 0;
+    const uint4* k4 = reinterpret_cast<const uint4*>(keys);
+    for (uint32_t i = blockIdx.x * kSortThreads + threadIdx.x; i < quads; i += stride) {
+        const uint4 q = k4[i];
+        count(q.x);
+        count(q.y);
+        count(q.z);
+        count(q.w);
     }
+    for (uint32_t i = 4 * quads + blockIdx.x * kSortThreads + threadIdx.x; i < n; i += stride) count(keys[i]);
     __syncthreads();
-    hist[threadIdx.x * tiles + blockIdx.x] = bins[threadIdx.x];
+    for (uint32_t i = threadIdx.x; i < passes * 256; i += kSortThreads)
+        if (bins[i]) atomicAdd(&totals[i], bins[i]);
 }
 
 // Block-wide exclusive scan of one value per thread (256 threads); returns
@@ -245,119 +294,35 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
     return out;
 }
 
-// Scan, level 1: each block sums its chunk.
-__global__ void __launch_bounds__(kSortThreads) scanReduceKernel(const uint32_t* __restrict__ in, uint32_t n,
-                                                                 uint32_t* __restrict__ partial) {
-    pdlWait();  // the keys and counts come from the kernel before
-    pdlLaunchNext();
-    __shared__ uint32_t warpSums[kWarps + 1];
-    const uint32_t base = blockIdx.x * kScanChunk;
-    uint32_t sum = 0;
-    for (uint32_t r = 0; r < kScanChunk / kSortThreads; r++) {
-        const uint32_t idx = base + r * kSortThreads + threadIdx.x;
-        if (idx < n) sum += in[idx];
-    }
-    uint32_t total;
-    blockExclusiveScan(sum, warpSums, total);
-    if (threadIdx.x == 0) partial[blockIdx.x] = total;
-}
-
-// Scan, level 2: one block scans the chunk sums (at most kScanMaxChunks).
-__global__ void __launch_bounds__(kSortThreads) scanPartialKernel(uint32_t* __restrict__ partial, uint32_t chunks) {
-    pdlWait();  // the keys and counts come from the kernel before
-    pdlLaunchNext();
-    __shared__ uint32_t warpSums[kWarps + 1];
-    constexpr uint32_t per = kScanMaxChunks / kSortThreads;
-    uint32_t v[per];
-    uint32_t sum = 0;
-#pragma unroll
-    for (uint32_t i = 0; i < per; i++) {
-        const uint32_t idx = threadIdx.x * per + i;
-        v[i] = idx < chunks ? partial[idx] : 0;
-        sum += v[i];
-    }
-    uint32_t total;
-    uint32_t run = blockExclusiveScan(sum, warpSums, total);
-#pragma unroll
-    for (uint32_t i = 0; i < per; i++) {
-        const uint32_t idx = threadIdx.x * per + i;
-        if (idx < chunks) partial[idx] = run;
-        run += v[i];
-    }
-}
-
-// Scan, level 3: each block scans its chunk from its offset, in place.
-__global__ void __launch_bounds__(kSortThreads) scanDownKernel(uint32_t* __restrict__ data, uint32_t n,
-                                                               const uint32_t* __restrict__ partial) {
-    pdlWait();  // the keys and counts come from the kernel before
-    pdlLaunchNext();
-    __shared__ uint32_t warpSums[kWarps + 1];
-    constexpr uint32_t per = kScanChunk / kSortThreads;
-    const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * per;
-    uint32_t v[per];
-    uint32_t sum = 0;
-#pragma unroll
-    for (uint32_t i = 0; i < per; i++) {
-        v[i] = base + i < n ? data[base + i] : 0;
-        sum += v[i];
-    }
-    uint32_t total;
-    uint32_t run = blockExclusiveScan(sum, warpSums, total) + partial[blockIdx.x];
-#pragma unroll
-    for (uint32_t i = 0; i < per; i++) {
-        if (base + i < n) data[base + i] = run;
-        run += v[i];
-    }
-}
-
-// Scan, levels 2 and 3 in one launch when the chunks are few (at most
-// kFoldChunks): each block sums the chunk totals before its own (one per
-// thread at most) instead of reading them scanned by scanPartialKernel.
-
-__global__ void __launch_bounds__(kSortThreads) scanDownFoldKernel(uint32_t* __restrict__ data, uint32_t n,
-                                                                   const uint32_t* __restrict__ partial) {
-    pdlWait();  // the counts and chunk totals come from the kernels before
-    pdlLaunchNext();
-    __shared__ uint32_t warpSums[kWarps + 1];
-    uint32_t before;
-    blockExclusiveScan(threadIdx.x < blockIdx.x ? partial[threadIdx.x] : 0u, warpSums, before);
-    constexpr uint32_t per = kScanChunk / kSortThreads;
-    const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * per;
-    uint32_t v[per];
-    uint32_t sum = 0;
-#pragma unroll
-    for (uint32_t i = 0; i < per; i++) {
-        v[i] = base + i < n ? data[base + i] : 0;
-        sum += v[i];
-    }
-    uint32_t total;
-    uint32_t run = blockExclusiveScan(sum, warpSums, total) + before;
-#pragma unroll
-    for (uint32_t i = 0; i < per; i++) {
-        if (base + i < n) data[base + i] = run;
-        run += v[i];
-    }
-}
-
-__global__ void __launch_bounds__(kSortThreads) sortScatterKernel(const uint32_t* __restrict__ keysIn,
-                                                                  const uint32_t* __restrict__ valsIn, uint32_t n,
-                                                                  uint32_t shift, uint32_t mask, uint32_t tiles,
-                                                                  const uint32_t* __restrict__ offsets,
-                                                                  uint32_t* __restrict__ keysOut,
-                                                                  uint32_t* __restrict__ valsOut) {
-    pdlWait();  // the keys and counts come from the kernel before
-    pdlLaunchNext();
+// One pass: rank a tile, find its digits' global offsets by decoupled
+// look-back, scatter. `status` is this pass's (tile, digit) words, `totals`
+// its 256 digit counts over all keys.
+__global__ void __launch_bounds__(kSortThreads) sortPassKernel(const uint32_t* __restrict__ keysIn,
+                                                               const uint32_t* __restrict__ valsIn, uint32_t n,
+                                                               uint32_t shift, uint32_t mask,
+                                                               const uint32_t* __restrict__ totals,
+                                                               uint32_t* __restrict__ status,
+                                                               uint32_t* __restrict__ ticket,
+                                                               uint32_t* __restrict__ error,
+                                                               uint32_t* __restrict__ keysOut,
+                                                               uint32_t* __restrict__ valsOut) {
     __shared__ uint32_t sKeys[kSortTile];
     __shared__ uint32_t sVals[kSortTile];
     __shared__ uint32_t warpHist[kWarps][256];
     __shared__ uint32_t digitStart[256];
     __shared__ uint32_t globalStart[256];
     __shared__ uint32_t warpSums[kWarps + 1];
+    __shared__ uint32_t sTile;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // The ticket counter was cleared before the sort's first launch, which
+    // this one follows in stream order: safe to take before the wait.
+    if (threadIdx.x == 0) sTile = atomicAdd(ticket, 1u);
     for (uint32_t i = threadIdx.x; i < kWarps * 256; i += kSortThreads) (&warpHist[0][0])[i] = 0;
+    pdlWait();  // the keys and totals come from the kernels before
+    pdlLaunchNext();
     __syncthreads();
-
-    const uint32_t tileBase = blockIdx.x * kSortTile;
+    const uint32_t tile = sTile;
+    const uint32_t tileBase = tile * kSortTile;
     const uint32_t warpBase = tileBase + warp * 32 * kSortItems;
     const uint32_t lt = (1u << lane) - 1u;
     uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
@@ -376,19 +341,42 @@ __global__ void __launch_bounds__(kSortThreads) sortScatterKernel(const uint32_t
         rank[r] = before + __popc(peers & lt);
     }
     __syncthreads();
-    // Per digit: exclusive prefix over warps, then over digits.
     {
         const uint32_t d = threadIdx.x;
-        uint32_t running = 0;
+        // Per digit: exclusive prefix over warps, and the tile's count.
+        uint32_t count = 0;
 #pragma unroll
         for (uint32_t w = 0; w < kWarps; w++) {
             const uint32_t c = warpHist[w][d];
-            warpHist[w][d] = running;
-            running += c;
+            warpHist[w][d] = count;
+            count += c;
+        }
+        uint32_t* mine = status + size_t(tile) * 256 + d;
+        storeRelaxed(mine, (tile == 0 ? kStatusPrefix : kStatusCount) | count);
+        // Decoupled look-back over the tiles before this one.
+        uint32_t before = 0;
+        if (tile > 0) {
+            uint32_t j = tile - 1, polls = 0;
+            while (true) {
+                const uint32_t word = loadRelaxed(status + size_t(j) * 256 + d);
+                if ((word & ~kStatusValue) == 0) {  // tile j has not published yet
+                    if (++polls > kLookbackSpinLimit) {
+                        atomicOr(error, 1u);
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                before += word & kStatusValue;
+                if ((word & ~kStatusValue) == kStatusPrefix || j == 0) break;
+                j--;
+            }
+            storeRelaxed(mine, kStatusPrefix | (before + count));
         }
         uint32_t total;
-        digitStart[d] = blockExclusiveScan(running, warpSums, total);
-        globalStart[d] = offsets[d * tiles + blockIdx.x];
+        digitStart[d] = blockExclusiveScan(count, warpSums, total);
+        const uint32_t digitBase = blockExclusiveScan(totals[d], warpSums, total);
+        globalStart[d] = digitBase + before;
     }
     __syncthreads();
 #pragma unroll
@@ -416,7 +404,7 @@ namespace {
 // A sort kernel launched with programmatic dependent launch: its blocks may
 // start while the kernel before finishes, and wait (pdlWait) before reading.
 template <class... KArgs, class... Args>
-void pdl(void (*kernel)(KArgs...), uint32_t grid, cudaStream_t st, Args... args) {
+cudaError_t pdl(void (*kernel)(KArgs...), uint32_t grid, cudaStream_t st, Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(kSortThreads);
@@ -426,27 +414,35 @@ void pdl(void (*kernel)(KArgs...), uint32_t grid, cudaStream_t st, Args... args)
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 }  // namespace
 
 cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint32_t keyBits, void* temp,
                          size_t tempBytes, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    if (tempBytes < radixSortTempBytes(n)) return cudaErrorInvalidValue;
+    if (tempBytes < radixSortTempBytes(n) || n > kStatusValue || keyBits < 1 || keyBits > 32)
+        return cudaErrorInvalidValue;
     const uint32_t tiles = tilesOf(n);
-    const uint32_t histCount = 256 * tiles;
-    const uint32_t chunks = (histCount + kScanChunk - 1) / kScanChunk;
-    if (chunks > kScanMaxChunks) return cudaErrorInvalidValue;
     char* p = static_cast<char*>(temp);
     const size_t vec = align256(size_t(n) * 4);
     uint32_t* keysA = reinterpret_cast<uint32_t*>(p);
     uint32_t* keysB = reinterpret_cast<uint32_t*>(p + vec);
     uint32_t* valsA = reinterpret_cast<uint32_t*>(p + 2 * vec);
     uint32_t* valsB = reinterpret_cast<uint32_t*>(p + 3 * vec);
-    uint32_t* hist = reinterpret_cast<uint32_t*>(p + 4 * vec);
-    uint32_t* partial = reinterpret_cast<uint32_t*>(p + 4 * vec + align256(size_t(histCount) * 4));
+    char* cleared = p + 4 * vec;
+    uint32_t* status = reinterpret_cast<uint32_t*>(cleared);
+    uint32_t* totals = reinterpret_cast<uint32_t*>(cleared + sortStatusBytes(n));
+    uint32_t* tickets = reinterpret_cast<uint32_t*>(cleared + sortStatusBytes(n) + align256(kSortMaxPasses * 256 * 4));
+    uint32_t* error = tickets + kSortMaxPasses;
     const uint32_t passes = (keyBits + 7) / 8;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(cleared, 0, sortClearedBytes(n), st))) return e;
+    int device = 0, sms = 0;
+    if ((e = cudaGetDevice(&device)) || (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)))
+        return e;
+    const uint32_t countGrid = std::min<uint32_t>(tiles, 2u * uint32_t(sms));
+    if ((e = pdl(sortDigitCountKernel, countGrid, st, keys, n, keyBits, totals))) return e;
     const uint32_t* kin = keys;
     const uint32_t* vin = nullptr;
     for (uint32_t pass = 0; pass < passes; pass++) {
@@ -456,19 +452,13 @@ cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint
         const bool last = pass + 1 == passes;
         uint32_t* kout = last ? nullptr : (pass % 2 == 0 ? keysA : keysB);
         uint32_t* vout = last ? order : (pass % 2 == 0 ? valsA : valsB);
-        pdl(sortHistKernel, tiles, st, kin, n, shift, mask, tiles, hist);
-        pdl(scanReduceKernel, chunks, st, (const uint32_t*)hist, histCount, partial);
-        if (chunks <= kFoldChunks) {
-            pdl(scanDownFoldKernel, chunks, st, hist, histCount, (const uint32_t*)partial);
-        } else {
-            pdl(scanPartialKernel, 1u, st, partial, chunks);
-            pdl(scanDownKernel, chunks, st, hist, histCount, (const uint32_t*)partial);
-        }
-        pdl(sortScatterKernel, tiles, st, kin, vin, n, shift, mask, tiles, (const uint32_t*)hist, kout, vout);
+        if ((e = pdl(sortPassKernel, tiles, st, kin, vin, n, shift, mask, (const uint32_t*)(totals + 256 * pass),
+                     status + size_t(pass) * tiles * 256, tickets + pass, error, kout, vout)))
+            return e;
         kin = kout;
         vin = vout;
     }
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 }  // namespace vsim
@@ -483,12 +473,14 @@ cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint
 // takes its scratch from a fixed array compiled into this library instead of
 // from the caller: it allocates nothing and frees nothing.
 //
-// The array holds the scratch of kNoAllocMaxKeys keys (about 16 MiB) and lives
+// The array holds the scratch of kNoAllocMaxKeys keys (about 17 MiB) and lives
 // on every GPU that loads the library until the process exits. Every call
 // shares it, so calls whose work overlaps on the GPU -- on two streams, or from
-// two threads -- race and corrupt each other's results; serialise them. Each
-// call writes every scratch word it reads before reading it, so nothing has
-// to be cleared between calls.
+// two threads -- race and corrupt each other's results; serialise them. The
+// array keeps the last call's contents: each call first clears (with a memset
+// on its stream) the words that must start at zero -- the look-back status
+// words, digit totals and tile tickets -- and writes every other word before
+// reading it.
 
 namespace vsim {
 namespace {

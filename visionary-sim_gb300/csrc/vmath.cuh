@@ -24,10 +24,12 @@ __device__ __forceinline__ V mk(float x, float y, float z) { return V{x, y, z}; 
 __device__ __forceinline__ V xyz(float4 a) { return V{a.x, a.y, a.z}; }
 
 // fma3 issues x and y as one packed FP32x2 fused multiply-add (sm_100 and
-// later), which rounds each lane to nearest exactly as fmaf does. Adds and
-// multiplies stay scalar: a packed multiply did not reproduce the scalar
-// products bit for bit, and packed adds made the colour pass keep its cell
-// in local memory.
+// later), which rounds each lane to nearest exactly as fmaf does. Adds,
+// subtractions and multiplies stay scalar: their packed forms round each
+// lane exactly as the scalar operations do (checked bit for bit on the GPU,
+// subnormal and signed-zero operands included), but using them made the
+// compiler keep the colour pass's cell in local memory (a 144-byte stack
+// frame in every colour-pass kernel).
 __device__ __forceinline__ float2 xyOf(V a) { return make_float2(a.x, a.y); }
 __device__ __forceinline__ V withXy(float2 xy, float z) { return V{xy.x, xy.y, z}; }
 __device__ __forceinline__ V operator+(V a, V b) { return V{a.x + b.x, a.y + b.y, a.z + b.z}; }

@@ -179,6 +179,7 @@ SIGNATURES = {
     "vsim_server_clock": (C.c_double, [_P]),
     "vsim_server_submit": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(Drag), C.POINTER(C.c_uint64)]),
     "vsim_server_tick": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
+    "vsim_server_set_tick_budget": (C.c_int, [_P, C.c_uint64]),
     "vsim_server_poll": (C.c_int, [_P, C.POINTER(Completion), C.c_uint32, C.POINTER(C.c_uint32)]),
     "vsim_server_get_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "vsim_server_node_count": (C.c_uint32, [_P, C.c_uint32]),

@@ -77,6 +77,11 @@ class Server:
                                        C.byref(rid)))
         return int(rid.value)
 
+    def set_tick_budget(self, cells: int):
+        """Cap the occupied cells one tick steps (0: no cap); see
+        vsim_server_set_tick_budget."""
+        check(lib().vsim_server_set_tick_budget(self._h, int(cells)))
+
     def tick(self) -> int:
         stepped = C.c_uint32()
         check(lib().vsim_server_tick(self._h, C.byref(stepped)))

@@ -689,10 +689,12 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
     For each tick budget (occupied cells one tick may step, 0 = no cap;
     vsim_server_set_tick_budget): saturation measured closed-loop (every
     session always has a request), then Poisson arrivals at 25/50/70/90 % of
-    that saturation, the 70 % point `repeats_at_70` times. Each of these
-    starts from the same settled state (every session checkpointed after the
-    settling frames and written back before the measurement). Frame latency
-    of a request = (completion - arrival) / k."""
+    that saturation, the 70 % point `repeats_at_70` times, each run by the
+    library's own request loop (vsim_server_run) against a pre-drawn
+    schedule, so no client code sits between ticks. Each of these starts from
+    the same settled state (every session checkpointed after the settling
+    frames and written back before the measurement). Frame latency of a
+    request = (completion - scheduled arrival) / k."""
     import vsim.scenes as sc
     from vsim.server import Server
 
@@ -703,17 +705,8 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
     server = Server(bodies, tank, budget_bytes=150e9)
     admitted = server.admitted
     rng = np.random.default_rng(7)
-    drags = {}
-
-    def request(session):
-        frames = int(rng.integers(1, 5))
-        drag = None
-        if rng.random() < 0.5:
-            if session not in drags:
-                drags[session] = sc.drag_request(bodies[session], rng)
-            node, control, speed = drags[session]
-            drag = (node, control, speed)
-        return frames, drag
+    # every session's drag: a random surface node along a seeded Bezier curve
+    drags = [sc.drag_request(bodies[s], rng) for s in range(admitted)]
 
     def drain():
         while server.stats()["pending"]:
@@ -736,61 +729,34 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
         for s in range(admitted):
             server.write_state(s, *checkpoint[s])
 
+    def specs(count):
+        return rng.integers(1, 5, count), rng.random(count) < 0.5
+
     def saturation():
         restore()
-        arrival = {}
-        for s in range(admitted):
-            f, d = request(s)
-            arrival[server.submit(s, f, d)] = server.clock()
-        start = server.clock()
-        frames_done, requests_done, ticks = 0, 0, 0
+        frames, flags = specs(200_000)
         c0 = server.stats()["cell_updates"]
-        while server.clock() - start < seconds_per_point:
-            server.tick()
-            ticks += 1
-            for c in server.poll():
-                requests_done += 1
-                frames_done += c["frames"]
-                f, d = request(c["session"])
-                arrival[server.submit(c["session"], f, d)] = server.clock()
-        elapsed = server.clock() - start
+        _, rep = server.run(None, None, frames, flags, drags, closed_loop_seconds=seconds_per_point)
         cells = server.stats()["cell_updates"] - c0
-        drain()
-        return {"requests_per_s": round(requests_done / elapsed, 1),
-                "session_frames_per_s": round(frames_done / elapsed, 1), "ticks": ticks,
-                "cell_updates_per_s": round(cells / elapsed)}
+        return {"requests_per_s": round(rep["requests"] / rep["seconds"], 1),
+                "session_frames_per_s": round(rep["frames"] / rep["seconds"], 1), "ticks": rep["ticks"],
+                "cell_updates_per_s_incl_drain": round(cells / rep["seconds"]),
+                "method": "closed loop in the library's request loop (vsim_server_run): every session always has "
+                          "a request"}
 
     def point(frac, sat_rate):
         restore()
         lam = frac * sat_rate
-        arrival = {}
-        lat, req_lat = [], []
-        t = server.clock()
-        next_arrival = t + rng.exponential(1 / lam)
-        end = t + seconds_per_point
-        stepped = []
+        gaps = rng.exponential(1 / lam, int(lam * seconds_per_point * 1.5) + 16)
+        arrivals = np.cumsum(gaps)
+        arrivals = arrivals[arrivals < seconds_per_point]
+        sessions = rng.integers(0, admitted, arrivals.size)
+        frames, flags = specs(arrivals.size)
         st_before = server.stats()
-        c_before = st_before["cell_updates"]
-        t_begin = t
-        while True:
-            now = server.clock()
-            while next_arrival <= now and next_arrival < end:
-                s = int(rng.integers(0, admitted))
-                f, d = request(s)
-                arrival[server.submit(s, f, d)] = next_arrival
-                next_arrival += rng.exponential(1 / lam)
-            if server.stats()["pending"]:
-                stepped.append(server.tick())
-            elif next_arrival >= end:
-                break
-            else:
-                time.sleep(max(0.0, min(next_arrival - server.clock(), 0.0001)))
-            for c in server.poll():
-                total = c["completed"] - arrival.pop(c["request"])
-                req_lat.append(total)
-                lat.append(total / c["frames"])
-        elapsed = server.clock() - t_begin
+        done, rep = server.run(arrivals, sessions, frames, flags, drags)
         st_after = server.stats()
+        lat = np.array([(c["completed"] - c["submitted"]) / c["frames"] for c in done])
+        req_lat = np.array([c["completed"] - c["submitted"] for c in done])
         ticks_run = max(1, st_after["ticks"] - st_before["ticks"])
         tick_ms = {k: round(1e3 * (st_after[f"{k}_seconds"] - st_before[f"{k}_seconds"]) / ticks_run, 3)
                    for k in ("tick", "prepare", "frame")}
@@ -800,9 +766,9 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
                 "request_latency_ms": {"p50": round(1e3 * float(np.percentile(req_lat, 50)), 3),
                                        "p99": round(1e3 * float(np.percentile(req_lat, 99)), 3)},
                 "requests": len(lat),
-                "sessions_per_tick": round(float(np.mean(stepped)), 1) if stepped else 0,
+                "sessions_per_tick": round((st_after["session_frames"] - st_before["session_frames"]) / ticks_run, 1),
                 "mean_tick_ms": tick_ms,
-                "cell_updates_per_s": round((server.stats()["cell_updates"] - c_before) / elapsed)}
+                "cell_updates_per_s": round((st_after["cell_updates"] - st_before["cell_updates"]) / rep["seconds"])}
 
     runs = {}
     for budget in budgets:

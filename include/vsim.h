@@ -328,7 +328,7 @@ int vsim_contact_surface(vsim_sim* sim, uint32_t* nodes, uint32_t* bodies, size_
 
 /* Kernel groups a frame is made of. */
 #define VSIM_KIND_PREDICT 0
-#define VSIM_KIND_DRIVE 1
+#define VSIM_KIND_DRIVE 1     /* unused: the drive runs inside the pass that predicts each substep */
 #define VSIM_KIND_ELASTIC 2   /* the colour passes */
 #define VSIM_KIND_LIMIT 3     /* limit-only stretch sweeps */
 #define VSIM_KIND_CONTACT 4   /* bin, segment, scatter, order, collide, settle */
@@ -515,6 +515,42 @@ int vsim_server_tick(vsim_server* server, uint32_t* stepped);
    bounds a tick's length -- and so the frame latency under load -- at some
    cost in throughput. No reference counterpart. */
 int vsim_server_set_tick_budget(vsim_server* server, uint64_t cells);
+/* One request of a run (vsim_server_run). */
+typedef struct vsim_scheduled_request {
+    double arrival;       /* seconds after the run starts (unused in a closed-loop run) */
+    uint32_t session;     /* (unused in a closed-loop run) */
+    uint32_t frames;
+    uint32_t drag;        /* nonzero: the request drags along drags[session] */
+    uint32_t pad;
+} vsim_scheduled_request;
+
+/* Open loop: the whole run. Closed loop: the measured span, from the start
+   to the first tick that ends after closed_loop_seconds (the drain after it
+   not counted). */
+typedef struct vsim_run_report {
+    uint64_t requests;    /* completed */
+    uint64_t frames;      /* session-frames run */
+    uint64_t ticks;
+    uint32_t returned;    /* completions written to `out` (all of the run's, up to capacity) */
+    uint32_t pad;
+    double seconds;       /* wall time */
+} vsim_run_report;
+
+/* The server's request loop, run in the library against its own clock (no
+   caller round trips between ticks). Open loop (closed_loop_seconds == 0):
+   each request is submitted when its arrival time comes -- its completion
+   records that scheduled time as `submitted` -- ticks run while anything is
+   pending, and the loop returns once every request has completed. Closed
+   loop (closed_loop_seconds > 0): every resident session starts with a
+   request and gets the list's next one (cycling; its session and arrival
+   unused) the moment its last completes, for that long; then the loop
+   drains. Completions go to `out` (up to `capacity`; NULL: counts only),
+   not to vsim_server_poll. Needs no request pending at the start. A drag
+   request drags drags[session] (indexed by session id: one per session
+   offered). No reference counterpart. */
+int vsim_server_run(vsim_server* server, const vsim_scheduled_request* requests, uint32_t n,
+                    const vsim_drag* drags, double closed_loop_seconds, vsim_completion* out,
+                    uint32_t capacity, vsim_run_report* report);
 /* Requests completed since the last poll (at most `capacity`). */
 int vsim_server_poll(vsim_server* server, vsim_completion* out, uint32_t capacity, uint32_t* count);
 int vsim_server_get_stats(const vsim_server* server, vsim_server_stats* out);

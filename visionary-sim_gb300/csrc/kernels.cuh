@@ -39,6 +39,7 @@ struct DeviceState {
     // drive
     uint32_t* driven = nullptr;
     float4* drivenOffset = nullptr;
+    int32_t* drivenOf = nullptr;  // per node: its row in driven[], -1 for none
 };
 
 struct LaunchCtx {
@@ -161,8 +162,12 @@ Span denseSpan(uint32_t count, uint32_t block);
 // so that every SM gets a share.
 Span elasticSpan(uint32_t count, uint32_t block, uint32_t sms);
 
-cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, const Span& nodes);
-cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drivenCount);
+// Prediction of the frame's first substep; with `drive` the driven nodes
+// then take the drive law (driveHard/driveCompliant.wgsl), the substep's
+// first constraint.
+cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, const Span& nodes, bool drive);
+// drivenOf[driven[i]] := i for the n driven records, or := -1 with `clear`.
+cudaError_t launchMarkDriven(cudaStream_t st, const uint32_t* driven, uint32_t n, int32_t* drivenOf, bool clear);
 cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, const Span& span,
                           bool limitOnly, const StretchLengths& lens);
 
@@ -178,9 +183,9 @@ inline bool streamsColourPass(uint32_t count, uint32_t sms) {
 
 // The substep's closing pass; with `contact` it first applies the contact
 // corrections and empties the grid, with `predictNext` it goes on into the
-// next substep's prediction.
+// next substep's prediction (and, with `drive`, its drive).
 cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span& nodes, bool contact,
-                           bool predictNext);
+                           bool predictNext, bool drive);
 // `records` covers the surface records of the stepped bodies; at most
 // `recordItems` of them are binned. `mapping` is a VSIM_GATHER_* value.
 // `marks`, when given, are six events recorded around the five kernels (before

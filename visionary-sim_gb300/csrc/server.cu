@@ -25,6 +25,7 @@
 #include <cstring>
 #include <deque>
 #include <new>
+#include <thread>
 
 #include "sim_internal.cuh"
 
@@ -366,9 +367,13 @@ int vsim_server_set_resident(vsim_server* s, const uint32_t* sessions, uint32_t 
 
 double vsim_server_clock(const vsim_server* s) { return s ? seconds(s) : 0.0; }
 
-int vsim_server_submit(vsim_server* s, uint32_t session, uint32_t frames, const vsim_drag* drag, uint64_t* request) {
-    clearError();
-    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
+}  // extern "C"
+
+namespace {
+
+// Queues a request stamped as submitted at `submitted` (server clock).
+int submitAt(vsim_server* s, uint32_t session, uint32_t frames, const vsim_drag* drag, double submitted,
+             uint64_t* request) {
     uint32_t body;
     if (int rc = residentBody(s, session, body)) return rc;
     if (frames < 1) return fail(VSIM_ERR_RANGE, "frames must be at least 1");
@@ -376,7 +381,7 @@ int vsim_server_submit(vsim_server* s, uint32_t session, uint32_t frames, const 
     r.id = s->nextId++;
     r.session = session;
     r.frames = frames;
-    r.submitted = seconds(s);
+    r.submitted = submitted;
     if (drag) {
         const vsim_sim* sim = s->sim;
         if (drag->node >= sim->lat[body].nodeCount) return fail(VSIM_ERR_RANGE, "drag node outside the session");
@@ -391,6 +396,16 @@ int vsim_server_submit(vsim_server* s, uint32_t session, uint32_t frames, const 
     s->pending++;
     if (request) *request = r.id;
     return VSIM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vsim_server_submit(vsim_server* s, uint32_t session, uint32_t frames, const vsim_drag* drag, uint64_t* request) {
+    clearError();
+    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
+    return submitAt(s, session, frames, drag, seconds(s), request);
 }
 
 int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
@@ -523,6 +538,79 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
     s->ticks++;
     s->tickSeconds += seconds(s) - entered;
     if (stepped) *stepped = active;
+    return VSIM_OK;
+}
+
+int vsim_server_run(vsim_server* s, const vsim_scheduled_request* requests, uint32_t n, const vsim_drag* drags,
+                    double closed_loop_seconds, vsim_completion* out, uint32_t capacity, vsim_run_report* report) {
+    clearError();
+    if (!s || (n > 0 && !requests)) return fail(VSIM_ERR_INVALID, "server or requests is NULL");
+    if (!(closed_loop_seconds >= 0) || !std::isfinite(closed_loop_seconds))
+        return fail(VSIM_ERR_RANGE, "closed_loop_seconds must be finite and not negative");
+    const bool closed = closed_loop_seconds > 0;
+    if (closed && n == 0) return fail(VSIM_ERR_INVALID, "a closed-loop run needs requests to draw from");
+    if (s->pending) return fail(VSIM_ERR_INVALID, "requests are already pending");
+    for (uint32_t i = 0; i < n; i++)
+        if (requests[i].drag && !drags) return fail(VSIM_ERR_INVALID, "a request drags but drags is NULL");
+    std::vector<vsim_completion> done;
+    const uint64_t frames0 = s->sessionFrames, ticks0 = s->ticks;
+    uint64_t requestsDone = 0;
+    uint32_t next = 0;
+    auto spec = [&](uint32_t session, const vsim_scheduled_request& q, double at) {
+        return submitAt(s, session, q.frames, q.drag ? &drags[session] : nullptr, at, nullptr);
+    };
+    const double t0 = seconds(s);
+    int rc = VSIM_OK;
+    bool windowClosed = false;
+    uint64_t windowRequests = 0, windowFrames = 0, windowTicks = 0;
+    double windowSeconds = 0;
+    if (closed) {
+        for (uint32_t session : s->resident) {
+            if ((rc = spec(session, requests[next], seconds(s)))) return rc;
+            next = (next + 1) % n;
+        }
+    }
+    while (true) {
+        const double now = seconds(s);
+        if (!closed)
+            while (next < n && t0 + requests[next].arrival <= now) {
+                if ((rc = spec(requests[next].session, requests[next], t0 + requests[next].arrival))) return rc;
+                next++;
+            }
+        if (s->pending) {
+            if ((rc = vsim_server_tick(s, nullptr))) return rc;
+            const bool refill = closed && seconds(s) - t0 < closed_loop_seconds;
+            if (closed && !refill && !windowClosed) {  // the closed loop's measured span ends here
+                windowClosed = true;
+                windowRequests = requestsDone + s->completed.size();
+                windowFrames = s->sessionFrames - frames0;
+                windowTicks = s->ticks - ticks0;
+                windowSeconds = seconds(s) - t0;
+            }
+            for (const vsim_completion& c : s->completed) {
+                requestsDone++;
+                if (out && done.size() < capacity) done.push_back(c);
+                if (refill) {
+                    if ((rc = spec(c.session, requests[next], seconds(s)))) return rc;
+                    next = (next + 1) % n;
+                }
+            }
+            s->completed.clear();
+            continue;
+        }
+        if (closed || next >= n) break;
+        // Idle until the next arrival: sleep while it is far, then spin.
+        const double wait = t0 + requests[next].arrival - seconds(s);
+        if (wait > 2e-4) std::this_thread::sleep_for(std::chrono::duration<double>(wait - 1e-4));
+    }
+    if (out) std::copy(done.begin(), done.end(), out);
+    if (report) {
+        report->requests = closed ? windowRequests : requestsDone;
+        report->returned = uint32_t(done.size());
+        report->frames = closed ? windowFrames : s->sessionFrames - frames0;
+        report->ticks = closed ? windowTicks : s->ticks - ticks0;
+        report->seconds = closed ? windowSeconds : seconds(s) - t0;
+    }
     return VSIM_OK;
 }
 

@@ -278,17 +278,14 @@ cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMod
     // The first substep's prediction runs on its own; every later one rides
     // on the closing pass of the substep before it.
     const FramePlan& plan = s->plan;
+    // The drive (the substep's first constraint) rides on the pass that
+    // predicts the substep.
     if (steps > 0) {
         begin(VSIM_KIND_PREDICT, 1);
-        if ((e = launchPredict(c, s->d, plan.nodes))) return e;
+        if ((e = launchPredict(c, s->d, plan.nodes, driving))) return e;
         end();
     }
     for (uint32_t step = 0; step < steps; step++) {
-        if (driving) {
-            begin(VSIM_KIND_DRIVE, 1);
-            if ((e = launchDrive(c, s->d, VSIM_MAX_DRIVEN))) return e;
-            end();
-        }
         for (uint32_t it = 0; it < s->iterations; it++)
             for (int col = 0; col < 8; col++) {
                 if (!plan.colour[col].grid) continue;
@@ -312,7 +309,8 @@ cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMod
             end();
         }
         begin(VSIM_KIND_FINALIZE, 1);
-        if ((e = launchFinalize(c, s->d, plan.nodes, contact && mode == ContactMode::Solve, step + 1 < steps)))
+        if ((e = launchFinalize(c, s->d, plan.nodes, contact && mode == ContactMode::Solve, step + 1 < steps,
+                                driving)))
             return e;
         end();
     }
@@ -393,7 +391,7 @@ void freeSim(vsim_sim* s) {
     DeviceState& d = s->d;
     void* ptrs[] = {d.pos, d.prev, d.vel, d.baseW, d.active, d.activeBody, d.cells, d.bodies, d.fp,
                     d.surf, d.key, d.rank, d.entries, d.count, d.start, d.cursor, d.delta, d.driven,
-                    d.drivenOffset, d.nodeRecord, d.sMeta, d.sPos, d.sMoved, d.sRec, d.sKey, d.bodyActive, d.grabs,
+                    d.drivenOffset, d.drivenOf, d.nodeRecord, d.sMeta, d.sPos, d.sMoved, d.sRec, d.sKey, d.bodyActive, d.grabs,
                     s->chunkDev, s->staging, s->pairs, s->pairCount, s->sp.embed, s->sp.quat,
                     s->sp.scaleBody, s->sp.bodies, s->sp.meanDepth, s->sp.cov, s->sp.keys, s->sp.order,
                     s->sp.sortTemp};
@@ -577,6 +575,7 @@ int createSim(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, v
     CK(allocN(&d.cursor, 1), "allocate contact cursor");
     CK(allocN(&d.driven, VSIM_MAX_DRIVEN), "allocate drive");
     CK(allocN(&d.drivenOffset, VSIM_MAX_DRIVEN), "allocate drive");
+    CK(allocN(&d.drivenOf, N), "allocate drive");
     CK(allocN(&s->pairCount, 4), "allocate pair counter");  // [0] pairs, [1..3] the contact census
     CK(cudaMallocHost(&s->activePinned, s->activeHost.size() * 4), "allocate staging");
     CK(cudaMallocHost(&s->grabsPinned, s->grabsHost.size() * 16), "allocate staging");
@@ -627,6 +626,7 @@ int createSim(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, v
     CK(cudaMemcpyAsync(d.pos, s->restPos.data(), N * 16, cudaMemcpyHostToDevice, s->stream), "upload state");
     CK(cudaMemcpyAsync(d.prev, s->restPos.data(), N * 16, cudaMemcpyHostToDevice, s->stream), "upload state");
     CK(cudaMemsetAsync(d.vel, 0, N * 16, s->stream), "upload state");
+    CK(cudaMemsetAsync(d.drivenOf, 0xff, N * 4, s->stream), "clear drive rows");  // -1: not driven
     CK(cudaMemcpyAsync(d.baseW, s->baseW.data(), N * 4, cudaMemcpyHostToDevice, s->stream), "upload masses");
     CK(cudaMemcpyAsync(d.active, active.data(), active.size() * 4, cudaMemcpyHostToDevice, s->stream), "upload");
     CK(cudaMemcpyAsync(d.activeBody, activeBody.data(), activeBody.size() * 4, cudaMemcpyHostToDevice, s->stream),
@@ -812,6 +812,7 @@ int holdNodes(vsim_sim* s, const uint32_t* nodes, const float* offsets, uint32_t
     const uint32_t kept = std::min<uint32_t>(count, VSIM_MAX_DRIVEN);
     int rc = restoreHeld(s);
     if (rc) return rc;
+    CK(launchMarkDriven(s->stream, s->d.driven, uint32_t(s->held.size()), s->d.drivenOf, true), "release hold");
     std::vector<float4> off(kept);
     s->heldBody.resize(kept);
     for (uint32_t i = 0; i < kept; i++) {
@@ -826,6 +827,7 @@ int holdNodes(vsim_sim* s, const uint32_t* nodes, const float* offsets, uint32_t
     // Copies from pageable memory return once the data is staged, so `off`
     // may go out of scope; everything after them is in stream order.
     s->held.assign(nodes, nodes + kept);
+    CK(launchMarkDriven(s->stream, s->d.driven, kept, s->d.drivenOf, false), "upload hold");
     rc = zeroHeld(s);
     if (rc) return rc;
     s->frameDirty = true;
@@ -835,6 +837,7 @@ int holdNodes(vsim_sim* s, const uint32_t* nodes, const float* offsets, uint32_t
 int releaseNodes(vsim_sim* s) {
     int rc = restoreHeld(s);
     if (rc) return rc;
+    CK(launchMarkDriven(s->stream, s->d.driven, uint32_t(s->held.size()), s->d.drivenOf, true), "release hold");
     s->held.clear();
     s->heldBody.clear();
     s->frameDirty = true;
@@ -1221,7 +1224,6 @@ uint32_t vsim_frame_launches(const vsim_sim* s, uint32_t steps) {
     uint32_t colours = 0;
     for (int c = 0; c < 8; c++) colours += s->colorStart[c + 1] > s->colorStart[c] ? 1 : 0;
     uint32_t per = 1 + colours * s->iterations;
-    if (!s->held.empty()) per += 1;
     if (anyStretch(s)) per += 3 * colours;
     if (s->contact && s->surfaceCount > 0) per += kContactKernels;
     return steps ? 1 + per * steps : 0;

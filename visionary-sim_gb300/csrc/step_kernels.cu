@@ -219,44 +219,20 @@ __device__ __forceinline__ void cornerNodes(uint4 e, uint32_t (&ids)[8]) {
 
 // ------------------------------------------------------------- kernels --
 
-// predict.wgsl:19-36 over the active nodes.
-__global__ void predictKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ active,
-                              const uint32_t* __restrict__ activeBody, const uint32_t* __restrict__ bodyActive,
-                              float4* __restrict__ pos, float4* __restrict__ prev, float4* __restrict__ vel) {
-    struct Pre {
-        uint32_t n, live;
-    };
-    auto pre = [&](uint32_t i) { return Pre{active[i], bodyActive[activeBody[i]]}; };
-    forEachItemAfterWait(work, pre, [&](uint32_t i, Pre q) {
-        if (!q.live) return;
-        const uint32_t n = q.n;
-        const float4 P = pos[n];
-        if (P.w == 0.0f) return;
-        const float dt = fp->dt;
-        const V g = mk(fp->gx, fp->gy, fp->gz);
-        const V v = xyz(vel[n]) + g * dt;
-        const V p = xyz(P);
-        prev[n] = withW(p, 0.0f);
-        pos[n] = withW(p + v * dt, P.w);
-        vel[n] = withW(v, 0.0f);
-    });
-}
-
-// driveHard.wgsl:15-35 and driveCompliant.wgsl:24-41.
-// Each driven record carries its body in offsets.w; the target is the scene's
-// single grab target, or with perBodyGrab the body's own row of `grabs`.
-__global__ void driveKernel(const FrameParams* __restrict__ fp, const uint32_t* __restrict__ driven,
-                            const float4* __restrict__ offsets, const uint32_t* __restrict__ bodyActive,
-                            const float4* __restrict__ grabs, float4* __restrict__ pos, float4* __restrict__ prev,
-                            float4* __restrict__ vel) {
-    pdlWait();
-    pdlLaunchNext();
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= fp->drivenCount) return;
-    const float4 off = offsets[i];
+// driveHard.wgsl:15-35 and driveCompliant.wgsl:24-41 for driven record d,
+// node n, whose state is P (its position just predicted, or as it stands
+// where the hard law holds it with w = 0). The record carries its body in
+// offsets.w; the target is the scene's single grab target, or with
+// perBodyGrab the body's own row of `grabs`. Runs inside the pass that
+// predicts the substep, for the node that pass has just handled: the state
+// it reads is the one the reference's drive pass, the next in its order,
+// would read.
+__device__ __forceinline__ void applyDrive(const FrameParams* __restrict__ fp, const float4* __restrict__ offsets,
+                                           const float4* __restrict__ grabs, int32_t d, uint32_t n, float4 P,
+                                           float4* __restrict__ pos, float4* __restrict__ prev,
+                                           float4* __restrict__ vel) {
+    const float4 off = offsets[d];
     const uint32_t body = __float_as_uint(off.w);
-    if (!bodyActive[body]) return;
-    const uint32_t n = driven[i];
     const float dt = fp->dt;
     V target = mk(fp->grabTarget[0], fp->grabTarget[1], fp->grabTarget[2]);
     V velocity = mk(fp->grabVelocity[0], fp->grabVelocity[1], fp->grabVelocity[2]);
@@ -265,7 +241,6 @@ __global__ void driveKernel(const FrameParams* __restrict__ fp, const uint32_t* 
         velocity = xyz(grabs[2 * body + 1]);
     }
     const V goal = target + xyz(off);
-    const float4 P = pos[n];
     if (fp->law == VSIM_DRIVE_HARD) {
         const V here = xyz(P);
         const V step = velocity * dt;
@@ -281,6 +256,53 @@ __global__ void driveKernel(const FrameParams* __restrict__ fp, const uint32_t* 
         const float frac = dt2 / (dt2 + tau2);
         pos[n] = withW(p + (goal - p) * frac, P.w);
     }
+}
+
+// The drive's tables, for the passes that predict (DRIVE variants only).
+struct DriveTables {
+    const int32_t* drivenOf;  // per node: its row in the driven records, -1 for none
+    const float4* offsets;    // per driven record: offset from the target, body as bits
+    const float4* grabs;      // per body: drive target, drive target velocity
+};
+
+// predict.wgsl:19-36 over the active nodes; with DRIVE, a driven node then
+// takes the drive law (the reference's next pass in the substep).
+template <bool DRIVE>
+__global__ void predictKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ active,
+                              const uint32_t* __restrict__ activeBody, const uint32_t* __restrict__ bodyActive,
+                              DriveTables drive, float4* __restrict__ pos, float4* __restrict__ prev,
+                              float4* __restrict__ vel) {
+    struct Pre {
+        uint32_t n, live;
+        int32_t driven;
+    };
+    auto pre = [&](uint32_t i) {
+        const uint32_t n = active[i];
+        return Pre{n, bodyActive[activeBody[i]], DRIVE ? drive.drivenOf[n] : -1};
+    };
+    forEachItemAfterWait(work, pre, [&](uint32_t i, Pre q) {
+        if (!q.live) return;
+        const uint32_t n = q.n;
+        float4 P = pos[n];
+        if (P.w != 0.0f) {
+            const float dt = fp->dt;
+            const V g = mk(fp->gx, fp->gy, fp->gz);
+            const V v = xyz(vel[n]) + g * dt;
+            const V p = xyz(P);
+            P = withW(p + v * dt, P.w);
+            prev[n] = withW(p, 0.0f);
+            pos[n] = P;
+            vel[n] = withW(v, 0.0f);
+        }
+        if (DRIVE && q.driven >= 0) applyDrive(fp, drive.offsets, drive.grabs, q.driven, n, P, pos, prev, vel);
+    });
+}
+
+// Marks (or, with row < 0, clears) the driven nodes' rows in drivenOf.
+__global__ void markDrivenKernel(const uint32_t* __restrict__ driven, uint32_t n, int32_t* __restrict__ drivenOf,
+                                 int clear) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) drivenOf[driven[i]] = clear ? -1 : int32_t(i);
 }
 
 // project.wgsl:35-184: one colour pass, one thread per occupied cell.
@@ -416,23 +438,26 @@ __device__ __forceinline__ V resolvePlane(V p, V prev, V normal, float depth, fl
 // bucket -- so no separate pass runs between contact and the closing pass.
 // With PREDICT it continues straight into the next substep's
 // predict.wgsl:19-36 from the position and velocity it has just computed,
-// which are the values that pass would read back.
-template <bool CONTACT, bool PREDICT>
+// which are the values that pass would read back; with DRIVE as well a
+// driven node then takes the drive law, that substep's first constraint.
+template <bool CONTACT, bool PREDICT, bool DRIVE>
 __global__ void finalizeKernel(const FrameParams* __restrict__ fp, Work work, const uint32_t* __restrict__ active,
                                const uint32_t* __restrict__ activeBody, const DevBody* __restrict__ bodies,
                                float4* __restrict__ pos, float4* __restrict__ prevState, float4* __restrict__ vel,
                                const int32_t* __restrict__ nodeRecord, const float4* __restrict__ delta,
                                const uint32_t* __restrict__ key, uint32_t* __restrict__ count,
-                               uint32_t* __restrict__ cursor, const uint32_t* __restrict__ bodyActive) {
+                               uint32_t* __restrict__ cursor, const uint32_t* __restrict__ bodyActive,
+                               DriveTables drive) {
     struct Pre {
         uint32_t n, live;
-        int32_t record;
+        int32_t record, driven;
         float friction, damp;
     };
     auto pre = [&](uint32_t i) {
         const uint32_t body = activeBody[i];
         const uint32_t n = active[i];
-        return Pre{n, bodyActive[body], CONTACT ? nodeRecord[n] : -1, bodies[body].friction, bodies[body].damp};
+        return Pre{n, bodyActive[body], CONTACT ? nodeRecord[n] : -1, DRIVE ? drive.drivenOf[n] : -1,
+                   bodies[body].friction, bodies[body].damp};
     };
     forEachItemAfterWait(work, pre, [&](uint32_t, const Pre& q) {
         if (!q.live) return;
@@ -450,7 +475,12 @@ __global__ void finalizeKernel(const FrameParams* __restrict__ fp, Work work, co
                 count[key[r]] = 0;
             }
         }
-        if (P.w == 0.0f) return;
+        if (P.w == 0.0f) {
+            // held by the hard law: the next substep's drive takes it from here
+            if (DRIVE && PREDICT && q.driven >= 0) applyDrive(fp, drive.offsets, drive.grabs, q.driven, n, P, pos,
+                                                               prevState, vel);
+            return;
+        }
         const V prev = xyz(prevState[n]);
         const float fr = q.friction;
         const V mn = mk(fp->tankMin[0], fp->tankMin[1], fp->tankMin[2]);
@@ -467,9 +497,12 @@ __global__ void finalizeKernel(const FrameParams* __restrict__ fp, Work work, co
         if (PREDICT) {
             const V g = mk(fp->gx, fp->gy, fp->gz);
             const V v2 = v + g * dt;
+            const float4 next = withW(p + v2 * dt, P.w);
             prevState[n] = withW(p, 0.0f);
-            pos[n] = withW(p + v2 * dt, P.w);
+            pos[n] = next;
             vel[n] = withW(v2, 0.0f);
+            if (DRIVE && q.driven >= 0) applyDrive(fp, drive.offsets, drive.grabs, q.driven, n, next, pos, prevState,
+                                                   vel);
         } else {
             pos[n] = withW(p, P.w);
             vel[n] = withW(v, 0.0f);
@@ -1042,14 +1075,24 @@ Span elasticSpan(uint32_t count, uint32_t block, uint32_t sms) {
     return denseSpan(count, block);
 }
 
-cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, const Span& n) {
-    return launch(c, predictKernel, n.grid, n.block, s.fp, n.work, s.active, s.activeBody,
-                  (const uint32_t*)s.bodyActive, s.pos, s.prev, s.vel);
+namespace {
+DriveTables driveTables(const DeviceState& s) {
+    return DriveTables{s.drivenOf, s.drivenOffset, s.grabs};
+}
+}  // namespace
+
+cudaError_t launchPredict(const LaunchCtx& c, const DeviceState& s, const Span& n, bool drive) {
+    auto go = [&](auto kernel) {
+        return launch(c, kernel, n.grid, n.block, s.fp, n.work, s.active, s.activeBody,
+                      (const uint32_t*)s.bodyActive, driveTables(s), s.pos, s.prev, s.vel);
+    };
+    return drive ? go(predictKernel<true>) : go(predictKernel<false>);
 }
 
-cudaError_t launchDrive(const LaunchCtx& c, const DeviceState& s, uint32_t drivenCount) {
-    return launch(c, driveKernel, blocks(drivenCount, 256), 256, s.fp, s.driven, s.drivenOffset,
-                  (const uint32_t*)s.bodyActive, (const float4*)s.grabs, s.pos, s.prev, s.vel);
+cudaError_t launchMarkDriven(cudaStream_t st, const uint32_t* driven, uint32_t n, int32_t* drivenOf, bool clear) {
+    if (n == 0) return cudaSuccess;
+    markDrivenKernel<<<blocks(n, 256), 256, 0, st>>>(driven, n, drivenOf, clear ? 1 : 0);
+    return cudaGetLastError();
 }
 
 cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, const Span& sp,
@@ -1066,14 +1109,17 @@ cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4*
                   (const uint32_t*)s.bodyActive, s.pos, (const float4*)s.prev, lens);
 }
 
-cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span& n, bool contact, bool predictNext) {
+cudaError_t launchFinalize(const LaunchCtx& c, const DeviceState& s, const Span& n, bool contact, bool predictNext,
+                           bool drive) {
     auto go = [&](auto kernel) {
         return launch(c, kernel, n.grid, n.block, s.fp, n.work, s.active, s.activeBody, s.bodies, s.pos, s.prev,
                       s.vel, (const int32_t*)s.nodeRecord, (const float4*)s.delta, (const uint32_t*)s.key, s.count,
-                      s.cursor, (const uint32_t*)s.bodyActive);
+                      s.cursor, (const uint32_t*)s.bodyActive, driveTables(s));
     };
-    if (contact) return predictNext ? go(finalizeKernel<true, true>) : go(finalizeKernel<true, false>);
-    return predictNext ? go(finalizeKernel<false, true>) : go(finalizeKernel<false, false>);
+    if (predictNext && drive)
+        return contact ? go(finalizeKernel<true, true, true>) : go(finalizeKernel<false, true, true>);
+    if (contact) return predictNext ? go(finalizeKernel<true, true, false>) : go(finalizeKernel<true, false, false>);
+    return predictNext ? go(finalizeKernel<false, true, false>) : go(finalizeKernel<false, false, false>);
 }
 
 // Solve mode leaves the corrections in `delta` for the closing pass, which

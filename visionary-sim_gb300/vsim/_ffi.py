@@ -148,6 +148,16 @@ VSIM_GRIP_SINGLE_NODE = 0
 VSIM_GRIP_WITHIN_RADIUS = 1
 
 
+class ScheduledRequest(C.Structure):
+    _fields_ = [("arrival", C.c_double), ("session", C.c_uint32), ("frames", C.c_uint32), ("drag", C.c_uint32),
+                ("pad", C.c_uint32)]
+
+
+class RunReport(C.Structure):
+    _fields_ = [("requests", C.c_uint64), ("frames", C.c_uint64), ("ticks", C.c_uint64), ("returned", C.c_uint32),
+                ("pad", C.c_uint32), ("seconds", C.c_double)]
+
+
 class ServerStats(C.Structure):
     _fields_ = [("sessions", C.c_uint32), ("rejected", C.c_uint32), ("resident_bytes", C.c_double),
                 ("ticks", C.c_uint64), ("session_frames", C.c_uint64), ("cell_updates", C.c_uint64),
@@ -180,6 +190,8 @@ SIGNATURES = {
     "vsim_server_submit": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(Drag), C.POINTER(C.c_uint64)]),
     "vsim_server_tick": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
     "vsim_server_set_tick_budget": (C.c_int, [_P, C.c_uint64]),
+    "vsim_server_run": (C.c_int, [_P, C.POINTER(ScheduledRequest), C.c_uint32, C.POINTER(Drag), C.c_double,
+                                  C.POINTER(Completion), C.c_uint32, C.POINTER(RunReport)]),
     "vsim_server_poll": (C.c_int, [_P, C.POINTER(Completion), C.c_uint32, C.POINTER(C.c_uint32)]),
     "vsim_server_get_stats": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "vsim_server_node_count": (C.c_uint32, [_P, C.c_uint32]),

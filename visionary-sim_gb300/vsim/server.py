@@ -82,6 +82,43 @@ class Server:
         vsim_server_set_tick_budget."""
         check(lib().vsim_server_set_tick_budget(self._h, int(cells)))
 
+    def run(self, arrivals, sessions, frames, drag_flags, drags=None, closed_loop_seconds: float = 0.0,
+            keep: int | None = None):
+        """The library's request loop (vsim_server_run) over a schedule:
+        arrival times (seconds from the start), sessions, frames, drag flags,
+        and per-session drags [(node, control 4x3, speed)] indexed by session
+        id (None: no drags). Returns (completions as dicts, report dict)."""
+        n = len(frames)
+        if keep is None:
+            keep = n if closed_loop_seconds == 0 else 0
+        reqs = (_ffi.ScheduledRequest * max(n, 1))()
+        for i in range(n):
+            reqs[i].arrival = float(arrivals[i]) if arrivals is not None else 0.0
+            reqs[i].session = int(sessions[i]) if sessions is not None else 0
+            reqs[i].frames = int(frames[i])
+            reqs[i].drag = int(bool(drag_flags[i]))
+        table = None
+        if drags is not None:
+            table = (_ffi.Drag * len(drags))()
+            for k, d in enumerate(drags):
+                if d is None:
+                    continue
+                node, control, speed = d
+                table[k].node = int(node)
+                ctl = np.asarray(control, np.float32).reshape(4, 3)
+                for i in range(4):
+                    for a in range(3):
+                        table[k].control[i][a] = float(ctl[i, a])
+                table[k].speed = float(speed)
+        out = (_ffi.Completion * keep)() if keep > 0 else None
+        report = _ffi.RunReport()
+        check(lib().vsim_server_run(self._h, reqs, n, table, float(closed_loop_seconds), out, keep,
+                                    C.byref(report)))
+        done = [{"request": out[i].request, "session": out[i].session, "frames": out[i].frames,
+                 "submitted": out[i].submitted, "completed": out[i].completed, "first_tick": out[i].first_tick,
+                 "last_tick": out[i].last_tick} for i in range(report.returned)]
+        return done, {name: getattr(report, name) for name, _ in report._fields_ if name != "pad"}
+
     def tick(self) -> int:
         stepped = C.c_uint32()
         check(lib().vsim_server_tick(self._h, C.byref(stepped)))

@@ -334,6 +334,37 @@ def test_material_change_midrun(lib):
         assert_same(sim, orc, scene, f"after change {frame}")
 
 
+def test_state_io_through_pinned_and_pageable_buffers(lib, gpu):
+    """Node state written from and read into page-locked host buffers
+    (asynchronous copies) equals the same through pageable numpy buffers
+    (copies the driver stages): a frame from a written state, then every
+    array read back both ways, bit for bit."""
+    import torch
+    import vsim.scenes as sc
+    from vsim._ffi import check, fptr
+
+    scene = sc.noise_blob(n=12, seed=7, splats=0)
+    a, b = make(scene)[0], make(scene)[0]
+    for _ in range(3):
+        a.dispatch(scene.substeps)
+    state = a.read_state()
+    n = a.node_count
+    pinned = [torch.empty((n, 4), dtype=torch.float32, pin_memory=True) for _ in range(6)]
+    for t, arr in zip(pinned[:3], state):
+        t.numpy()[:] = arr
+    L = lib.lib()
+    check(L.vsim_write_state(b.handle, *(fptr(t.numpy()) for t in pinned[:3]), n))  # pinned in
+    a.write_state(*state)  # pageable in (same values)
+    a.dispatch(scene.substeps)
+    b.dispatch(scene.substeps)
+    check(L.vsim_read_state(b.handle, *(fptr(t.numpy()) for t in pinned[3:]), n))  # pinned out
+    for x, y in zip(a.read_state(), pinned[3:]):  # pageable out
+        assert np.array_equal(x, y.numpy())
+    check(L.vsim_read_positions(b.handle, fptr(pinned[3].numpy()), n))
+    assert np.array_equal(a.read_positions(), pinned[3].numpy())
+    assert np.all(pinned[3].numpy()[:, 3] == 0)
+
+
 def test_timing_colour_passes_leaves_state(lib):
     """vsim_time_colour_passes restores what the timed passes moved: the
     next frame still equals the oracle's."""

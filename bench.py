@@ -678,7 +678,7 @@ def drift(frames: int = 300):
 
 
 def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, settle_frames: int = 30,
-                  repeats_at_70: int = 3):
+                  repeats_at_70: int = 3, engines=("sessions", "frames")):
     """Continuous batching under load: a pool of sessions resident on the
     GPU; requests advance a session k ~ U{1..4} frames, half of them dragging
     a random surface node along a seeded Bezier curve at 0.5 m/s. Every
@@ -686,15 +686,20 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
     bodies have landed and flattened -- the state they spend their life in,
     with far more self contact than at rest -- before anything is measured.
 
-    For each tick budget (occupied cells one tick may step, 0 = no cap;
-    vsim_server_set_tick_budget): saturation measured closed-loop (every
-    session always has a request), then Poisson arrivals at 25/50/70/90 % of
-    that saturation, the 70 % point `repeats_at_70` times, each run by the
-    library's own request loop (vsim_server_run) against a pre-drawn
-    schedule, so no client code sits between ticks. Each of these starts from
-    the same settled state (every session checkpointed after the settling
-    frames and written back before the measurement). Frame latency of a
-    request = (completion - scheduled arrival) / k."""
+    For each engine of the library's request loop (vsim_server_set_engine:
+    "sessions", small sessions' requests run whole by the session kernel,
+    launches overlapping, the larger ones in ticks alongside; "frames",
+    ticks of one shared frame for all, under each tick budget -- occupied
+    cells one tick may step, 0 = no cap): saturation measured closed-loop
+    (as many requests outstanding as sessions, each completion replaced by
+    one to a uniformly drawn session: the capacity for the open loop's
+    session mix), then Poisson arrivals
+    at 25/50/70/90 % of that saturation, the 70 % point `repeats_at_70`
+    times, each run by vsim_server_run against a pre-drawn schedule, so no
+    client code sits between launches. Each of these starts from the same
+    settled state (every session checkpointed after the settling frames and
+    written back before the measurement). Frame latency of a request =
+    (completion - scheduled arrival) / k."""
     import vsim.scenes as sc
     from vsim.server import Server
 
@@ -735,14 +740,15 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
     def saturation():
         restore()
         frames, flags = specs(200_000)
+        sessions = rng.integers(0, admitted, frames.size)
         c0 = server.stats()["cell_updates"]
-        _, rep = server.run(None, None, frames, flags, drags, closed_loop_seconds=seconds_per_point)
+        _, rep = server.run(None, sessions, frames, flags, drags, closed_loop_seconds=seconds_per_point)
         cells = server.stats()["cell_updates"] - c0
         return {"requests_per_s": round(rep["requests"] / rep["seconds"], 1),
                 "session_frames_per_s": round(rep["frames"] / rep["seconds"], 1), "ticks": rep["ticks"],
                 "cell_updates_per_s_incl_drain": round(cells / rep["seconds"]),
-                "method": "closed loop in the library's request loop (vsim_server_run): every session always has "
-                          "a request"}
+                "method": "closed loop in the library's request loop (vsim_server_run): as many requests "
+                          "outstanding as sessions, each completion replaced by one to a uniformly drawn session"}
 
     def point(frac, sat_rate):
         restore()
@@ -770,24 +776,53 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
                 "mean_tick_ms": tick_ms,
                 "cell_updates_per_s": round((st_after["cell_updates"] - st_before["cell_updates"]) / rep["seconds"])}
 
-    runs = {}
-    for budget in budgets:
-        server.set_tick_budget(budget)
+    def sweep():
         sat = saturation()
         points = []
         for frac in (0.25, 0.5, 0.7, 0.9):
             for _ in range(repeats_at_70 if frac == 0.7 else 1):
                 points.append(point(frac, sat["requests_per_s"]))
         p99_70 = [p["frame_latency_ms"]["p99"] for p in points if p["load"] == 0.7]
-        runs[str(budget)] = {"tick_cell_budget": budget, "saturation": sat, "sweep": points,
-                             "p99_frame_latency_ms_at_70pct": {"max": max(p99_70), "all": p99_70}}
+        return {"saturation": sat, "sweep": points,
+                "p99_frame_latency_ms_at_70pct": {"max": max(p99_70), "all": p99_70}}
+
+    def floors(engine):
+        """One 1-frame request alone on the idle server, for the smallest,
+        median and largest resident session: median of 15 (completion -
+        arrival), the latency with no queueing at all."""
+        order = sorted(range(admitted), key=lambda q: bodies[q].cell_count)
+        out = {}
+        for label, q in (("smallest", order[0]), ("median", order[len(order) // 2]), ("largest", order[-1])):
+            lat = []
+            for _ in range(15):
+                done, _ = server.run(np.zeros(1), np.array([q]), np.ones(1, np.int64), np.zeros(1, np.int64))
+                lat.append(done[0]["completed"] - done[0]["submitted"])
+            out[label] = {"session_cells": bodies[q].cell_count, "ms": round(1e3 * float(np.median(lat)), 3)}
+        return out
+
+    by_engine = {}
+    for engine in engines:
+        if engine == "sessions":
+            server.set_engine(server.SESSIONS)
+            restore()
+            by_engine[engine] = {"one_request_floor": floors(engine), **sweep()}
+        else:
+            server.set_engine(server.FRAMES)
+            restore()
+            by_engine[engine] = {"one_request_floor": floors(engine)}
+            runs = {}
+            for budget in budgets:
+                server.set_tick_budget(budget)
+                runs[str(budget)] = {"tick_cell_budget": budget, **sweep()}
+            server.set_tick_budget(0)
+            by_engine[engine]["by_tick_budget"] = runs
     st = server.stats()
     server.destroy()
     return {"workload": f"{admitted} sessions ({count} offered), noise blobs on 8^3-64^3 grids, "
                         f"{sum(b.cell_count for b in bodies[:admitted])} cells resident, "
                         f"{st['resident_bytes'] / 1e9:.2f} GB of the 150 GB budget; k ~ U{{1..4}} frames, "
                         f"50% with a Bezier drag at 0.5 m/s",
-            "by_tick_budget": runs, "settle": {"frames": settle_frames, "seconds": round(settle_s, 1)},
+            "by_engine": by_engine, "settle": {"frames": settle_frames, "seconds": round(settle_s, 1)},
             "pool_generation_s": round(gen_s, 1)}
 
 
@@ -810,6 +845,8 @@ def main():
     ap.add_argument("--batch-only", action="store_true", help="only the batching comparison")
     ap.add_argument("--tick-budgets", default=None,
                     help="comma-separated tick cell budgets for the serving sweep (0 = no cap)")
+    ap.add_argument("--serve-engines", default="sessions,frames",
+                    help="comma-separated request-loop engines for the serving sweep (sessions, frames)")
     ap.add_argument("--capture-tick", type=int, default=None, metavar="K",
                     help="profiler capture mode: one server tick of K sessions, for `ncu --profile-from-start off`")
     ap.add_argument("--capture-after", type=int, default=None, metavar="N",
@@ -861,7 +898,7 @@ def main():
         return
     budgets = [int(float(v)) for v in args.tick_budgets.split(",")] if args.tick_budgets else [0]
     if args.serve_only:
-        print(json.dumps({"serving": serving_sweep(args.quick, budgets)}))
+        print(json.dumps({"serving": serving_sweep(args.quick, budgets, engines=args.serve_engines.split(","))}))
         return
     if args.batch_only:
         print(json.dumps({"batching": batched_vs_plain(10, args.quick, cpu=not args.no_cpu)}))
@@ -914,7 +951,7 @@ def main():
     if rank == 0 and not args.no_batch:
         detail["batching"] = batched_vs_plain(10, args.quick, cpu=not args.no_cpu)
     if rank == 0 and not args.no_serve:
-        detail["serving"] = serving_sweep(args.quick, budgets)
+        detail["serving"] = serving_sweep(args.quick, budgets, engines=args.serve_engines.split(","))
     if rank == 0 and not args.no_stress:
         detail["stress"] = stress(args.quick, hbm)
     if rank == 0 and not args.no_cloud:

@@ -541,16 +541,33 @@ typedef struct vsim_run_report {
    each request is submitted when its arrival time comes -- its completion
    records that scheduled time as `submitted` -- ticks run while anything is
    pending, and the loop returns once every request has completed. Closed
-   loop (closed_loop_seconds > 0): every resident session starts with a
-   request and gets the list's next one (cycling; its session and arrival
-   unused) the moment its last completes, for that long; then the loop
-   drains. Completions go to `out` (up to `capacity`; NULL: counts only),
+   loop (closed_loop_seconds > 0): as many requests as sessions are resident
+   are submitted at once, the list's first (cycling), and each completion
+   submits the list's next one (its arrival unused) to the session it
+   names, for that long; then the loop drains. With sessions drawn
+   uniformly the outstanding requests gather where service is slowest, so
+   the rate measured is the capacity for that mix. Completions go to `out` (up to `capacity`; NULL: counts only),
    not to vsim_server_poll. Needs no request pending at the start. A drag
    request drags drags[session] (indexed by session id: one per session
-   offered). No reference counterpart. */
+   offered). How requests run is the server's engine
+   (vsim_server_set_engine); a tick of the session engine is one launch.
+   No reference counterpart. */
 int vsim_server_run(vsim_server* server, const vsim_scheduled_request* requests, uint32_t n,
                     const vsim_drag* drags, double closed_loop_seconds, vsim_completion* out,
                     uint32_t capacity, vsim_run_report* report);
+/* Engines of vsim_server_run. FRAMES: ticks, one frame at a time for every
+   session with a request, as vsim_server_tick runs them. SESSIONS (the
+   default): a session whose largest colour has at most `block_cells` cells
+   (default 256) runs each request whole -- all its frames -- in one block
+   of the session kernel, else, with at most `cluster_cells`, in one
+   cluster of 8 blocks (default 0: none); every such session that has a
+   request and none running starts in the next launch, launches overlap,
+   and a request completes when its own job ends. Larger sessions run in
+   ticks of shared frames on the server's stream at the same time. Every
+   engine gives every session the same result, bit for bit. */
+#define VSIM_SERVE_FRAMES 0
+#define VSIM_SERVE_SESSIONS 1
+int vsim_server_set_engine(vsim_server* server, int engine, uint32_t block_cells, uint32_t cluster_cells);
 /* Requests completed since the last poll (at most `capacity`). */
 int vsim_server_poll(vsim_server* server, vsim_completion* out, uint32_t capacity, uint32_t* count);
 int vsim_server_get_stats(const vsim_server* server, vsim_server_stats* out);

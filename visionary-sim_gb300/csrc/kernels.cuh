@@ -203,6 +203,66 @@ cudaError_t launchRefreshW(cudaStream_t st, uint32_t first, uint32_t n, const fl
 cudaError_t launchMergeXyz(cudaStream_t st, const float4* in, uint32_t n, float4* pos);
 cudaError_t launchDropW(cudaStream_t st, const float4* in, uint32_t n, float4* out);
 
+// ---- session kernel (session.cu) -------------------------------------------
+
+// One request of an isolated session: its body's ranges and the frames to
+// run. Read by the kernel from host-mapped memory.
+struct SessionJob {
+    uint32_t nodeFirst, nodeCount;  // its range of the active-node list
+    uint32_t recFirst, recCount;    // its range of the surface records
+    uint32_t cellFirst[8];          // per colour: its first cell in the cell list
+    uint32_t cellCount[8];
+    uint32_t body;
+    uint32_t frames;
+    int32_t heldBefore;             // global node the session held until now, -1 for none
+    int32_t held;                   // global node this request holds, -1 for none
+    uint32_t driveFirst;            // its first frame's row pair in the drive table
+    uint32_t ticket;                // written to done[body] when the request has run
+    uint32_t pad[2];
+};
+
+constexpr uint32_t kSessionCluster = 8;   // blocks of a cluster
+constexpr uint32_t kSessionBlock = 256;   // threads of a block
+constexpr uint32_t kNoJob = 0xffffffffu;
+
+// Checks a job can fail (SessionLaunch::fault, ::status). A failed job
+// skips the rest of its work; the host reports it as an error.
+enum SessionFault : uint32_t {
+    kFaultNone = 0,
+    kFaultRange = 1,    // a range of the job outside the pool's tables
+    kFaultRecords = 2,  // the buckets' runs do not add up to the session's records
+    kFaultRun = 3,      // a bucket's run outside the session's records
+    kFaultScatter = 4,  // a record's place outside its bucket's run
+};
+
+// A cluster's work: one wide job run by all its blocks, or up to
+// kSessionCluster narrow jobs, one per block (kNoJob: none).
+struct SessionGroup {
+    uint32_t wide;
+    uint32_t job[kSessionCluster];
+};
+
+struct SessionLaunch {
+    const SessionGroup* groups;
+    uint32_t groupCount;
+    const SessionJob* jobs;
+    const float4* drive;   // per frame of a dragging job: target, target velocity
+    uint32_t* cursor;      // per body: segment cursor of its records
+    uint32_t* fault;       // per body, device: the check the running job failed, 0 for none
+    uint32_t* done;        // per body: ticket of its last request run (host-mapped)
+    uint32_t* status;      // per body: its last job's fault, written before the ticket (host-mapped)
+    // What the jobs' ranges are checked against.
+    uint32_t activeCount, cellCount, surfaceCount, nodeCount, bodyCount, driveRows;
+    uint32_t substeps;
+    uint32_t iterations;
+    uint32_t limited;      // any body has a stretch limit
+    uint32_t contact;
+    uint32_t warpRecords;  // the gather takes a warp per record while records <= warpRecords x warps
+    StretchLengths lens;
+};
+
+cudaError_t launchSessions(cudaStream_t st, const DeviceState& d, const SessionLaunch& L);
+
 // ---- splats ---------------------------------------------------------------
 
 struct SplatBody {

@@ -19,12 +19,22 @@
 // disjoint node ranges, their contact grids are disjoint, and inactive bodies
 // are skipped by every kernel. So a request's result is the same whether it
 // ran alone or among others.
+//
+// The request loop (vsim_server_run) has a second engine: session kernels
+// (session.cu). There a request is a job -- its session's frames, all of
+// them, run by one block or one cluster -- and the loop launches every
+// ready request as soon as one of a few launch slots is free, without
+// waiting for requests already running; each job reports its end through a
+// ticket in host-mapped memory, so a short request is retired when it ends,
+// not when its launch does. The explicit tick (vsim_server_tick) stays the
+// frame-at-a-time engine above; both give every session the same result.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <deque>
 #include <new>
+#include <string>
 #include <thread>
 
 #include "sim_internal.cuh"
@@ -74,6 +84,35 @@ struct Session {
 
 int applyHolds(vsim_server* s);
 
+// One launch of session kernels in flight: its stream, its end, and the
+// tables its kernel reads -- groups, jobs, drive rows -- staged in pinned
+// memory and copied to the device in stream order before the launch (both
+// rewritten only once it has ended).
+struct LaunchSlot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t start = nullptr, end = nullptr;
+    bool busy = false;
+    double launched = 0;
+    std::vector<uint32_t> sessions;  // the sessions it runs
+    unsigned char* staging = nullptr;
+    unsigned char* tables = nullptr;
+    size_t tableCap = 0;
+};
+
+constexpr int kLaunchSlots = 8;
+
+// The session-kernel engine of one device pool.
+struct SessionEngine {
+    LaunchSlot slot[kLaunchSlots];
+    uint32_t* done = nullptr;      // per body: ticket of the last job run (host-mapped)
+    uint32_t* doneDev = nullptr;
+    uint32_t* status = nullptr;    // per body: fault of the last job run (host-mapped)
+    uint32_t* statusDev = nullptr;
+    uint32_t* cursor = nullptr;    // per body, device
+    uint32_t* fault = nullptr;     // per body, device
+    uint32_t ticket = 0;
+};
+
 }  // namespace
 
 struct vsim_server {
@@ -96,6 +135,16 @@ struct vsim_server {
     uint64_t tickCellBudget = 0;  // cells one tick may step; 0: every session with a pending request
     std::chrono::steady_clock::time_point origin = std::chrono::steady_clock::now();
     cudaEvent_t frameStart = nullptr, frameDone = nullptr;
+    int engine = VSIM_SERVE_SESSIONS;  // how vsim_server_run runs requests
+    // Session engine: a session whose largest colour has at most blockCells
+    // cells runs in one block, else at most clusterCells in one cluster,
+    // else in ticks of shared frames.
+    uint32_t blockCells = kSessionBlock, clusterCells = 0;
+    SessionEngine* sessionEngine = nullptr;  // built on first use for the current pool
+    std::vector<uint8_t> kernelHolds;  // per session, during a run: its drag holds are the session kernel's
+    // The tick in flight (startTick .. finishTick).
+    bool tickInFlight = false;
+    double tickEntered = 0;
 };
 
 namespace {
@@ -104,6 +153,7 @@ namespace {
 int applyHolds(vsim_server* s) {
     std::vector<uint32_t> nodes;
     for (uint32_t b = 0; b < s->resident.size(); b++) {
+        if (!s->kernelHolds.empty() && s->kernelHolds[s->resident[b]]) continue;
         const int64_t local = s->held[s->resident[b]];
         if (local >= 0) nodes.push_back(s->sim->offsets[b] + uint32_t(local));
     }
@@ -153,7 +203,38 @@ void dropSim(vsim_sim*& sim) {
     sim = nullptr;
 }
 
+void freeMapped(void*& p) {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+}
+
+// Waits for every launch in flight and frees the engine.
+void dropEngine(vsim_server* s) {
+    SessionEngine* e = s->sessionEngine;
+    if (!e) return;
+    for (LaunchSlot& l : e->slot) {
+        if (l.stream) {
+            cudaStreamSynchronize(l.stream);
+            cudaStreamDestroy(l.stream);
+        }
+        if (l.start) cudaEventDestroy(l.start);
+        if (l.end) cudaEventDestroy(l.end);
+        freeMapped(reinterpret_cast<void*&>(l.staging));
+        if (l.tables) cudaFree(l.tables);
+    }
+    freeMapped(reinterpret_cast<void*&>(e->done));
+    freeMapped(reinterpret_cast<void*&>(e->status));
+    if (e->cursor) cudaFree(e->cursor);
+    if (e->fault) cudaFree(e->fault);
+    delete e;
+    s->sessionEngine = nullptr;
+}
+
 int destroyServer(vsim_server* s) {
+    if (s->sim) {
+        DeviceGuard guard(s->sim->device);
+        dropEngine(s);
+    }
     if (s->sim) {
         DeviceGuard guard(s->sim->device);
         cudaStreamSynchronize(s->sim->stream);
@@ -328,6 +409,7 @@ int vsim_server_set_resident(vsim_server* s, const uint32_t* sessions, uint32_t 
     std::vector<uint32_t> members(sessions, sessions + count);
     vsim_sim* next = nullptr;
     if (int rc = buildPool(s, members, &next)) return rc;  // the old pool is untouched on failure
+    dropEngine(s);  // its tables are sized for the old pool
     // States back: each member's checkpoint, or its rest state if it has none.
     {
         const size_t n = next->nodeCount;
@@ -408,12 +490,17 @@ int vsim_server_submit(vsim_server* s, uint32_t session, uint32_t frames, const 
     return submitAt(s, session, frames, drag, seconds(s), request);
 }
 
-int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
-    clearError();
-    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
-    if (stepped) *stepped = 0;
+}  // extern "C"
+
+namespace {
+
+// The first half of a tick: picks the sessions the frame runs (those with a
+// pending request, `eligible` ones only when given), sets their holds and
+// drag targets and launches the frame on the pool's stream without waiting.
+// *stepped: how many sessions it runs (0: nothing launched).
+int startTick(vsim_server* s, const std::vector<uint8_t>* eligible, uint32_t* stepped) {
+    *stepped = 0;
     vsim_sim* sim = s->sim;
-    DeviceGuard guard(sim->device);
     const double frameDt = s->config.substeps * s->config.step_duration;
     const double entered = seconds(s);
     const uint32_t bodies = uint32_t(s->resident.size());
@@ -426,7 +513,7 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
         std::vector<uint32_t> started, waiting;
         for (uint32_t b = 0; b < bodies; b++) {
             const auto& q = s->queue[s->resident[b]];
-            if (q.empty()) continue;
+            if (q.empty() || (eligible && !(*eligible)[s->resident[b]])) continue;
             (q.front().done > 0 ? started : waiting).push_back(b);
         }
         if (s->tickCellBudget == 0) {
@@ -517,11 +604,21 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
     rc = runFrame(sim, s->config.substeps);
     if (rc) return rc;
     CK(cudaEventRecord(s->frameDone, sim->stream), "serve frame");
+    s->tickInFlight = true;
+    s->tickEntered = entered;
+    *stepped = active;
+    return VSIM_OK;
+}
+
+// The second half: waits for the frame and retires what it finished.
+int finishTick(vsim_server* s) {
+    vsim_sim* sim = s->sim;
+    s->tickInFlight = false;
     CK(cudaEventSynchronize(s->frameDone), "serve frame");
     float frameMs = 0;
     if (cudaEventElapsedTime(&frameMs, s->frameStart, s->frameDone) == cudaSuccess) s->frameSeconds += 1e-3 * frameMs;
     const double now = seconds(s);
-    for (uint32_t b = 0; b < bodies; b++) {
+    for (uint32_t b = 0; b < s->resident.size(); b++) {
         if (!sim->activeHost[b]) continue;
         const uint32_t i = s->resident[b];
         Request& r = s->queue[i].front();
@@ -536,10 +633,412 @@ int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
         }
     }
     s->ticks++;
-    s->tickSeconds += seconds(s) - entered;
+    s->tickSeconds += seconds(s) - s->tickEntered;
+    return VSIM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vsim_server_tick(vsim_server* s, uint32_t* stepped) {
+    clearError();
+    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
+    if (stepped) *stepped = 0;
+    DeviceGuard guard(s->sim->device);
+    uint32_t active = 0;
+    if (int rc = startTick(s, nullptr, &active)) return rc;
+    if (active == 0) return VSIM_OK;
+    if (int rc = finishTick(s)) return rc;
     if (stepped) *stepped = active;
     return VSIM_OK;
 }
+
+}  // extern "C"
+
+namespace {
+
+// What both engines' request loops share: the schedule, the closed loop's
+// refills and measured window, the completions handed back.
+struct RunState {
+    const vsim_scheduled_request* requests;
+    uint32_t n;
+    const vsim_drag* drags;
+    bool closed;
+    double closedSeconds;
+    vsim_completion* out;
+    uint32_t capacity;
+    std::vector<vsim_completion> done;
+    uint64_t frames0 = 0, ticks0 = 0, requestsDone = 0;
+    uint32_t next = 0;
+    double t0 = 0;
+    bool windowClosed = false;
+    uint64_t windowRequests = 0, windowFrames = 0, windowTicks = 0;
+    double windowSeconds = 0;
+
+    int submit(vsim_server* s, uint32_t session, const vsim_scheduled_request& q, double at) {
+        return submitAt(s, session, q.frames, q.drag ? &drags[session] : nullptr, at, nullptr);
+    }
+    // Open loop: queue every request whose arrival time has come.
+    int admitDue(vsim_server* s) {
+        if (closed) return VSIM_OK;
+        const double now = seconds(s);
+        while (next < n && t0 + requests[next].arrival <= now) {
+            if (int rc = submit(s, requests[next].session, requests[next], t0 + requests[next].arrival)) return rc;
+            next++;
+        }
+        return VSIM_OK;
+    }
+    // Takes the server's new completions; in a closed loop each is replaced
+    // by the list's next request, to the session that request names, until
+    // the span ends.
+    int collect(vsim_server* s) {
+        if (s->completed.empty()) return VSIM_OK;
+        const bool refill = closed && seconds(s) - t0 < closedSeconds;
+        if (closed && !refill && !windowClosed) {  // the closed loop's measured span ends here
+            windowClosed = true;
+            windowRequests = requestsDone + s->completed.size();
+            windowFrames = s->sessionFrames - frames0;
+            windowTicks = s->ticks - ticks0;
+            windowSeconds = seconds(s) - t0;
+        }
+        for (const vsim_completion& c : s->completed) {
+            requestsDone++;
+            if (out && done.size() < capacity) done.push_back(c);
+            if (refill) {
+                if (int rc = submit(s, requests[next].session, requests[next], seconds(s))) return rc;
+                next = (next + 1) % n;
+            }
+        }
+        s->completed.clear();
+        return VSIM_OK;
+    }
+    // Sleeps until shortly before the next arrival.
+    void idle(const vsim_server* s) const {
+        const double wait = t0 + requests[next].arrival - seconds(s);
+        if (wait > 2e-4) std::this_thread::sleep_for(std::chrono::duration<double>(wait - 1e-4));
+    }
+};
+
+int runFrames(vsim_server* s, RunState& st) {
+    while (true) {
+        if (int rc = st.admitDue(s)) return rc;
+        if (s->pending) {
+            if (int rc = vsim_server_tick(s, nullptr)) return rc;
+            if (int rc = st.collect(s)) return rc;
+            continue;
+        }
+        if (st.closed || st.next >= st.n) return VSIM_OK;
+        st.idle(s);
+    }
+}
+
+// Room for `need` bytes of tables in the slot's staging and device buffers.
+int growTables(LaunchSlot& l, size_t need) {
+    if (need <= l.tableCap) return VSIM_OK;
+    const size_t want = std::max<size_t>(need, 2 * l.tableCap);
+    if (l.staging) cudaFreeHost(l.staging);
+    if (l.tables) cudaFree(l.tables);
+    l.staging = l.tables = nullptr;
+    l.tableCap = 0;
+    CK(cudaMallocHost(reinterpret_cast<void**>(&l.staging), want), "allocate job tables");
+    CK(cudaMalloc(reinterpret_cast<void**>(&l.tables), want), "allocate job tables");
+    l.tableCap = want;
+    return VSIM_OK;
+}
+
+inline size_t align16(size_t n) { return (n + 15) & ~size_t(15); }
+
+template <class T>
+T* devicePointer(T* host) {
+    void* d = nullptr;
+    return cudaHostGetDevicePointer(&d, host, 0) == cudaSuccess ? static_cast<T*>(d) : nullptr;
+}
+
+int buildEngine(vsim_server* s) {
+    if (s->sessionEngine) return VSIM_OK;
+    auto* e = new (std::nothrow) SessionEngine();
+    if (!e) return fail(VSIM_ERR_NOMEM, "out of host memory");
+    s->sessionEngine = e;
+    const size_t bodies = std::max<size_t>(1, s->resident.size());
+    CK(cudaHostAlloc(reinterpret_cast<void**>(&e->done), bodies * 4, cudaHostAllocMapped), "allocate tickets");
+    std::memset(e->done, 0, bodies * 4);
+    CK(cudaHostAlloc(reinterpret_cast<void**>(&e->status), bodies * 4, cudaHostAllocMapped), "allocate tickets");
+    std::memset(e->status, 0, bodies * 4);
+    e->doneDev = devicePointer(e->done);
+    e->statusDev = devicePointer(e->status);
+    if (!e->doneDev || !e->statusDev) return fail(VSIM_ERR_CUDA, "map tickets");
+    CK(cudaMalloc(reinterpret_cast<void**>(&e->cursor), bodies * 4), "allocate segment cursors");
+    CK(cudaMalloc(reinterpret_cast<void**>(&e->fault), bodies * 4), "allocate job checks");
+    for (LaunchSlot& l : e->slot) {
+        CK(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking), "create launch stream");
+        CK(cudaEventCreate(&l.start), "create launch event");
+        CK(cudaEventCreate(&l.end), "create launch event");
+    }
+    return VSIM_OK;
+}
+
+// Marks session i's running request done, at `now`.
+void retire(vsim_server* s, uint32_t i, double now) {
+    Request& r = s->queue[i].front();
+    r.done = r.frames;
+    s->sessionFrames += r.frames;
+    s->cellUpdates += uint64_t(s->sessions[i].cells) * s->config.substeps * r.frames;
+    s->completed.push_back(vsim_completion{r.id, r.session, r.frames, r.submitted, now, r.firstTick, r.firstTick});
+    s->queue[i].pop_front();
+    s->pending--;
+}
+
+// One launch over every session that has a request and none running, if a
+// launch slot is free. A request's drag targets for all its frames are
+// computed here, as the frame-at-a-time engine computes them frame by frame.
+int launchReady(vsim_server* s, const std::vector<uint8_t>& inKernel, std::vector<int8_t>& running,
+                std::vector<uint32_t>& ticketOf, bool& launched) {
+    launched = false;
+    SessionEngine* e = s->sessionEngine;
+    LaunchSlot* l = nullptr;
+    for (LaunchSlot& c : e->slot)
+        if (!c.busy) {
+            l = &c;
+            break;
+        }
+    if (!l) return VSIM_OK;
+    const double entered = seconds(s);
+    vsim_sim* sim = s->sim;
+    std::vector<uint32_t> ready;
+    size_t driveRows = 0;
+    for (uint32_t i : s->resident)
+        if (inKernel[i] && running[i] < 0 && !s->queue[i].empty()) {
+            ready.push_back(i);
+            if (s->queue[i].front().drag) driveRows += s->queue[i].front().frames;
+        }
+    if (ready.empty()) return VSIM_OK;
+    const size_t groupBytes = align16(ready.size() * sizeof(SessionGroup));
+    const size_t jobBytes = align16(ready.size() * sizeof(SessionJob));
+    if (int rc = growTables(*l, groupBytes + jobBytes + 2 * std::max<size_t>(driveRows, 1) * sizeof(float4)))
+        return rc;
+    auto* groupTable = reinterpret_cast<SessionGroup*>(l->staging);
+    auto* jobTable = reinterpret_cast<SessionJob*>(l->staging + groupBytes);
+    auto* driveTable = reinterpret_cast<float4*>(l->staging + groupBytes + jobBytes);
+    const double frameDt = s->config.substeps * s->config.step_duration;
+    std::vector<uint32_t> wide, narrow;
+    uint32_t rows = 0;
+    for (uint32_t k = 0; k < ready.size(); k++) {
+        const uint32_t i = ready[k];
+        const uint32_t b = uint32_t(s->slot[i]);
+        Request& r = s->queue[i].front();
+        SessionJob& j = jobTable[k];
+        j = SessionJob{};
+        j.nodeFirst = sim->nodeBodyStart[b];
+        j.nodeCount = sim->nodeBodyStart[b + 1] - sim->nodeBodyStart[b];
+        j.recFirst = sim->recordBodyStart[b];
+        j.recCount = sim->recordBodyStart[b + 1] - sim->recordBodyStart[b];
+        uint32_t widest = 0;
+        for (int c = 0; c < 8; c++) {
+            j.cellFirst[c] = sim->colorStart[c] + sim->colourBodyStart[c][b];
+            j.cellCount[c] = sim->colourBodyStart[c][b + 1] - sim->colourBodyStart[c][b];
+            widest = std::max(widest, j.cellCount[c]);
+        }
+        j.body = b;
+        j.frames = r.frames;
+        j.heldBefore = s->held[i] >= 0 ? int32_t(sim->offsets[b] + uint32_t(s->held[i])) : -1;
+        s->held[i] = r.drag ? int64_t(r.path.node) : int64_t(-1);
+        j.held = s->held[i] >= 0 ? int32_t(sim->offsets[b] + uint32_t(s->held[i])) : -1;
+        j.driveFirst = rows;
+        if (r.drag) {
+            // The drag starts on its curve (the grab's placement) and
+            // advances one frame at a time at its speed; velocity is each
+            // frame's motion over its duration (simulator.js:309-315).
+            double prev[3], p[3], dp[3];
+            bezier(r.path.control, 0.0, prev, dp);
+            for (uint32_t f = 0; f < r.frames; f++) {
+                bezier(r.path.control, r.t, p, dp);
+                const double rate = std::sqrt(dp[0] * dp[0] + dp[1] * dp[1] + dp[2] * dp[2]);
+                r.t = std::min(1.0, r.t + r.path.speed * frameDt / std::max(rate, 1e-9));
+                bezier(r.path.control, r.t, p, dp);
+                driveTable[2 * (rows + f)] = make_float4(float(p[0]), float(p[1]), float(p[2]), 0.0f);
+                driveTable[2 * (rows + f) + 1] =
+                    make_float4(float((p[0] - prev[0]) / frameDt), float((p[1] - prev[1]) / frameDt),
+                                float((p[2] - prev[2]) / frameDt), 0.0f);
+                for (int a = 0; a < 3; a++) prev[a] = p[a];
+            }
+            for (int a = 0; a < 3; a++) s->prevTarget[3 * i + a] = prev[a];
+            rows += r.frames;
+        }
+        j.ticket = ++e->ticket;
+        ticketOf[i] = j.ticket;
+        (widest > s->blockCells ? wide : narrow).push_back(k);
+    }
+    // Wide jobs first (each a cluster), then the narrow ones, a block each.
+    uint32_t groups = 0;
+    for (uint32_t k : wide) {
+        SessionGroup& g = groupTable[groups++];
+        g.wide = 1;
+        g.job[0] = k;
+        for (uint32_t r = 1; r < kSessionCluster; r++) g.job[r] = kNoJob;
+    }
+    for (size_t at = 0; at < narrow.size(); at += kSessionCluster) {
+        SessionGroup& g = groupTable[groups++];
+        g.wide = 0;
+        for (uint32_t r = 0; r < kSessionCluster; r++) g.job[r] = at + r < narrow.size() ? narrow[at + r] : kNoJob;
+    }
+    SessionLaunch L{};
+    L.groups = reinterpret_cast<const SessionGroup*>(l->tables);
+    L.groupCount = groups;
+    L.jobs = reinterpret_cast<const SessionJob*>(l->tables + groupBytes);
+    L.drive = reinterpret_cast<const float4*>(l->tables + groupBytes + jobBytes);
+    L.cursor = e->cursor;
+    L.fault = e->fault;
+    L.done = e->doneDev;
+    L.status = e->statusDev;
+    L.activeCount = sim->activeCount;
+    L.cellCount = sim->cellCount;
+    L.surfaceCount = sim->surfaceCount;
+    L.nodeCount = sim->nodeCount;
+    L.bodyCount = uint32_t(s->resident.size());
+    L.driveRows = rows;
+    L.substeps = s->config.substeps;
+    L.iterations = sim->iterations;
+    L.limited = anyStretch(sim) ? 1u : 0u;
+    L.contact = sim->contact && sim->surfaceCount > 0 ? 1u : 0u;
+    L.warpRecords = 4;
+    L.lens = stretchLengths();
+    CK(cudaMemcpyAsync(l->tables, l->staging, groupBytes + jobBytes + 2 * size_t(rows) * sizeof(float4),
+                       cudaMemcpyHostToDevice, l->stream),
+       "upload job tables");
+    CK(cudaEventRecord(l->start, l->stream), "launch sessions");
+    CK(launchSessions(l->stream, sim->d, L), "launch sessions");
+    CK(cudaEventRecord(l->end, l->stream), "launch sessions");
+    l->busy = true;
+    l->launched = seconds(s);
+    l->sessions = ready;
+    for (uint32_t i : ready) {
+        running[i] = int8_t(l - e->slot);  // the slot it runs in
+        s->queue[i].front().firstTick = s->ticks;
+    }
+    s->ticks++;
+    s->prepareSeconds += l->launched - entered;
+    launched = true;
+    return VSIM_OK;
+}
+
+int runSessions(vsim_server* s, RunState& st) {
+    if (int rc = buildEngine(s)) return rc;
+    vsim_sim* sim = s->sim;
+    if (int rc = syncParams(sim)) return rc;
+    CK(cudaStreamSynchronize(sim->stream), "serve sessions");
+    SessionEngine* e = s->sessionEngine;
+    // Sessions small enough for a block (or, if allowed, a cluster) run in
+    // the session kernel; the rest in ticks of shared frames on the pool's
+    // stream, alongside. The kernel sessions' drag holds are the kernel's
+    // own while the run lasts, so the pool's hold list -- which the ticks
+    // rewrite -- leaves their nodes alone.
+    std::vector<uint8_t> inKernel(s->sessions.size(), 0), inTicks(s->sessions.size(), 0);
+    for (uint32_t b = 0; b < s->resident.size(); b++) {
+        uint32_t widest = 0;
+        for (int c = 0; c < 8; c++) widest = std::max(widest, sim->colourBodyStart[c][b + 1] - sim->colourBodyStart[c][b]);
+        const uint32_t i = s->resident[b];
+        inKernel[i] = widest <= std::max(s->blockCells, s->clusterCells);
+        inTicks[i] = !inKernel[i];
+    }
+    s->kernelHolds = inKernel;
+    if (int rc = applyHolds(s)) return rc;
+    // Per session: the launch slot its request runs in, -1 for none. A
+    // session retired by its ticket may run again in another slot while the
+    // first slot still runs others, so a slot answers only for its own.
+    std::vector<int8_t> running(s->sessions.size(), -1);
+    std::vector<uint32_t> ticketOf(s->sessions.size(), 0);
+    bool faulted = false;
+    int fault = VSIM_OK;
+    // An error leaves nothing in flight behind it.
+    auto bail = [&](int rc) {
+        for (LaunchSlot& l : e->slot) cudaStreamSynchronize(l.stream);
+        if (s->tickInFlight) finishTick(s);
+        s->kernelHolds.clear();
+        for (int k = 0; k < kLaunchSlots; k++) {
+            LaunchSlot& l = e->slot[k];
+            for (uint32_t i : l.sessions)
+                if (running[i] == k) {
+                    retire(s, i, seconds(s));
+                    running[i] = -1;
+                }
+            l.sessions.clear();
+            l.busy = false;
+        }
+        s->completed.clear();
+        return rc;
+    };
+    while (true) {
+        if (int rc = st.admitDue(s)) return bail(rc);
+        // Retire the jobs that have ended: by their tickets, or all of a
+        // launch once it has ended.
+        bool anyRunning = false, progressed = false;
+        for (int k = 0; k < kLaunchSlots; k++) {
+            LaunchSlot& l = e->slot[k];
+            if (!l.busy) continue;
+            const cudaError_t q = cudaEventQuery(l.end);
+            if (q != cudaSuccess && q != cudaErrorNotReady) return bail(cudaFail(q, "serve sessions"));
+            const bool ended = q == cudaSuccess;
+            const double now = seconds(s);
+            for (uint32_t i : l.sessions) {
+                if (running[i] != k) continue;
+                const uint32_t b = uint32_t(s->slot[i]);
+                const bool seen = __atomic_load_n(&e->done[b], __ATOMIC_ACQUIRE) == ticketOf[i];
+                if (!seen && !ended) continue;
+                const uint32_t check = seen ? e->status[b] : 0xffffffffu;
+                retire(s, i, now);
+                running[i] = -1;
+                progressed = true;
+                if (check != kFaultNone && !faulted) {
+                    faulted = true;
+                    fault = fail(VSIM_ERR_CUDA, "session kernel: session " + std::to_string(i) +
+                                                    (seen ? " failed check " + std::to_string(check)
+                                                          : " ended without its ticket"));
+                }
+            }
+            if (ended) {
+                float ms = 0;
+                if (cudaEventElapsedTime(&ms, l.start, l.end) == cudaSuccess) s->frameSeconds += 1e-3 * ms;
+                s->tickSeconds += now - l.launched;
+                l.sessions.clear();
+                l.busy = false;
+            } else {
+                anyRunning = true;
+            }
+        }
+        if (faulted) return bail(fault);
+        if (s->tickInFlight) {
+            const cudaError_t q = cudaEventQuery(s->frameDone);
+            if (q != cudaSuccess && q != cudaErrorNotReady) return bail(cudaFail(q, "serve frame"));
+            if (q == cudaSuccess) {
+                if (int rc = finishTick(s)) return bail(rc);
+                progressed = true;
+            }
+        }
+        if (int rc = st.collect(s)) return bail(rc);
+        bool launched;
+        if (int rc = launchReady(s, inKernel, running, ticketOf, launched)) return bail(rc);
+        if (!s->tickInFlight) {
+            uint32_t stepped = 0;
+            if (int rc = startTick(s, &inTicks, &stepped)) return bail(rc);
+            launched = launched || stepped > 0;
+        }
+        anyRunning = anyRunning || launched || s->tickInFlight;
+        if (anyRunning) {
+            if (!progressed && !launched) std::this_thread::yield();
+            continue;
+        }
+        if (st.closed || st.next >= st.n) break;
+        st.idle(s);
+    }
+    // The device pool's hold list follows what the jobs left held.
+    s->kernelHolds.clear();
+    return applyHolds(s);
+}
+
+}  // namespace
+
+extern "C" {
 
 int vsim_server_run(vsim_server* s, const vsim_scheduled_request* requests, uint32_t n, const vsim_drag* drags,
                     double closed_loop_seconds, vsim_completion* out, uint32_t capacity, vsim_run_report* report) {
@@ -552,65 +1051,37 @@ int vsim_server_run(vsim_server* s, const vsim_scheduled_request* requests, uint
     if (s->pending) return fail(VSIM_ERR_INVALID, "requests are already pending");
     for (uint32_t i = 0; i < n; i++)
         if (requests[i].drag && !drags) return fail(VSIM_ERR_INVALID, "a request drags but drags is NULL");
-    std::vector<vsim_completion> done;
-    const uint64_t frames0 = s->sessionFrames, ticks0 = s->ticks;
-    uint64_t requestsDone = 0;
-    uint32_t next = 0;
-    auto spec = [&](uint32_t session, const vsim_scheduled_request& q, double at) {
-        return submitAt(s, session, q.frames, q.drag ? &drags[session] : nullptr, at, nullptr);
-    };
-    const double t0 = seconds(s);
-    int rc = VSIM_OK;
-    bool windowClosed = false;
-    uint64_t windowRequests = 0, windowFrames = 0, windowTicks = 0;
-    double windowSeconds = 0;
+    DeviceGuard guard(s->sim->device);
+    RunState st{requests, n, drags, closed, closed_loop_seconds, out, capacity};
+    st.frames0 = s->sessionFrames;
+    st.ticks0 = s->ticks;
+    st.t0 = seconds(s);
     if (closed) {
-        for (uint32_t session : s->resident) {
-            if ((rc = spec(session, requests[next], seconds(s)))) return rc;
-            next = (next + 1) % n;
+        for (size_t k = 0; k < s->resident.size(); k++) {
+            if (int rc = st.submit(s, requests[st.next].session, requests[st.next], seconds(s))) return rc;
+            st.next = (st.next + 1) % n;
         }
     }
-    while (true) {
-        const double now = seconds(s);
-        if (!closed)
-            while (next < n && t0 + requests[next].arrival <= now) {
-                if ((rc = spec(requests[next].session, requests[next], t0 + requests[next].arrival))) return rc;
-                next++;
-            }
-        if (s->pending) {
-            if ((rc = vsim_server_tick(s, nullptr))) return rc;
-            const bool refill = closed && seconds(s) - t0 < closed_loop_seconds;
-            if (closed && !refill && !windowClosed) {  // the closed loop's measured span ends here
-                windowClosed = true;
-                windowRequests = requestsDone + s->completed.size();
-                windowFrames = s->sessionFrames - frames0;
-                windowTicks = s->ticks - ticks0;
-                windowSeconds = seconds(s) - t0;
-            }
-            for (const vsim_completion& c : s->completed) {
-                requestsDone++;
-                if (out && done.size() < capacity) done.push_back(c);
-                if (refill) {
-                    if ((rc = spec(c.session, requests[next], seconds(s)))) return rc;
-                    next = (next + 1) % n;
-                }
-            }
-            s->completed.clear();
-            continue;
-        }
-        if (closed || next >= n) break;
-        // Idle until the next arrival: sleep while it is far, then spin.
-        const double wait = t0 + requests[next].arrival - seconds(s);
-        if (wait > 2e-4) std::this_thread::sleep_for(std::chrono::duration<double>(wait - 1e-4));
-    }
-    if (out) std::copy(done.begin(), done.end(), out);
+    const int rc = s->engine == VSIM_SERVE_SESSIONS ? runSessions(s, st) : runFrames(s, st);
+    if (rc) return rc;
+    if (out) std::copy(st.done.begin(), st.done.end(), out);
     if (report) {
-        report->requests = closed ? windowRequests : requestsDone;
-        report->returned = uint32_t(done.size());
-        report->frames = closed ? windowFrames : s->sessionFrames - frames0;
-        report->ticks = closed ? windowTicks : s->ticks - ticks0;
-        report->seconds = closed ? windowSeconds : seconds(s) - t0;
+        report->requests = closed ? st.windowRequests : st.requestsDone;
+        report->returned = uint32_t(st.done.size());
+        report->frames = closed ? st.windowFrames : s->sessionFrames - st.frames0;
+        report->ticks = closed ? st.windowTicks : s->ticks - st.ticks0;
+        report->seconds = closed ? st.windowSeconds : seconds(s) - st.t0;
     }
+    return VSIM_OK;
+}
+
+int vsim_server_set_engine(vsim_server* s, int engine, uint32_t block_cells, uint32_t cluster_cells) {
+    clearError();
+    if (!s) return fail(VSIM_ERR_INVALID, "server is NULL");
+    if (engine != VSIM_SERVE_FRAMES && engine != VSIM_SERVE_SESSIONS) return fail(VSIM_ERR_RANGE, "unknown engine");
+    s->engine = engine;
+    s->blockCells = block_cells;
+    s->clusterCells = cluster_cells;
     return VSIM_OK;
 }
 

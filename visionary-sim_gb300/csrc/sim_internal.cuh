@@ -135,6 +135,9 @@ namespace vsim {
 
 int createSim(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void* stream, bool isolated,
               vsim_sim* s);
+// stretch.js:5-7 rest lengths, and whether any body limits its stretch.
+StretchLengths stretchLengths();
+bool anyStretch(const vsim_sim* s);
 void freeSim(vsim_sim* s);
 int runFrame(vsim_sim* s, uint32_t steps);
 int syncParams(vsim_sim* s);

@@ -190,6 +190,7 @@ SIGNATURES = {
     "vsim_server_submit": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(Drag), C.POINTER(C.c_uint64)]),
     "vsim_server_tick": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
     "vsim_server_set_tick_budget": (C.c_int, [_P, C.c_uint64]),
+    "vsim_server_set_engine": (C.c_int, [_P, C.c_int, C.c_uint32, C.c_uint32]),
     "vsim_server_run": (C.c_int, [_P, C.POINTER(ScheduledRequest), C.c_uint32, C.POINTER(Drag), C.c_double,
                                   C.POINTER(Completion), C.c_uint32, C.POINTER(RunReport)]),
     "vsim_server_poll": (C.c_int, [_P, C.POINTER(Completion), C.c_uint32, C.POINTER(C.c_uint32)]),

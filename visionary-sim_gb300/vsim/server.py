@@ -82,6 +82,16 @@ class Server:
         vsim_server_set_tick_budget."""
         check(lib().vsim_server_set_tick_budget(self._h, int(cells)))
 
+    FRAMES, SESSIONS = 0, 1
+
+    def set_engine(self, engine: int, block_cells: int = 256, cluster_cells: int = 0):
+        """How run() executes requests (vsim_server_set_engine): FRAMES,
+        ticks of shared frames; SESSIONS, a session whose largest colour has
+        at most `block_cells` cells runs each request whole in one block of
+        the session kernel, at most `cluster_cells` in one cluster, the rest
+        in ticks alongside."""
+        check(lib().vsim_server_set_engine(self._h, int(engine), int(block_cells), int(cluster_cells)))
+
     def run(self, arrivals, sessions, frames, drag_flags, drags=None, closed_loop_seconds: float = 0.0,
             keep: int | None = None):
         """The library's request loop (vsim_server_run) over a schedule:
@@ -94,7 +104,7 @@ class Server:
         reqs = (_ffi.ScheduledRequest * max(n, 1))()
         for i in range(n):
             reqs[i].arrival = float(arrivals[i]) if arrivals is not None else 0.0
-            reqs[i].session = int(sessions[i]) if sessions is not None else 0
+            reqs[i].session = int(sessions[i]) if sessions is not None else i % max(1, self.admitted)
             reqs[i].frames = int(frames[i])
             reqs[i].drag = int(bool(drag_flags[i]))
         table = None

@@ -475,6 +475,14 @@ def single_body_pass(quick: bool, hbm: float):
     out = {"workload": f"noise blob {scene.bodies[0].cell_dims[0]}^3 alone, {scene.cells} cells",
            "achieved_gbs": round(achieved, 1), "frac_of_measured_hbm": round(achieved / hbm, 4),
            "bytes_per_launch": round(per_launch), "avg_launch_us": round(per_launch_s * 1e6, 2)}
+    # The same passes in the TMA brick form (vsim_set_tma_pass), measured
+    # against the streaming form it would replace.
+    sim.set_tma_pass(True)
+    per_launch, per_launch_s = colour_pass_rate(sim)
+    sim.synchronize()
+    achieved = per_launch / per_launch_s / 1e9
+    out["tma_bricks"] = {"achieved_gbs": round(achieved, 1), "frac_of_measured_hbm": round(achieved / hbm, 4),
+                         "avg_launch_us": round(per_launch_s * 1e6, 2)}
     sim.destroy()
     return out
 
@@ -678,7 +686,7 @@ def drift(frames: int = 300):
 
 
 def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, settle_frames: int = 30,
-                  repeats_at_70: int = 3, engines=("sessions", "frames")):
+                  repeats_at_70: int = 3, engines=("sessions", "frames"), block_cells=(256,)):
     """Continuous batching under load: a pool of sessions resident on the
     GPU; requests advance a session k ~ U{1..4} frames, half of them dragging
     a random surface node along a seeded Bezier curve at 0.5 m/s. Every
@@ -803,9 +811,11 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
     by_engine = {}
     for engine in engines:
         if engine == "sessions":
-            server.set_engine(server.SESSIONS)
-            restore()
-            by_engine[engine] = {"one_request_floor": floors(engine), **sweep()}
+            for cells in block_cells:
+                server.set_engine(server.SESSIONS, cells)
+                restore()
+                key = engine if len(block_cells) == 1 else f"{engine}_block{cells}"
+                by_engine[key] = {"block_cells": cells, "one_request_floor": floors(engine), **sweep()}
         else:
             server.set_engine(server.FRAMES)
             restore()
@@ -840,11 +850,14 @@ def main():
     ap.add_argument("--no-cloud", action="store_true")
     ap.add_argument("--stress-only", action="store_true", help="only the stress workload's frames (for captures)")
     ap.add_argument("--cloud-only", action="store_true", help="only the cloud voxeliser section (for captures)")
+    ap.add_argument("--pass-only", action="store_true", help="only the single large body's colour pass, both forms")
     ap.add_argument("--tick-sweep", action="store_true", help="only the server's tick time against sessions per tick")
     ap.add_argument("--serve-only", action="store_true", help="only the serving sweep")
     ap.add_argument("--batch-only", action="store_true", help="only the batching comparison")
     ap.add_argument("--tick-budgets", default=None,
                     help="comma-separated tick cell budgets for the serving sweep (0 = no cap)")
+    ap.add_argument("--serve-block-cells", default="256",
+                    help="comma-separated block thresholds of the session engine (cells of a session's largest colour)")
     ap.add_argument("--serve-engines", default="sessions,frames",
                     help="comma-separated request-loop engines for the serving sweep (sessions, frames)")
     ap.add_argument("--capture-tick", type=int, default=None, metavar="K",
@@ -896,9 +909,13 @@ def main():
     if args.cloud_only:
         print(json.dumps({"cloud_voxelize": cloud_voxelize(args.quick)}))
         return
+    if args.pass_only:
+        print(json.dumps({"single_body_elastic_pass": single_body_pass(args.quick, peaks()[0])}))
+        return
     budgets = [int(float(v)) for v in args.tick_budgets.split(",")] if args.tick_budgets else [0]
     if args.serve_only:
-        print(json.dumps({"serving": serving_sweep(args.quick, budgets, engines=args.serve_engines.split(","))}))
+        print(json.dumps({"serving": serving_sweep(args.quick, budgets, engines=args.serve_engines.split(","),
+                                   block_cells=[int(v) for v in args.serve_block_cells.split(",")])}))
         return
     if args.batch_only:
         print(json.dumps({"batching": batched_vs_plain(10, args.quick, cpu=not args.no_cpu)}))
@@ -951,7 +968,8 @@ def main():
     if rank == 0 and not args.no_batch:
         detail["batching"] = batched_vs_plain(10, args.quick, cpu=not args.no_cpu)
     if rank == 0 and not args.no_serve:
-        detail["serving"] = serving_sweep(args.quick, budgets, engines=args.serve_engines.split(","))
+        detail["serving"] = serving_sweep(args.quick, budgets, engines=args.serve_engines.split(","),
+                                   block_cells=[int(v) for v in args.serve_block_cells.split(",")])
     if rank == 0 and not args.no_stress:
         detail["stress"] = stress(args.quick, hbm)
     if rank == 0 and not args.no_cloud:

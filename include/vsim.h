@@ -265,6 +265,15 @@ int vsim_set_graph(vsim_sim* sim, int enabled);
    cell order inside each colour (0: lattice order, 4 or 8: bricks of that
    many cells per axis). Chosen by vsim_tune; settable for sweeps. */
 int vsim_set_launch_shape(vsim_sim* sim, uint32_t block, uint32_t brick);
+/* The large colour passes (a dense pass of at least two cells per resident
+   thread) through tensor-memory-accelerator brick tiles: each block takes
+   bricks of 8 x 4 x 4 same-colour cells, loads their 16 x 8 x 8 node boxes
+   of positions and previous positions with bulk tensor copies, solves in
+   shared memory and stores the position box back. Results equal the other
+   forms bit for bit. For scenes of 1 to 4 bodies (else VSIM_ERR_RANGE); off
+   by default. A block whose copies never arrive (bounded wait) makes the
+   next vsim_synchronize fail. */
+int vsim_set_tma_pass(vsim_sim* sim, int enabled);
 /* Time every {brick 0,4,8} x {block 128,256,512} shape on `frames` frames of
    the live state (which is saved and restored) and keep the fastest.
    Writes the chosen shape to *block and *brick when non-NULL. */

@@ -117,6 +117,41 @@ def test_large_colour_passes_stream_bit_exact(lib):
     assert_same(sim, orc, scene, "streamed frame")
 
 
+def test_tma_colour_pass_bit_exact(lib):
+    """The TMA brick form of the large colour passes (vsim_set_tma_pass)
+    leaves every node where the streaming form leaves it: a dense box whose
+    cell grid is no multiple of a brick (boxes reaching past the node grid)
+    and a noise blob (bricks partly empty), one frame with ground and self
+    contact each, synchronised with the fault word checked. More than four
+    bodies are refused."""
+    import vsim.scenes as sc
+    from vsim import _ffi
+    from vsim.simulator import Simulator
+
+    mat = dict(sc.DEFAULT_MATERIAL, youngs_modulus=2e5, poisson_ratio=0.45, density=1000.0)
+    nx, ny, nz = 130, 90, 135  # 1,579,500 cells
+    box = sc.Body((nx, ny, nz), (0.0, 2 * sc.H, 0.0), sc.H, np.ones(nx * ny * nz, np.uint8), mat)
+    ext = (nx * sc.H, (ny + 4) * sc.H, nz * sc.H)
+    dense = sc.Scene([box], ((-0.1, 0.0, -0.1), (ext[0] + 0.1, ext[1] + 0.1, ext[2] + 0.1)),
+                     step_duration=1 / 600, substeps=10)
+    blob = sc.noise_blob(n=160, seed=4, splats=0)
+    for name, scene in (("dense box", dense), ("noise blob", blob)):
+        plain, tiled = Simulator(scene), Simulator(scene)
+        tiled.set_tma_pass(True)
+        assert min(tiled.color_counts()) >= 155_648, name
+        for sim in (plain, tiled):
+            sim.dispatch(scene.substeps)
+            sim.synchronize()
+        for a, b, what in zip(plain.read_state(), tiled.read_state(), ("pos", "prev", "vel")):
+            assert np.array_equal(a, b), f"{name}: {what}"
+        plain.destroy()
+        tiled.destroy()
+    many = Simulator(sc.box_batch(5))
+    with pytest.raises(_ffi.VsimError):
+        many.set_tma_pass(True)
+    many.destroy()
+
+
 @pytest.mark.parametrize("mapping", ["warp", "thread"])
 def test_gather_mappings_agree(lib, mapping):
     """Both record-to-thread mappings of the contact gather give the oracle's

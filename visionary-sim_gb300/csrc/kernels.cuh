@@ -203,6 +203,22 @@ cudaError_t launchRefreshW(cudaStream_t st, uint32_t first, uint32_t n, const fl
 cudaError_t launchMergeXyz(cudaStream_t st, const float4* in, uint32_t n, float4* pos);
 cudaError_t launchDropW(cudaStream_t st, const float4* in, uint32_t n, float4* out);
 
+// ---- TMA brick colour pass (colour_tma.cu) -----------------------------------
+
+constexpr uint32_t kTmaBodies = 4;   // bodies whose node arrays get tensor maps
+constexpr uint32_t kTmaBlock = 128;  // threads: one per cell of an 8 x 4 x 4 brick
+
+// The pass's tables: per colour, the bricks holding its cells (two uint4
+// each: body and brick coordinates, then 128 occupancy bits).
+struct TmaPass {
+    bool ready = false;    // built for the simulator's current arrays
+    bool enabled = false;  // large dense passes use it (vsim_set_tma_pass)
+    void* maps = nullptr;  // host: the bodies' position and previous-position tensor maps
+    uint4* bricks = nullptr;
+    uint32_t first[8] = {}, count[8] = {};
+    uint32_t* fault = nullptr;  // set by a block whose copies did not arrive
+};
+
 // ---- session kernel (session.cu) -------------------------------------------
 
 // One request of an isolated session: its body's ranges and the frames to

@@ -770,8 +770,12 @@ int buildEngine(vsim_server* s) {
     if (!e->doneDev || !e->statusDev) return fail(VSIM_ERR_CUDA, "map tickets");
     CK(cudaMalloc(reinterpret_cast<void**>(&e->cursor), bodies * 4), "allocate segment cursors");
     CK(cudaMalloc(reinterpret_cast<void**>(&e->fault), bodies * 4), "allocate job checks");
+    // Session launches yield to the ticks' frames: each of those is a chain
+    // of short dependent launches whose blocks should get SMs first.
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest), "query stream priorities");
     for (LaunchSlot& l : e->slot) {
-        CK(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking), "create launch stream");
+        CK(cudaStreamCreateWithPriority(&l.stream, cudaStreamNonBlocking, least), "create launch stream");
         CK(cudaEventCreate(&l.start), "create launch event");
         CK(cudaEventCreate(&l.end), "create launch event");
     }

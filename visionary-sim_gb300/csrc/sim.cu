@@ -260,6 +260,16 @@ struct Profiler {
 
 constexpr uint32_t kContactKernels = 5;  // bin, segment, scatter, order, collide
 
+// One colour pass: the TMA brick form for a large dense pass when it is on,
+// else launchElastic's choice.
+cudaError_t launchColourPass(const LaunchCtx& c, const vsim_sim* s, int col, bool limitOnly,
+                             const StretchLengths& lens) {
+    const Span& sp = s->plan.colour[col];
+    if (!limitOnly && s->tma.enabled && s->tma.ready && !sp.work.table && streamsColourPass(sp.work.count, c.sms))
+        return launchElasticTma(c, s, col, lens);
+    return launchElastic(c, s->d, s->d.cells + s->colorStart[col], sp, limitOnly, lens);
+}
+
 // stepper.js:101-108 with simulator.js:83's constraint order.
 cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMode mode = ContactMode::Solve,
                         Profiler* prof = nullptr) {
@@ -290,8 +300,7 @@ cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMod
             for (int col = 0; col < 8; col++) {
                 if (!plan.colour[col].grid) continue;
                 begin(VSIM_KIND_ELASTIC, 1);
-                if ((e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], plan.colour[col], false, lens)))
-                    return e;
+                if ((e = launchColourPass(c, s, col, false, lens))) return e;
                 end();
             }
         if (limited)
@@ -299,8 +308,7 @@ cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMod
                 for (int col = 0; col < 8; col++) {
                     if (!plan.colour[col].grid) continue;
                     begin(VSIM_KIND_LIMIT, 1);
-                    if ((e = launchElastic(c, s->d, s->d.cells + s->colorStart[col], plan.colour[col], true, lens)))
-                        return e;
+                    if ((e = launchColourPass(c, s, col, true, lens))) return e;
                     end();
                 }
         if (contact && plan.records.grid) {
@@ -327,6 +335,7 @@ uint64_t graphKey(const vsim_sim* s, uint32_t steps) {
     k = k * 31 + (s->pdl ? 1 : 0);
     k = k * 31 + (s->plan.chunked ? 1 : 0);
     k = k * 31 + uint64_t(s->gatherMapping);
+    k = k * 31 + (s->tma.enabled ? 1 : 0);
     return k;
 }
 
@@ -397,6 +406,7 @@ void freeSim(vsim_sim* s) {
                     s->sp.sortTemp};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    freeTmaPass(s->tma);
     void* pinned[] = {s->chunkPinned, s->activePinned, s->grabsPinned};
     for (void* p : pinned)
         if (p) cudaFreeHost(p);
@@ -700,6 +710,21 @@ int vsim_destroy(vsim_sim* sim) {
 int vsim_synchronize(vsim_sim* s) {
     SIM_GUARD(s);
     CK(cudaStreamSynchronize(s->stream), "synchronize");
+    if (s->tma.fault) {
+        uint32_t fault = 0;
+        CK(cudaMemcpy(&fault, s->tma.fault, 4, cudaMemcpyDeviceToHost), "synchronize");
+        if (fault) return fail(VSIM_ERR_CUDA, "TMA colour pass: a block's copies did not arrive");
+    }
+    return VSIM_OK;
+}
+
+int vsim_set_tma_pass(vsim_sim* s, int enabled) {
+    SIM_GUARD(s);
+    if (enabled && !s->tma.ready) {
+        if (int rc = buildTmaPass(s)) return rc;
+        if (!s->tma.ready) return fail(VSIM_ERR_RANGE, "the TMA colour pass takes 1 to 4 bodies");
+    }
+    s->tma.enabled = enabled != 0;
     return VSIM_OK;
 }
 
@@ -1258,8 +1283,7 @@ int vsim_time_colour_passes(vsim_sim* s, uint32_t sweeps, float* ms) {
         cudaError_t enc = cudaSuccess;
         for (uint32_t sweep = 0; sweep < sweeps && enc == cudaSuccess; sweep++)
             for (int col = 0; col < 8 && enc == cudaSuccess; col++)
-                if (s->plan.colour[col].grid)
-                    enc = launchElastic(c, s->d, s->d.cells + s->colorStart[col], s->plan.colour[col], false, lens);
+                if (s->plan.colour[col].grid) enc = launchColourPass(c, s, col, false, lens);
         const cudaError_t end = cudaStreamEndCapture(s->capture, &graph);
         if (enc) return enc;
         if (end) return end;

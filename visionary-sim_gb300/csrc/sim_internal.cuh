@@ -129,12 +129,19 @@ struct vsim_sim {
     size_t chunkCapacity = 0;      // chunks, not counting the descriptors
     uint32_t* activePinned = nullptr;  // host staging of the activity and drive tables
     float4* grabsPinned = nullptr;
+    vsim::TmaPass tma;
 };
 
 namespace vsim {
 
 int createSim(const vsim_body_desc* bodies, uint32_t n, const vsim_tank* tank, void* stream, bool isolated,
               vsim_sim* s);
+// The TMA brick colour pass (colour_tma.cu): tables built for the
+// simulator's bodies (up to kTmaBodies; with more it stays unbuilt), freed,
+// and one pass launched.
+int buildTmaPass(vsim_sim* s);
+void freeTmaPass(TmaPass& t);
+cudaError_t launchElasticTma(const LaunchCtx& c, const vsim_sim* s, int colour, const StretchLengths& lens);
 // stretch.js:5-7 rest lengths, and whether any body limits its stretch.
 StretchLengths stretchLengths();
 bool anyStretch(const vsim_sim* s);

@@ -229,6 +229,7 @@ SIGNATURES = {
     "vsim_tune": (C.c_int, [_P, C.c_uint32, _U, _U]),
     "vsim_set_pdl": (C.c_int, [_P, C.c_int]),
     "vsim_set_gather_mapping": (C.c_int, [_P, C.c_int]),
+    "vsim_set_tma_pass": (C.c_int, [_P, C.c_int]),
     "vsim_grab": (C.c_int, [_P, _D, _D, C.c_int, C.c_double, C.POINTER(GrabResult)]),
     "vsim_time_colour_passes": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_float)]),
     "vsim_kuhn_rest_inverse": (C.c_int, [_F]),

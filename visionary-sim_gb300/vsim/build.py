@@ -25,7 +25,7 @@ NVCC_FLAGS = [
     "-O3", "-std=c++17", "-lineinfo", "-fmad=false", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", f"-I{INCLUDE}",
 ]
-SOURCES = ["host.cpp", "sim.cu", "server.cu", "step_kernels.cu", "session.cu", "splat_sort.cu", "grab.cu",
+SOURCES = ["host.cpp", "sim.cu", "server.cu", "step_kernels.cu", "colour_tma.cu", "session.cu", "splat_sort.cu", "grab.cu",
            "cloud_volume.cu"]
 
 

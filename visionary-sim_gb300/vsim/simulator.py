@@ -285,6 +285,10 @@ class Simulator:
     def set_launch_shape(self, block: int, brick: int):
         check(lib().vsim_set_launch_shape(self._h, int(block), int(brick)))
 
+    def set_tma_pass(self, enabled: bool):
+        """Large colour passes through TMA brick tiles (vsim_set_tma_pass)."""
+        check(lib().vsim_set_tma_pass(self._h, int(bool(enabled))))
+
     def tune(self, frames: int = 3):
         block, brick = C.c_uint32(), C.c_uint32()
         check(lib().vsim_tune(self._h, int(frames), C.byref(block), C.byref(brick)))

@@ -601,6 +601,37 @@ def cloud_voxelize(quick: bool, reps: int = 5):
             "grid_equal_to_host": host.dims == dims and bool(np.array_equal(host.occupancy, occupancy.numpy()))}
 
 
+def capture_sessions(settle_frames: int = 30):
+    """Profiler capture of one session-kernel launch: the 64-session pool
+    (every session settled for `settle_frames` frames), then one request of
+    one frame for each session small enough for a block, run through the
+    request loop with only that launch between cudaProfilerStart/Stop, for
+    `ncu --profile-from-start off -k regex:sessionKernel`."""
+    import torch
+
+    import vsim.scenes as sc
+    from vsim.server import Server
+
+    bodies, tank = sc.session_pool(64, seed=3)
+    server = Server(bodies, tank, budget_bytes=150e9)
+    n = server.admitted
+    for q in range(n):
+        server.submit(q, settle_frames)
+    while server.stats()["pending"]:
+        server.tick()
+        server.poll()
+    small = [q for q in range(n) if bodies[q].cell_count <= 1500]
+    ones = np.ones(len(small), np.int64)
+    server.run(np.zeros(len(small)), np.array(small), ones, np.zeros(len(small), np.int64))  # warm
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    done, _ = server.run(np.zeros(len(small)), np.array(small), ones, np.zeros(len(small), np.int64))
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    server.destroy()
+    return {"captured_session_requests": len(small), "cells": int(sum(bodies[q].cell_count for q in small))}
+
+
 def tick_sweep(quick: bool, capture: int | None = None, reps: int = 25, settle_frames: int = 30):
     """Tick time of the session server against the number of sessions a tick
     runs: the 1000-session pool of the serving workload (64 with --quick),
@@ -860,6 +891,8 @@ def main():
                     help="comma-separated block thresholds of the session engine (cells of a session's largest colour)")
     ap.add_argument("--serve-engines", default="sessions,frames",
                     help="comma-separated request-loop engines for the serving sweep (sessions, frames)")
+    ap.add_argument("--capture-sessions", action="store_true",
+                    help="profiler capture mode: one session-kernel launch over the 64-session pool's small sessions")
     ap.add_argument("--capture-tick", type=int, default=None, metavar="K",
                     help="profiler capture mode: one server tick of K sessions, for `ncu --profile-from-start off`")
     ap.add_argument("--capture-after", type=int, default=None, metavar="N",
@@ -919,6 +952,9 @@ def main():
         return
     if args.batch_only:
         print(json.dumps({"batching": batched_vs_plain(10, args.quick, cpu=not args.no_cpu)}))
+        return
+    if args.capture_sessions:
+        print(json.dumps({"capture_sessions": capture_sessions()}))
         return
     if args.tick_sweep or args.capture_tick is not None:
         print(json.dumps({"tick_sweep": tick_sweep(args.quick, args.capture_tick)}))

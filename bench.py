@@ -717,7 +717,7 @@ def drift(frames: int = 300):
 
 
 def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, settle_frames: int = 30,
-                  repeats_at_70: int = 3, engines=("sessions", "frames"), block_cells=(256,)):
+                  repeats_at_70: int = 3, engines=("sessions", "frames"), block_cells=(32,)):
     """Continuous batching under load: a pool of sessions resident on the
     GPU; requests advance a session k ~ U{1..4} frames, half of them dragging
     a random surface node along a seeded Bezier curve at 0.5 m/s. Every
@@ -827,11 +827,13 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
 
     def floors(engine):
         """One 1-frame request alone on the idle server, for the smallest,
-        median and largest resident session: median of 15 (completion -
-        arrival), the latency with no queueing at all."""
+        median and largest resident session and the sessions at the 10th to
+        40th percentiles of size: median of 15 (completion - arrival), the
+        latency with no queueing at all."""
         order = sorted(range(admitted), key=lambda q: bodies[q].cell_count)
         out = {}
-        for label, q in (("smallest", order[0]), ("median", order[len(order) // 2]), ("largest", order[-1])):
+        picks = [("smallest", order[0])] + [(f"p{k}", order[len(order) * k // 100]) for k in (10, 20, 30, 40)]
+        for label, q in picks + [("median", order[len(order) // 2]), ("largest", order[-1])]:
             lat = []
             for _ in range(15):
                 done, _ = server.run(np.zeros(1), np.array([q]), np.ones(1, np.int64), np.zeros(1, np.int64))
@@ -887,7 +889,7 @@ def main():
     ap.add_argument("--batch-only", action="store_true", help="only the batching comparison")
     ap.add_argument("--tick-budgets", default=None,
                     help="comma-separated tick cell budgets for the serving sweep (0 = no cap)")
-    ap.add_argument("--serve-block-cells", default="256",
+    ap.add_argument("--serve-block-cells", default="32",
                     help="comma-separated block thresholds of the session engine (cells of a session's largest colour)")
     ap.add_argument("--serve-engines", default="sessions,frames",
                     help="comma-separated request-loop engines for the serving sweep (sessions, frames)")

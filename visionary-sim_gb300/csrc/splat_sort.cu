@@ -297,15 +297,11 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
 // One pass: rank a tile, find its digits' global offsets by decoupled
 // look-back, scatter. `status` is this pass's (tile, digit) words, `totals`
 // its 256 digit counts over all keys.
-__global__ void __launch_bounds__(kSortThreads) sortPassKernel(const uint32_t* __restrict__ keysIn,
-                                                               const uint32_t* __restrict__ valsIn, uint32_t n,
-                                                               uint32_t shift, uint32_t mask,
-                                                               const uint32_t* __restrict__ totals,
-                                                               uint32_t* __restrict__ status,
-                                                               uint32_t* __restrict__ ticket,
-                                                               uint32_t* __restrict__ error,
-                                                               uint32_t* __restrict__ keysOut,
-                                                               uint32_t* __restrict__ valsOut) {
+__device__ __forceinline__ void sortPass(const uint32_t* __restrict__ keysIn, const uint32_t* __restrict__ valsIn,
+                                         uint32_t n, uint32_t shift, uint32_t mask,
+                                         const uint32_t* __restrict__ totals, uint32_t* __restrict__ status,
+                                         uint32_t* __restrict__ ticket, uint32_t* __restrict__ error,
+                                         uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut) {
     __shared__ uint32_t sKeys[kSortTile];
     __shared__ uint32_t sVals[kSortTile];
     __shared__ uint32_t warpHist[kWarps][256];
@@ -400,6 +396,35 @@ __global__ void __launch_bounds__(kSortThreads) sortPassKernel(const uint32_t* _
     }
 }
 
+// The pass as two kernels: sortPassKernel at the registers the compiler
+// picks (86: two blocks an SM), sortPassWideKernel squeezed to 80 so that
+// three fit. The second is faster once the tiles take several waves (20M
+// keys: 27.4 against 23.6 G keys/s), slower within one wave, where each
+// tile's latency is the pass (1M keys: 0.096 against 0.080 ms a sort).
+__global__ void __launch_bounds__(kSortThreads) sortPassKernel(const uint32_t* __restrict__ keysIn,
+                                                               const uint32_t* __restrict__ valsIn, uint32_t n,
+                                                               uint32_t shift, uint32_t mask,
+                                                               const uint32_t* __restrict__ totals,
+                                                               uint32_t* __restrict__ status,
+                                                               uint32_t* __restrict__ ticket,
+                                                               uint32_t* __restrict__ error,
+                                                               uint32_t* __restrict__ keysOut,
+                                                               uint32_t* __restrict__ valsOut) {
+    sortPass(keysIn, valsIn, n, shift, mask, totals, status, ticket, error, keysOut, valsOut);
+}
+
+__global__ void __launch_bounds__(kSortThreads, 3) sortPassWideKernel(const uint32_t* __restrict__ keysIn,
+                                                                      const uint32_t* __restrict__ valsIn,
+                                                                      uint32_t n, uint32_t shift, uint32_t mask,
+                                                                      const uint32_t* __restrict__ totals,
+                                                                      uint32_t* __restrict__ status,
+                                                                      uint32_t* __restrict__ ticket,
+                                                                      uint32_t* __restrict__ error,
+                                                                      uint32_t* __restrict__ keysOut,
+                                                                      uint32_t* __restrict__ valsOut) {
+    sortPass(keysIn, valsIn, n, shift, mask, totals, status, ticket, error, keysOut, valsOut);
+}
+
 namespace {
 // A sort kernel launched with programmatic dependent launch: its blocks may
 // start while the kernel before finishes, and wait (pdlWait) before reading.
@@ -445,16 +470,18 @@ cudaError_t radixSortU32(const uint32_t* keys, uint32_t* order, uint32_t n, uint
     if ((e = pdl(sortDigitCountKernel, countGrid, st, keys, n, keyBits, totals))) return e;
     const uint32_t* kin = keys;
     const uint32_t* vin = nullptr;
-    for (uint32_t pass = 0; pass < passes; pass++) {
-        const uint32_t shift = 8 * pass;
+    for (uint32_t pass_ = 0; pass_ < passes; pass_++) {
+        const uint32_t shift = 8 * pass_;
         const uint32_t bits = keyBits - shift < 8 ? keyBits - shift : 8;
         const uint32_t mask = (1u << bits) - 1u;
-        const bool last = pass + 1 == passes;
-        uint32_t* kout = last ? nullptr : (pass % 2 == 0 ? keysA : keysB);
-        uint32_t* vout = last ? order : (pass % 2 == 0 ? valsA : valsB);
-        if ((e = pdl(sortPassKernel, tiles, st, kin, vin, n, shift, mask, (const uint32_t*)(totals + 256 * pass),
-                     status + size_t(pass) * tiles * 256, tickets + pass, error, kout, vout)))
-            return e;
+        const bool last = pass_ + 1 == passes;
+        uint32_t* kout = last ? nullptr : (pass_ % 2 == 0 ? keysA : keysB);
+        uint32_t* vout = last ? order : (pass_ % 2 == 0 ? valsA : valsB);
+        auto pass = [&](auto kernel) {
+            return pdl(kernel, tiles, st, kin, vin, n, shift, mask, (const uint32_t*)(totals + 256 * pass_),
+                       status + size_t(pass_) * tiles * 256, tickets + pass_, error, kout, vout);
+        };
+        if ((e = tiles > 2u * uint32_t(sms) ? pass(sortPassWideKernel) : pass(sortPassKernel))) return e;
         kin = kout;
         vin = vout;
     }

@@ -87,9 +87,11 @@ __global__ void __launch_bounds__(256) splatDeformKernel(const float4* __restric
     if (i >= n) return;
     // The splat's embedding, scale and rotation do not change between
     // frames: loaded before waiting for the frame that moves the nodes.
-    const float4 e = embed[i];
-    const float4 sb = scaleBody[i];
-    const float4 q4 = quat[i];
+    // The splat streams are read and written once, marked evict-first
+    // (.cs), so that the node positions the corner gathers hit stay in L2.
+    const float4 e = __ldcs(embed + i);
+    const float4 sb = __ldcs(scaleBody + i);
+    const float4 q4 = __ldcs(quat + i);
     const SplatBody B = bodies[__float_as_uint(sb.w)];
     pdlWait();
     pdlLaunchNext();
@@ -129,10 +131,10 @@ __global__ void __launch_bounds__(256) splatDeformKernel(const float4* __restric
     const float yz = fmaf(a2.z, a2.y, fmaf(a1.z, a1.y, a0.z * a0.y));
     const float zz = fmaf(a2.z, a2.z, fmaf(a1.z, a1.z, a0.z * a0.z));
     const float depth = position.x * vx + position.y * vy + position.z * vz;
-    meanDepth[i] = make_float4(position.x, position.y, position.z, depth);
-    cov[3 * i] = make_float2(xx, xy);
-    cov[3 * i + 1] = make_float2(xz, yy);
-    cov[3 * i + 2] = make_float2(yz, zz);
+    __stcs(meanDepth + i, make_float4(position.x, position.y, position.z, depth));
+    __stcs(cov + 3 * i, make_float2(xx, xy));
+    __stcs(cov + 3 * i + 1, make_float2(xz, yy));
+    __stcs(cov + 3 * i + 2, make_float2(yz, zz));
     keys[i] = depthKey(depth);
     (void)order;
     if (AXES) {

@@ -222,7 +222,7 @@ struct TmaPass {
 // ---- session kernel (session.cu) -------------------------------------------
 
 // One request of an isolated session: its body's ranges and the frames to
-// run. Read by the kernel from host-mapped memory.
+// run.
 struct SessionJob {
     uint32_t nodeFirst, nodeCount;  // its range of the active-node list
     uint32_t recFirst, recCount;    // its range of the surface records

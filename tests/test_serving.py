@@ -260,6 +260,36 @@ def test_engines_give_the_same_result(lib, engine, block_cells, cluster_cells):
         srv.destroy()
 
 
+def test_session_kernel_stretch_limit_and_engine_checks(lib):
+    """Sessions whose material limits stretch (maxStretch > 1: three limit-only
+    sweeps of the eight colours every substep) leave the session kernel --
+    in one block and on a cluster -- where the ticks leave them; unknown
+    engines are refused."""
+    import dataclasses
+
+    import vsim.scenes as sc
+    from vsim import _ffi
+    from vsim.server import Server
+
+    bodies, tank = small_pool(5, seed=43)
+    bodies = [dataclasses.replace(b, material=dict(b.material, max_stretch=1.05)) for b in bodies]
+    rng = np.random.default_rng(12)
+    drags = [sc.drag_request(b, rng) for b in bodies]
+    requests = [(q, 3, drags[q] if q % 2 else None) for q in range(5)]
+    by_hand, _ = serve(bodies, tank, requests)
+    for block, cluster in ((1 << 30, 0), (0, 1 << 30)):
+        server = Server(bodies, tank)
+        server.set_engine(server.SESSIONS, block, cluster)
+        server.run(np.zeros(5), np.arange(5), np.full(5, 3), np.array([q % 2 for q in range(5)]), drags)
+        for q in range(5):
+            for a, b in zip(server.read_state(q), by_hand.read_state(q)):
+                assert np.array_equal(a, b), f"block {block} cluster {cluster} session {q}"
+        with pytest.raises(_ffi.VsimError):
+            server.set_engine(7)
+        server.destroy()
+    by_hand.destroy()
+
+
 def test_served_session_matches_oracle(lib):
     import pyoracle
     import vsim.scenes as sc

@@ -717,7 +717,7 @@ def drift(frames: int = 300):
 
 
 def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, settle_frames: int = 30,
-                  repeats_at_70: int = 3, engines=("sessions", "frames"), block_cells=(32,)):
+                  repeats_at_70: int = 3, engines=("sessions", "frames"), block_cells=(32,), cluster_cells=(512,)):
     """Continuous batching under load: a pool of sessions resident on the
     GPU; requests advance a session k ~ U{1..4} frames, half of them dragging
     a random surface node along a seeded Bezier curve at 0.5 m/s. Every
@@ -844,11 +844,13 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
     by_engine = {}
     for engine in engines:
         if engine == "sessions":
-            for cells in block_cells:
-                server.set_engine(server.SESSIONS, cells)
+            shapes = [(b, c) for b in block_cells for c in cluster_cells]
+            for cells, wide in shapes:
+                server.set_engine(server.SESSIONS, cells, wide)
                 restore()
-                key = engine if len(block_cells) == 1 else f"{engine}_block{cells}"
-                by_engine[key] = {"block_cells": cells, "one_request_floor": floors(engine), **sweep()}
+                key = engine if len(shapes) == 1 else f"{engine}_block{cells}_cluster{wide}"
+                by_engine[key] = {"block_cells": cells, "cluster_cells": wide, "one_request_floor": floors(engine),
+                                  **sweep()}
         else:
             server.set_engine(server.FRAMES)
             restore()
@@ -891,6 +893,8 @@ def main():
                     help="comma-separated tick cell budgets for the serving sweep (0 = no cap)")
     ap.add_argument("--serve-block-cells", default="32",
                     help="comma-separated block thresholds of the session engine (cells of a session's largest colour)")
+    ap.add_argument("--serve-cluster-cells", default="512",
+                    help="comma-separated cluster thresholds of the session engine (0: no cluster jobs)")
     ap.add_argument("--serve-engines", default="sessions,frames",
                     help="comma-separated request-loop engines for the serving sweep (sessions, frames)")
     ap.add_argument("--capture-sessions", action="store_true",
@@ -950,7 +954,8 @@ def main():
     budgets = [int(float(v)) for v in args.tick_budgets.split(",")] if args.tick_budgets else [0]
     if args.serve_only:
         print(json.dumps({"serving": serving_sweep(args.quick, budgets, engines=args.serve_engines.split(","),
-                                   block_cells=[int(v) for v in args.serve_block_cells.split(",")])}))
+                                   block_cells=[int(v) for v in args.serve_block_cells.split(",")],
+                                   cluster_cells=[int(v) for v in args.serve_cluster_cells.split(",")])}))
         return
     if args.batch_only:
         print(json.dumps({"batching": batched_vs_plain(10, args.quick, cpu=not args.no_cpu)}))
@@ -1007,7 +1012,8 @@ def main():
         detail["batching"] = batched_vs_plain(10, args.quick, cpu=not args.no_cpu)
     if rank == 0 and not args.no_serve:
         detail["serving"] = serving_sweep(args.quick, budgets, engines=args.serve_engines.split(","),
-                                   block_cells=[int(v) for v in args.serve_block_cells.split(",")])
+                                   block_cells=[int(v) for v in args.serve_block_cells.split(",")],
+                                   cluster_cells=[int(v) for v in args.serve_cluster_cells.split(",")])
     if rank == 0 and not args.no_stress:
         detail["stress"] = stress(args.quick, hbm)
     if rank == 0 and not args.no_cloud:

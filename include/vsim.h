@@ -567,9 +567,9 @@ int vsim_server_run(vsim_server* server, const vsim_scheduled_request* requests,
 /* Engines of vsim_server_run. FRAMES: ticks, one frame at a time for every
    session with a request, as vsim_server_tick runs them. SESSIONS (the
    default): a session whose largest colour has at most `block_cells` cells
-   (32 is the server's default) runs each request whole -- all its frames -- in one block
-   of the session kernel, else, with at most `cluster_cells`, in one
-   cluster of 8 blocks (default 0: none); every such session that has a
+   (32 is the server's default) runs each request whole -- all its frames --
+   in one block of the session kernel, else, with at most `cluster_cells`
+   (default 512), in one cluster of 8 blocks; every such session that has a
    request and none running starts in the next launch, launches overlap,
    and a request completes when its own job ends. Larger sessions run in
    ticks of shared frames on the server's stream at the same time. Every

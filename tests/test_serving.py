@@ -212,7 +212,7 @@ def test_native_request_loop(lib):
 
 
 @pytest.mark.parametrize("engine,block_cells,cluster_cells",
-                         [(0, 0, 0), (1, 32, 0), (1, 1 << 30, 0), (1, 0, 1 << 30), (1, 60, 120)],
+                         [(0, 0, 0), (1, 32, 512), (1, 1 << 30, 0), (1, 0, 1 << 30), (1, 60, 120)],
                          ids=["frames", "sessions-default", "sessions-all-block", "sessions-all-cluster",
                               "sessions-block-cluster-ticks"])
 def test_engines_give_the_same_result(lib, engine, block_cells, cluster_cells):

@@ -242,9 +242,12 @@ constexpr uint32_t kSessionBlock = 256;   // threads of a block
 constexpr uint32_t kNoJob = 0xffffffffu;
 // Largest colour (cells) of a session the serving engine runs in one block
 // by default: above it a session's substep -- mostly its contact gather,
-// ~10^5 warp instructions once it has settled -- issues faster as the
-// per-pass graph's launches over all SMs than on one SM.
+// ~10^5 warp instructions once it has settled -- issues faster on more
+// SMs. Up to kDefaultClusterCells it runs on a cluster of eight blocks,
+// which costs about the SM time of a tick but no tick's wait; larger
+// sessions run as ticks, whose launches spread them over every SM.
 constexpr uint32_t kDefaultBlockCells = 32;
+constexpr uint32_t kDefaultClusterCells = 512;
 
 // Checks a job can fail (SessionLaunch::fault, ::status). A failed job
 // skips the rest of its work; the host reports it as an error.

@@ -139,7 +139,7 @@ struct vsim_server {
     // Session engine: a session whose largest colour has at most blockCells
     // cells runs in one block, else at most clusterCells in one cluster,
     // else in ticks of shared frames.
-    uint32_t blockCells = kDefaultBlockCells, clusterCells = 0;
+    uint32_t blockCells = kDefaultBlockCells, clusterCells = kDefaultClusterCells;
     SessionEngine* sessionEngine = nullptr;  // built on first use for the current pool
     std::vector<uint8_t> kernelHolds;  // per session, during a run: its drag holds are the session kernel's
     // The tick in flight (startTick .. finishTick).

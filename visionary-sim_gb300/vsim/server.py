@@ -84,7 +84,7 @@ class Server:
 
     FRAMES, SESSIONS = 0, 1
 
-    def set_engine(self, engine: int, block_cells: int = 32, cluster_cells: int = 0):
+    def set_engine(self, engine: int, block_cells: int = 32, cluster_cells: int = 512):
         """How run() executes requests (vsim_server_set_engine): FRAMES,
         ticks of shared frames; SESSIONS, a session whose largest colour has
         at most `block_cells` cells runs each request whole in one block of

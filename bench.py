@@ -193,6 +193,10 @@ def roofline(sim, scene, hbm):
     ms, launches = prof["elastic"]
     per_launch_bytes, per_launch_s = colour_pass_rate(sim)
     achieved = per_launch_bytes / per_launch_s / 1e9
+    # The same passes with each cell split over four lanes (vsim_set_cell_lanes).
+    sim.set_cell_lanes(4)
+    _, quad_s = colour_pass_rate(sim)
+    sim.set_cell_lanes(1)
     traffic = profiled_traffic()
     share = {k: round(v[0] / sum(x[0] for x in prof.values()), 4) for k, v in prof.items()}
     return {
@@ -208,6 +212,7 @@ def roofline(sim, scene, hbm):
         "isolated_launch_us": round(1e3 * ms / (scene.substeps * scene.iterations *
                                                  int(np.count_nonzero(sim.color_counts()))), 3),
         "method": "10 sweeps x 8 colour passes back to back in one graph, CUDA events at its ends",
+        "four_lanes_a_cell_launch_us": round(quad_s * 1e6, 3),
     }, {k: {"ms": round(v[0], 4), "launches": v[1]} for k, v in prof.items()}, share
 
 

@@ -274,6 +274,12 @@ int vsim_set_launch_shape(vsim_sim* sim, uint32_t block, uint32_t brick);
    by default. A block whose copies never arrive (bounded wait) makes the
    next vsim_synchronize fail. */
 int vsim_set_tma_pass(vsim_sim* sim, int enabled);
+/* The small colour passes (under two cells per resident thread, dense) with
+   each cell split over four lanes: every lane runs the tetrahedra's serial
+   spine, lane q its corner's products and update, exchanged by shuffles.
+   Results equal the one-lane form bit for bit. `lanes` 1 (default) or 4
+   (else VSIM_ERR_RANGE). */
+int vsim_set_cell_lanes(vsim_sim* sim, uint32_t lanes);
 /* Time every {brick 0,4,8} x {block 128,256,512} shape on `frames` frames of
    the live state (which is saved and restored) and keep the fastest.
    Writes the chosen shape to *block and *brick when non-NULL. */

@@ -117,6 +117,29 @@ def test_large_colour_passes_stream_bit_exact(lib):
     assert_same(sim, orc, scene, "streamed frame")
 
 
+def test_cell_split_over_four_lanes_bit_exact(lib):
+    """The small colour passes with each cell split over four lanes
+    (vsim_set_cell_lanes) equal the oracle frame by frame: a noise blob with
+    ground and self contact, and the pinned bar with a stretch limit."""
+    import vsim.scenes as sc
+
+    blob = sc.noise_blob(n=16, seed=5, splats=0)
+    sim, orc = make(blob)
+    sim.set_cell_lanes(4)
+    for frame in range(6):
+        sim.dispatch(blob.substeps)
+        orc.dispatch(blob.substeps)
+        assert_same(sim, orc, blob, f"blob frame {frame}")
+    bar = sc.single_box()
+    bar.bodies[0].material["max_stretch"] = 1.05
+    sim, orc = make(bar)
+    sim.set_cell_lanes(4)
+    for frame in range(4):
+        sim.dispatch(bar.substeps)
+        orc.dispatch(bar.substeps)
+        assert_same(sim, orc, bar, f"bar frame {frame}")
+
+
 def test_tma_colour_pass_bit_exact(lib):
     """The TMA brick form of the large colour passes (vsim_set_tma_pass)
     leaves every node where the streaming form leaves it: a dense box whose

@@ -45,7 +45,8 @@ struct DeviceState {
 struct LaunchCtx {
     cudaStream_t stream;
     bool pdl;
-    uint32_t sms;  // multiprocessors of the device
+    uint32_t sms;            // multiprocessors of the device
+    bool quadCells = false;  // small dense colour passes split each cell over four lanes
 };
 
 // The items one launch covers. Dense (`table` null): [0, count), one thread

@@ -273,7 +273,7 @@ cudaError_t launchColourPass(const LaunchCtx& c, const vsim_sim* s, int col, boo
 // stepper.js:101-108 with simulator.js:83's constraint order.
 cudaError_t encodeFrame(vsim_sim* s, cudaStream_t st, uint32_t steps, ContactMode mode = ContactMode::Solve,
                         Profiler* prof = nullptr) {
-    const LaunchCtx c{st, s->pdl, s->sms};
+    const LaunchCtx c{st, s->pdl, s->sms, s->quadCells};
     const StretchLengths lens = stretchLengths();
     const bool limited = anyStretch(s);
     const bool driving = !s->held.empty();
@@ -336,6 +336,7 @@ uint64_t graphKey(const vsim_sim* s, uint32_t steps) {
     k = k * 31 + (s->plan.chunked ? 1 : 0);
     k = k * 31 + uint64_t(s->gatherMapping);
     k = k * 31 + (s->tma.enabled ? 1 : 0);
+    k = k * 31 + (s->quadCells ? 1 : 0);
     return k;
 }
 
@@ -715,6 +716,13 @@ int vsim_synchronize(vsim_sim* s) {
         CK(cudaMemcpy(&fault, s->tma.fault, 4, cudaMemcpyDeviceToHost), "synchronize");
         if (fault) return fail(VSIM_ERR_CUDA, "TMA colour pass: a block's copies did not arrive");
     }
+    return VSIM_OK;
+}
+
+int vsim_set_cell_lanes(vsim_sim* s, uint32_t lanes) {
+    SIM_GUARD(s);
+    if (lanes != 1 && lanes != 4) return fail(VSIM_ERR_RANGE, "lanes must be 1 or 4");
+    s->quadCells = lanes == 4;
     return VSIM_OK;
 }
 
@@ -1277,7 +1285,7 @@ int vsim_time_colour_passes(vsim_sim* s, uint32_t sweeps, float* ms) {
         cudaError_t e;
         if ((e = cudaMemcpyAsync(saved, s->d.pos, bytes, cudaMemcpyDeviceToDevice, s->stream))) return e;
         savedOk = true;
-        const LaunchCtx c{s->capture, s->pdl, s->sms};
+        const LaunchCtx c{s->capture, s->pdl, s->sms, s->quadCells};
         const StretchLengths lens = stretchLengths();
         if ((e = cudaStreamBeginCapture(s->capture, cudaStreamCaptureModeThreadLocal))) return e;
         cudaError_t enc = cudaSuccess;

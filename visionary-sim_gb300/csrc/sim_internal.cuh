@@ -130,6 +130,7 @@ struct vsim_sim {
     uint32_t* activePinned = nullptr;  // host staging of the activity and drive tables
     float4* grabsPinned = nullptr;
     vsim::TmaPass tma;
+    bool quadCells = false;  // small dense colour passes: four lanes a cell (vsim_set_cell_lanes)
 };
 
 namespace vsim {

@@ -200,6 +200,74 @@ __device__ __forceinline__ void solveCell(V (&p)[8], const V (&prev)[8], const f
     }
 }
 
+// projectTet with the cell split over the four lanes of a quad (lanes
+// 4k..4k+3 of a warp, `quad` their shuffle mask, q the lane's place): every
+// lane holds the cell and runs the tetrahedron's spine -- F, its norm, the
+// determinant, the gradient columns, the 2x2 solve -- as projectTet does;
+// lane q takes corner q's dot products and update, and the products reach
+// every lane for the reference's left-to-right chains. Same values, same
+// order: the result equals projectTet's bit for bit.
+template <int t>
+__device__ __forceinline__ void projectTetQuad(V (&p)[8], const V (&prev)[8], const float (&w)[8], float s, float ns,
+                                               float alphaDev, float alphaHyd, float gamma, float relax,
+                                               uint32_t q, uint32_t quad) {
+    constexpr int i0 = kTet(t, 0), i1 = kTet(t, 1), i2 = kTet(t, 2), i3 = kTet(t, 3);
+    const float w0 = w[i0], w1 = w[i1], w2 = w[i2], w3 = w[i3];
+    if (w0 + w1 + w2 + w3 == 0.0f) return;
+    const V base = p[i0];
+    const M F = timesB<t>(M{{p[i1] - base, p[i2] - base, p[i3] - base}}, s, ns);
+    const float cDev = sqrtf(dot(F.c[0], F.c[0]) + dot(F.c[1], F.c[1]) + dot(F.c[2], F.c[2]));
+    const float cHyd = determinant(F) - gamma;
+    const float inv = cDev > 1e-9f ? 1.0f / cDev : 0.0f;
+    const M mDev = timesBt<t>(F * inv, s, ns);
+    const M mHyd = timesBt<t>(M{{cross(F.c[1], F.c[2]), cross(F.c[2], F.c[0]), cross(F.c[0], F.c[1])}}, s, ns);
+    const V d1 = mDev.c[0], d2 = mDev.c[1], d3 = mDev.c[2];
+    const V d0 = -(d1 + d2 + d3);
+    const V h1 = mHyd.c[0], h2 = mHyd.c[1], h3 = mHyd.c[2];
+    const V h0 = -(h1 + h2 + h3);
+    auto pick = [&](V a0, V a1, V a2, V a3) { return q == 0 ? a0 : q == 1 ? a1 : q == 2 ? a2 : a3; };
+    const V d = pick(d0, d1, d2, d3), h = pick(h0, h1, h2, h3);
+    const V x = pick(p[i0], p[i1], p[i2], p[i3]) - pick(prev[i0], prev[i1], prev[i2], prev[i3]);
+    const float mine[5] = {dot(d, d), dot(d, h), dot(h, h), dot(d, x), dot(h, x)};
+    float e[5][4];
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) e[k][l] = __shfl_sync(quad, mine[k], l, 4);
+    const float gx = weighted4(w0, w1, w2, w3, e[0][0], e[0][1], e[0][2], e[0][3]);
+    const float gy = weighted4(w0, w1, w2, w3, e[1][0], e[1][1], e[1][2], e[1][3]);
+    const float gz = weighted4(w0, w1, w2, w3, e[2][0], e[2][1], e[2][2], e[2][3]);
+    const float rx = e[3][0] + e[3][1] + e[3][2] + e[3][3];
+    const float ry = e[4][0] + e[4][1] + e[4][2] + e[4][3];
+    float lx, ly;
+    couple(cDev, cHyd, alphaDev, alphaHyd, relax, rx, ry, gx, gy, gz, lx, ly);
+    const float wq = q == 0 ? w0 : q == 1 ? w1 : q == 2 ? w2 : w3;
+    const V moved_ = moved(pick(p[i0], p[i1], p[i2], p[i3]), d, h, lx, ly, wq);
+    auto from = [&](int l) {
+        return mk(__shfl_sync(quad, moved_.x, l, 4), __shfl_sync(quad, moved_.y, l, 4),
+                  __shfl_sync(quad, moved_.z, l, 4));
+    };
+    p[i0] = from(0);
+    p[i1] = from(1);
+    p[i2] = from(2);
+    p[i3] = from(3);
+}
+
+// solveCell<false> with the six tetrahedra split over a quad's lanes; the
+// stretch sweeps that follow run in every lane on the same values.
+__device__ __forceinline__ void solveCellQuad(V (&p)[8], const V (&prev)[8], const float (&w)[8],
+                                              const CellConsts& k, const StretchLengths& lens, uint32_t q,
+                                              uint32_t quad) {
+    const float s = k.restScale, ns = -s;
+    projectTetQuad<0>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax, q, quad);
+    projectTetQuad<1>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax, q, quad);
+    projectTetQuad<2>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax, q, quad);
+    projectTetQuad<3>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax, q, quad);
+    projectTetQuad<4>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax, q, quad);
+    projectTetQuad<5>(p, prev, w, s, ns, k.alphaDev, k.alphaHyd, k.gamma, k.relax, q, quad);
+    solveCell<true>(p, prev, w, k, lens);  // the stretch sweeps only
+}
+
 // The eight corner nodes of a cell entry (corner-0 node, body, y stride, z
 // stride), in corners.js order.
 __device__ __forceinline__ void cornerNodes(uint4 e, uint32_t (&ids)[8]) {

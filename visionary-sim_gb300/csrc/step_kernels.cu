@@ -72,6 +72,49 @@ __global__ void __launch_bounds__(512) elasticKernel(const uint4* __restrict__ c
     });
 }
 
+// The colour pass with each cell split over the four lanes of a quad
+// (solveCellQuad): four times the threads of elasticKernel, each running
+// the spine of the cell's chain and a quarter of its per-corner work. Dense
+// passes only (the cell list, not a chunk table); every lane loads the
+// cell, lane q stores corners q and q + 4.
+__global__ void __launch_bounds__(128) elasticQuadKernel(const uint4* __restrict__ cells, uint32_t count,
+                                                         const DevBody* __restrict__ bodies,
+                                                         const uint32_t* __restrict__ bodyActive,
+                                                         float4* __restrict__ pos,
+                                                         const float4* __restrict__ prevState, StretchLengths lens) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t slot = t >> 2, q = t & 3;
+    const uint32_t quad = 0xfu << (threadIdx.x & 28u);
+    const bool has = slot < count;
+    uint4 entry = make_uint4(0, 0, 0, 0);
+    uint32_t live = 0;
+    CellConsts k{};
+    if (has) {
+        entry = cells[slot];
+        live = bodyActive[entry.y];
+        k = cellConsts(bodies + entry.y);
+    }
+    pdlWait();
+    pdlLaunchNext();
+    if (!has || !live) return;  // the whole quad: its lanes share the cell
+    uint32_t ids[8];
+    cornerNodes(entry, ids);
+    V p[8], prev[8];
+    float w[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const float4 P = pos[ids[c]];
+        p[c] = xyz(P);
+        w[c] = P.w;
+    }
+#pragma unroll
+    for (int c = 0; c < 8; c++) prev[c] = xyz(prevState[ids[c]]);
+    solveCellQuad(p, prev, w, k, lens, q, quad);
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+        if ((c & 3) == int(q)) pos[ids[c]] = withW(p[c], w[c]);
+}
+
 // The colour pass for passes much larger than the GPU: each thread solves
 // cells in turn (grid-stride) and copies the next cell's eight positions and
 // eight previous positions into its slots of shared memory (cp.async) while
@@ -516,6 +559,9 @@ cudaError_t launchMarkDriven(cudaStream_t st, const uint32_t* driven, uint32_t n
 
 cudaError_t launchElastic(const LaunchCtx& c, const DeviceState& s, const uint4* cells, const Span& sp,
                           bool limitOnly, const StretchLengths& lens) {
+    if (c.quadCells && !limitOnly && !sp.work.table && !streamsColourPass(sp.work.count, c.sms))
+        return launch(c, elasticQuadKernel, blocks(4 * sp.work.count, 128), 128, cells, sp.work.count, s.bodies,
+                      (const uint32_t*)s.bodyActive, s.pos, (const float4*)s.prev, lens);
     if (!limitOnly && !sp.work.table && streamsColourPass(sp.work.count, c.sms))
         return launch(c, elasticStreamKernel, std::min(blocks(sp.work.count, kStreamBlock), kStreamBlocksPerSm * c.sms),
                       kStreamBlock,

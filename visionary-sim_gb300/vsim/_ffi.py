@@ -230,6 +230,7 @@ SIGNATURES = {
     "vsim_set_pdl": (C.c_int, [_P, C.c_int]),
     "vsim_set_gather_mapping": (C.c_int, [_P, C.c_int]),
     "vsim_set_tma_pass": (C.c_int, [_P, C.c_int]),
+    "vsim_set_cell_lanes": (C.c_int, [_P, C.c_uint32]),
     "vsim_grab": (C.c_int, [_P, _D, _D, C.c_int, C.c_double, C.POINTER(GrabResult)]),
     "vsim_time_colour_passes": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_float)]),
     "vsim_kuhn_rest_inverse": (C.c_int, [_F]),

@@ -285,6 +285,10 @@ class Simulator:
     def set_launch_shape(self, block: int, brick: int):
         check(lib().vsim_set_launch_shape(self._h, int(block), int(brick)))
 
+    def set_cell_lanes(self, lanes: int):
+        """Small colour passes with each cell over 1 or 4 lanes (vsim_set_cell_lanes)."""
+        check(lib().vsim_set_cell_lanes(self._h, int(lanes)))
+
     def set_tma_pass(self, enabled: bool):
         """Large colour passes through TMA brick tiles (vsim_set_tma_pass)."""
         check(lib().vsim_set_tma_pass(self._h, int(bool(enabled))))

@@ -290,6 +290,41 @@ def test_session_kernel_stretch_limit_and_engine_checks(lib):
     by_hand.destroy()
 
 
+def test_default_engine_on_the_serving_pool(lib):
+    """The serving workload's 64-session pool (noise blobs on 8^3-64^3 grids:
+    block, cluster and tick sessions under the default thresholds), settled
+    for 20 frames into self contact, then 200 seeded requests (k ~ U{1..4},
+    half dragging) arriving as a Poisson schedule: the session engine and
+    the frames engine leave every session's state equal bit for bit, and
+    the session engine's jobs pass their own checks."""
+    import vsim.scenes as sc
+    from vsim.server import Server
+
+    bodies, tank = sc.session_pool(64, seed=3)
+    rng = np.random.default_rng(21)
+    drags = [sc.drag_request(b, rng) for b in bodies]
+    arrivals = np.cumsum(rng.exponential(1 / 4000, 200))
+    sessions = rng.integers(0, 64, 200)
+    frames = rng.integers(1, 5, 200)
+    flags = (rng.random(200) < 0.5).astype(np.int64)
+    states = []
+    for engine in (Server.SESSIONS, Server.FRAMES):
+        server = Server(bodies, tank)
+        for q in range(64):
+            server.submit(q, 20)
+        while server.stats()["pending"]:
+            server.tick()
+        server.poll()
+        server.set_engine(engine)
+        done, report = server.run(arrivals, sessions, frames, flags, drags)
+        assert report["requests"] == 200 and report["frames"] == int(frames.sum())
+        states.append([server.read_state(q) for q in range(64)])
+        server.destroy()
+    for q in range(64):
+        for a, b, what in zip(states[0][q], states[1][q], ("pos", "prev", "vel")):
+            assert np.array_equal(a, b), f"session {q} {what}"
+
+
 def test_served_session_matches_oracle(lib):
     import pyoracle
     import vsim.scenes as sc

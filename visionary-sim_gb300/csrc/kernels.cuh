@@ -204,6 +204,17 @@ cudaError_t launchRefreshW(cudaStream_t st, uint32_t first, uint32_t n, const fl
 cudaError_t launchMergeXyz(cudaStream_t st, const float4* in, uint32_t n, float4* pos);
 cudaError_t launchDropW(cudaStream_t st, const float4* in, uint32_t n, float4* out);
 
+// Every contact entry in bucket order as canonRecord lays them out: its
+// record, its node's position, its motion over the substep with its body's
+// friction, its record index and its bucket.
+struct SortedEntries {
+    uint4* sMeta;
+    float4* sPos;
+    float4* sMoved;
+    uint32_t* sRec;
+    uint32_t* sKey;
+};
+
 // ---- TMA brick colour pass (colour_tma.cu) -----------------------------------
 
 constexpr uint32_t kTmaBodies = 4;   // bodies whose node arrays get tensor maps
@@ -286,7 +297,12 @@ struct SessionLaunch {
     StretchLengths lens;
 };
 
-cudaError_t launchSessions(cudaStream_t st, const DeviceState& d, const SessionLaunch& L);
+// `entries` and `sorted` are the session engine's own bucket-order arrays
+// (a job lays its runs out inside its session's record range, while a
+// tick running at the same time packs its runs from position 0 of the
+// simulator's).
+cudaError_t launchSessions(cudaStream_t st, const DeviceState& d, uint32_t* entries, const SortedEntries& sorted,
+                           const SessionLaunch& L);
 
 // ---- splats ---------------------------------------------------------------
 

@@ -110,6 +110,11 @@ struct SessionEngine {
     uint32_t* statusDev = nullptr;
     uint32_t* cursor = nullptr;    // per body, device
     uint32_t* fault = nullptr;     // per body, device
+    // The jobs' own bucket-order arrays, one slot per surface record: a job
+    // lays out its runs inside its session's record range, which a tick
+    // running alongside (its runs packed from position 0) must not touch.
+    uint32_t* entries = nullptr;
+    SortedEntries sorted{};
     uint32_t ticket = 0;
 };
 
@@ -226,6 +231,9 @@ void dropEngine(vsim_server* s) {
     freeMapped(reinterpret_cast<void*&>(e->status));
     if (e->cursor) cudaFree(e->cursor);
     if (e->fault) cudaFree(e->fault);
+    void* owned[] = {e->entries, e->sorted.sMeta, e->sorted.sPos, e->sorted.sMoved, e->sorted.sRec, e->sorted.sKey};
+    for (void* p : owned)
+        if (p) cudaFree(p);
     delete e;
     s->sessionEngine = nullptr;
 }
@@ -770,6 +778,13 @@ int buildEngine(vsim_server* s) {
     if (!e->doneDev || !e->statusDev) return fail(VSIM_ERR_CUDA, "map tickets");
     CK(cudaMalloc(reinterpret_cast<void**>(&e->cursor), bodies * 4), "allocate segment cursors");
     CK(cudaMalloc(reinterpret_cast<void**>(&e->fault), bodies * 4), "allocate job checks");
+    const size_t records = s->sim->surfaceCount;
+    CK(allocN(&e->entries, records), "allocate the jobs' bucket order");
+    CK(allocN(&e->sorted.sMeta, records), "allocate the jobs' bucket order");
+    CK(allocN(&e->sorted.sPos, records), "allocate the jobs' bucket order");
+    CK(allocN(&e->sorted.sMoved, records), "allocate the jobs' bucket order");
+    CK(allocN(&e->sorted.sRec, records), "allocate the jobs' bucket order");
+    CK(allocN(&e->sorted.sKey, records), "allocate the jobs' bucket order");
     // Session launches yield to the ticks' frames: each of those is a chain
     // of short dependent launches whose blocks should get SMs first.
     int least = 0, greatest = 0;
@@ -911,7 +926,7 @@ int launchReady(vsim_server* s, const std::vector<uint8_t>& inKernel, std::vecto
                        cudaMemcpyHostToDevice, l->stream),
        "upload job tables");
     CK(cudaEventRecord(l->start, l->stream), "launch sessions");
-    CK(launchSessions(l->stream, sim->d, L), "launch sessions");
+    CK(launchSessions(l->stream, sim->d, e->entries, e->sorted, L), "launch sessions");
     CK(cudaEventRecord(l->end, l->stream), "launch sessions");
     l->busy = true;
     l->launched = seconds(s);

@@ -254,11 +254,11 @@ __global__ void __launch_bounds__(kSessionBlock, 2) sessionKernel(SessionLaunch 
 
 }  // namespace
 
-cudaError_t launchSessions(cudaStream_t st, const DeviceState& d, const SessionLaunch& L) {
+cudaError_t launchSessions(cudaStream_t st, const DeviceState& d, uint32_t* entries, const SortedEntries& sorted,
+                           const SessionLaunch& L) {
     if (L.groupCount == 0) return cudaSuccess;
-    const SessionArrays a{d.fp,    d.bodies, d.cells,   d.active, d.nodeRecord, d.baseW, d.surf,
-                          d.pos,   d.prev,   d.vel,     d.key,    d.rank,       d.entries, d.count,
-                          d.start, d.delta,  SortedEntries{d.sMeta, d.sPos, d.sMoved, d.sRec, d.sKey}};
+    const SessionArrays a{d.fp,  d.bodies, d.cells, d.active, d.nodeRecord, d.baseW, d.surf,  d.pos, d.prev,
+                          d.vel, d.key,    d.rank,  entries,  d.count,      d.start, d.delta, sorted};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(L.groupCount * kSessionCluster);
     cfg.blockDim = dim3(kSessionBlock);

@@ -524,16 +524,6 @@ __device__ __forceinline__ void binRecord(uint32_t r, uint4 rec, const DevBody* 
     rank[r] = atomicAdd(&count[b], 1u);
 }
 
-// The bucket arrays, and every entry in bucket order as canonRecord lays
-// them out: its record, its node's position, its motion over the substep
-// with its body's friction, its record index and its bucket.
-struct SortedEntries {
-    uint4* sMeta;
-    float4* sPos;
-    float4* sMoved;
-    uint32_t* sRec;
-    uint32_t* sKey;
-};
 
 struct ContactArrays {
     const DevBody* bodies;

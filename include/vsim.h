@@ -579,7 +579,10 @@ int vsim_server_run(vsim_server* server, const vsim_scheduled_request* requests,
    request and none running starts in the next launch, launches overlap,
    and a request completes when its own job ends. Larger sessions run in
    ticks of shared frames on the server's stream at the same time. Every
-   engine gives every session the same result, bit for bit. */
+   engine gives every session the same result, bit for bit. The session
+   engine, once used, keeps its own contact arrays (60 B a surface record
+   of the resident pool, outside the admission budget) until the resident
+   set changes or the server is destroyed. */
 #define VSIM_SERVE_FRAMES 0
 #define VSIM_SERVE_SESSIONS 1
 int vsim_server_set_engine(vsim_server* server, int engine, uint32_t block_cells, uint32_t cluster_cells);

@@ -781,6 +781,14 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
     def specs(count):
         return rng.integers(1, 5, count), rng.random(count) < 0.5
 
+    def widest_colour(b):
+        occ = np.asarray(b.occupancy).reshape(b.cell_dims[2], b.cell_dims[1], b.cell_dims[0])
+        k, j, i = np.nonzero(occ)
+        return int(np.bincount((i & 1) | ((j & 1) << 1) | ((k & 1) << 2), minlength=8).max())
+
+    widest = np.array([widest_colour(b) for b in bodies])
+    engine_shape = {"block": 0, "cluster": 0}
+
     def saturation():
         restore()
         frames, flags = specs(200_000)
@@ -807,6 +815,14 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
         st_after = server.stats()
         lat = np.array([(c["completed"] - c["submitted"]) / c["frames"] for c in done])
         req_lat = np.array([c["completed"] - c["submitted"] for c in done])
+        # p99 by where the session runs under the session engine's thresholds
+        kernel_limit = max(engine_shape["block"], engine_shape["cluster"])
+        in_kernel = np.array([widest[c["session"]] <= kernel_limit for c in done])
+        by_class = {}
+        for name, sel in (("kernel", in_kernel), ("ticks", ~in_kernel)):
+            if sel.any():
+                by_class[name] = {"requests": int(sel.sum()),
+                                  "p99": round(1e3 * float(np.percentile(lat[sel], 99)), 3)}
         ticks_run = max(1, st_after["ticks"] - st_before["ticks"])
         tick_ms = {k: round(1e3 * (st_after[f"{k}_seconds"] - st_before[f"{k}_seconds"]) / ticks_run, 3)
                    for k in ("tick", "prepare", "frame")}
@@ -816,6 +832,7 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
                 "request_latency_ms": {"p50": round(1e3 * float(np.percentile(req_lat, 50)), 3),
                                        "p99": round(1e3 * float(np.percentile(req_lat, 99)), 3)},
                 "requests": len(lat),
+                "frame_latency_p99_by_class_ms": by_class,
                 "sessions_per_tick": round((st_after["session_frames"] - st_before["session_frames"]) / ticks_run, 1),
                 "mean_tick_ms": tick_ms,
                 "cell_updates_per_s": round((st_after["cell_updates"] - st_before["cell_updates"]) / rep["seconds"])}
@@ -852,12 +869,14 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
             shapes = [(b, c) for b in block_cells for c in cluster_cells]
             for cells, wide in shapes:
                 server.set_engine(server.SESSIONS, cells, wide)
+                engine_shape.update(block=cells, cluster=wide)
                 restore()
                 key = engine if len(shapes) == 1 else f"{engine}_block{cells}_cluster{wide}"
                 by_engine[key] = {"block_cells": cells, "cluster_cells": wide, "one_request_floor": floors(engine),
                                   **sweep()}
         else:
             server.set_engine(server.FRAMES)
+            engine_shape.update(block=0, cluster=0)
             restore()
             by_engine[engine] = {"one_request_floor": floors(engine)}
             runs = {}

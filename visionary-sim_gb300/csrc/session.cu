@@ -167,8 +167,10 @@ __device__ __forceinline__ void runJob(const SessionJob& job, const SessionLaunc
                     }
                 }
                 sync();
+                // The runs must add up to the session's records; checked
+                // here, seen by every thread after the scatter's barrier.
+                // The scatter guards each of its own writes meanwhile.
                 if (tid == 0 && *static_cast<volatile uint32_t*>(L.cursor + body) != records) *fault = kFaultRecords;
-                sync();
                 bool ok = !failed();
                 for (uint32_t i = tid; ok && i < records; i += threads) {
                     const uint32_t r = first + i;

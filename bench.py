@@ -866,14 +866,16 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
     by_engine = {}
     for engine in engines:
         if engine == "sessions":
-            shapes = [(b, c) for b in block_cells for c in cluster_cells]
-            for cells, wide in shapes:
+            shapes = [(b, c, t) for b in block_cells for c in cluster_cells for t in budgets]
+            for cells, wide, budget in shapes:
                 server.set_engine(server.SESSIONS, cells, wide)
+                server.set_tick_budget(budget)
                 engine_shape.update(block=cells, cluster=wide)
                 restore()
-                key = engine if len(shapes) == 1 else f"{engine}_block{cells}_cluster{wide}"
-                by_engine[key] = {"block_cells": cells, "cluster_cells": wide, "one_request_floor": floors(engine),
-                                  **sweep()}
+                key = engine if len(shapes) == 1 else f"{engine}_block{cells}_cluster{wide}_budget{budget}"
+                by_engine[key] = {"block_cells": cells, "cluster_cells": wide, "tick_cell_budget": budget,
+                                  "one_request_floor": floors(engine), **sweep()}
+            server.set_tick_budget(0)
         else:
             server.set_engine(server.FRAMES)
             engine_shape.update(block=0, cluster=0)

@@ -617,8 +617,11 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& 
         return e;
     if ((e = mark(4))) return e;
     // The gather runs over the bucket-ordered entries (at most recordItems),
-    // a warp each while fewer than 2048 per SM, else a thread each.
-    const uint32_t cg = std::min(blocks(recordItems, 8), 64 * c.sms);
+    // a warp each while fewer than 2048 per SM, else a thread each, on one
+    // resident wave of blocks (five an SM at its launch bounds) that loop
+    // over the records: on the headline body 32.8 against 34.8 us for a
+    // block per eight records.
+    const uint32_t cg = std::min(blocks(recordItems, 8), 5 * c.sms);
     const uint32_t warpModeBelow = mapping == VSIM_GATHER_WARP     ? 0xffffffffu
                                    : mapping == VSIM_GATHER_THREAD ? 0u
                                                                    : 2048 * c.sms;

@@ -617,11 +617,14 @@ cudaError_t launchContact(const LaunchCtx& c, const DeviceState& s, const Span& 
         return e;
     if ((e = mark(4))) return e;
     // The gather runs over the bucket-ordered entries (at most recordItems),
-    // a warp each while fewer than 2048 per SM, else a thread each, on one
-    // resident wave of blocks (five an SM at its launch bounds) that loop
-    // over the records: on the headline body 32.8 against 34.8 us for a
-    // block per eight records.
-    const uint32_t cg = std::min(blocks(recordItems, 8), 5 * c.sms);
+    // a warp each while fewer than 2048 per SM, else a thread each. Over one
+    // body (a dense span) one resident wave of blocks (five an SM at its
+    // launch bounds) loops over the records: on the headline body 32.8
+    // against 34.8 us for a block per eight records. Over many isolated
+    // bodies (a chunked span: settled sessions whose records' candidate
+    // counts vary widely) a block per eight records keeps the SMs balanced:
+    // the looping wave cut the serving pool's saturation by 7 %.
+    const uint32_t cg = std::min(blocks(recordItems, 8), (r.work.table ? 64u : 5u) * c.sms);
     const uint32_t warpModeBelow = mapping == VSIM_GATHER_WARP     ? 0xffffffffu
                                    : mapping == VSIM_GATHER_THREAD ? 0u
                                                                    : 2048 * c.sms;

@@ -20,14 +20,16 @@
 // are skipped by every kernel. So a request's result is the same whether it
 // ran alone or among others.
 //
-// The request loop (vsim_server_run) has a second engine: session kernels
-// (session.cu). There a request is a job -- its session's frames, all of
-// them, run by one block or one cluster -- and the loop launches every
-// ready request as soon as one of a few launch slots is free, without
-// waiting for requests already running; each job reports its end through a
-// ticket in host-mapped memory, so a short request is retired when it ends,
-// not when its launch does. The explicit tick (vsim_server_tick) stays the
-// frame-at-a-time engine above; both give every session the same result.
+// The request loop (vsim_server_run) has a second engine, the default: for
+// sessions small enough, session kernels (session.cu). There a request is
+// a job -- its session's frames, all of them, run by one block or one
+// cluster -- and the loop launches every ready request as soon as one of a
+// few launch slots is free, without waiting for requests already running;
+// each job reports its end through a ticket in host-mapped memory, so a
+// short request is retired when it ends, not when its launch does. The
+// larger sessions run as ticks of shared frames at the same time. The
+// explicit tick (vsim_server_tick) stays the frame-at-a-time engine above;
+// every engine gives every session the same result.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -208,7 +210,7 @@ void dropSim(vsim_sim*& sim) {
     sim = nullptr;
 }
 
-void freeMapped(void*& p) {
+void freePinned(void*& p) {
     if (p) cudaFreeHost(p);
     p = nullptr;
 }
@@ -224,11 +226,11 @@ void dropEngine(vsim_server* s) {
         }
         if (l.start) cudaEventDestroy(l.start);
         if (l.end) cudaEventDestroy(l.end);
-        freeMapped(reinterpret_cast<void*&>(l.staging));
+        freePinned(reinterpret_cast<void*&>(l.staging));
         if (l.tables) cudaFree(l.tables);
     }
-    freeMapped(reinterpret_cast<void*&>(e->done));
-    freeMapped(reinterpret_cast<void*&>(e->status));
+    freePinned(reinterpret_cast<void*&>(e->done));
+    freePinned(reinterpret_cast<void*&>(e->status));
     if (e->cursor) cudaFree(e->cursor);
     if (e->fault) cudaFree(e->fault);
     void* owned[] = {e->entries, e->sorted.sMeta, e->sorted.sPos, e->sorted.sMoved, e->sorted.sRec, e->sorted.sKey};

@@ -142,6 +142,8 @@ struct Span {
     Work work;
     uint32_t grid;
     uint32_t block;
+    // Records spans over chunk tables: blocks an SM of the contact gather.
+    uint32_t gatherPerSm = 64;
 };
 
 // Chunks of at most kChunk items per block.

@@ -221,6 +221,11 @@ int planBodies(vsim_sim* s, const std::vector<uint32_t>& bodies) {
     if (!ok) return fail(VSIM_ERR_CAPACITY, "chunk table too small (a body listed twice?)");
     CK(cudaMemcpyAsync(s->chunkDev, table, (kSpans + at) * sizeof(uint2), cudaMemcpyHostToDevice, s->stream),
        "upload work chunks");
+    // The gather's grid for this frame's records: small frames take fewer,
+    // looping blocks (a second captured graph serves them).
+    uint64_t records = 0;
+    for (uint32_t b : bodies) records += s->recordBodyStart[b + 1] - s->recordBodyStart[b];
+    s->chunked.records.gatherPerSm = records <= (1u << 18) ? 16 : 64;
     s->plan = s->chunked;
     return VSIM_OK;
 }
@@ -337,6 +342,7 @@ uint64_t graphKey(const vsim_sim* s, uint32_t steps) {
     k = k * 31 + uint64_t(s->gatherMapping);
     k = k * 31 + (s->tma.enabled ? 1 : 0);
     k = k * 31 + (s->quadCells ? 1 : 0);
+    k = k * 131 + s->plan.records.gatherPerSm;
     return k;
 }
 

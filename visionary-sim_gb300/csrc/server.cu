@@ -791,10 +791,17 @@ int buildEngine(vsim_server* s) {
     // of short dependent launches whose blocks should get SMs first.
     int least = 0, greatest = 0;
     CK(cudaDeviceGetStreamPriorityRange(&least, &greatest), "query stream priorities");
+    // Every slot sized up front for a launch of every resident session (and
+    // four drag frames each): growing one later frees device memory, which
+    // waits for every kernel in flight.
+    const size_t jobs = std::max<size_t>(1, s->resident.size());
+    const size_t tableBytes = align16(jobs * sizeof(SessionGroup)) + align16(jobs * sizeof(SessionJob)) +
+                              2 * 4 * jobs * sizeof(float4);
     for (LaunchSlot& l : e->slot) {
         CK(cudaStreamCreateWithPriority(&l.stream, cudaStreamNonBlocking, least), "create launch stream");
         CK(cudaEventCreate(&l.start), "create launch event");
         CK(cudaEventCreate(&l.end), "create launch event");
+        if (int rc = growTables(l, tableBytes)) return rc;
     }
     return VSIM_OK;
 }

@@ -37,6 +37,11 @@ import tempfile
 import time
 from pathlib import Path
 
+# One hardware queue per stream for the server's request loop (the vsim
+# package sets the same default; here it is set before anything can create
+# the CUDA context).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 import numpy as np
 
 ROOT = Path(__file__).resolve().parent
@@ -894,6 +899,7 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
                         f"{st['resident_bytes'] / 1e9:.2f} GB of the 150 GB budget; k ~ U{{1..4}} frames, "
                         f"50% with a Bezier drag at 0.5 m/s",
             "by_engine": by_engine, "settle": {"frames": settle_frames, "seconds": round(settle_s, 1)},
+            "hardware_queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS", "8 (driver default)"),
             "pool_generation_s": round(gen_s, 1)}
 
 

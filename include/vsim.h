@@ -582,7 +582,14 @@ int vsim_server_run(vsim_server* server, const vsim_scheduled_request* requests,
    engine gives every session the same result, bit for bit. The session
    engine, once used, keeps its own contact arrays (60 B a surface record
    of the resident pool, outside the admission budget) until the resident
-   set changes or the server is destroyed. */
+   set changes or the server is destroyed. The session engine keeps ten
+   streams busy (eight launch slots, the pool's stream and its capture
+   stream); the CUDA driver feeds streams to the GPU through
+   CUDA_DEVICE_MAX_CONNECTIONS hardware queues (8 unless set), and where a
+   slot shares the pool stream's queue the ticks wait behind session jobs.
+   Set CUDA_DEVICE_MAX_CONNECTIONS=32 in the environment before the
+   process's first CUDA call (the Python package sets it when imported
+   first, unless already set). */
 #define VSIM_SERVE_FRAMES 0
 #define VSIM_SERVE_SESSIONS 1
 int vsim_server_set_engine(vsim_server* server, int engine, uint32_t block_cells, uint32_t cluster_cells);

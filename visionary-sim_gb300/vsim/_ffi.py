@@ -6,8 +6,20 @@ fallback path.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import re
 from pathlib import Path
+
+# The server's request loop keeps up to ten streams busy at once (eight
+# session launch slots, the pool's stream, its capture stream). The CUDA
+# driver feeds streams to the GPU through CUDA_DEVICE_MAX_CONNECTIONS hardware
+# queues, eight unless set, assigned in turn as streams are created: with
+# eight, a slot's stream shares the pool stream's queue, and a tick's
+# launches wait behind a session job of several milliseconds queued ahead of
+# them. 32 (the most the driver takes) gives every stream its own queue. The
+# driver reads the variable when the process creates its CUDA context, so it
+# acts only if nothing has touched CUDA yet; a value the caller set is kept.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 LIB_PATH = Path(__file__).resolve().parent / "libvsim.so"
 HEADER = Path(__file__).resolve().parents[2] / "include" / "vsim.h"

@@ -494,6 +494,11 @@ typedef struct vsim_server_stats {
     double frame_seconds;     /* device time of the frames (CUDA events), summed */
 } vsim_server_stats;
 
+/* `stream` (a cudaStream_t, or NULL): the stream the ticks run on. NULL: the
+   server makes its own at the device's greatest priority, so that a tick's
+   launches start before the session engine's, whose streams are made at
+   the least; a stream given should have a priority above the least too
+   (cudaStreamCreateWithPriority). */
 int vsim_server_create(const vsim_body_desc* sessions, uint32_t count, const vsim_tank* tank,
                        const vsim_server_config* config, void* stream, vsim_server** out);
 int vsim_server_destroy(vsim_server* server);

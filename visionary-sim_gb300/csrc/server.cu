@@ -127,6 +127,8 @@ struct vsim_server {
     vsim_tank world{};
     vsim_server_config config{};
     void* stream = nullptr;
+    bool ownStream = false;  // made by the server (none given): destroyed with it
+    int streamDevice = 0;
     std::vector<Session> sessions;
     std::vector<uint32_t> resident;  // session of each body of `sim`
     std::vector<int32_t> slot;       // body of each session in `sim`, -1 when not resident
@@ -252,6 +254,10 @@ int destroyServer(vsim_server* s) {
         if (s->frameDone) cudaEventDestroy(s->frameDone);
     }
     dropSim(s->sim);
+    if (s->ownStream) {
+        DeviceGuard guard(s->streamDevice);
+        cudaStreamDestroy(static_cast<cudaStream_t>(s->stream));
+    }
     delete s;
     return VSIM_OK;
 }
@@ -303,6 +309,22 @@ int vsim_server_create(const vsim_body_desc* sessions, uint32_t count, const vsi
     if (!s) return fail(VSIM_ERR_NOMEM, "out of host memory");
     s->config = *config;
     s->stream = stream;
+    if (!stream) {
+        // The ticks' stream at the device's greatest priority. The session
+        // engine's launch slots are made at its least, which is also the
+        // priority of a stream made without one: blocks of a tick waiting
+        // to start then go before those of a session launch.
+        int least = 0, greatest = 0;
+        cudaStream_t own = nullptr;
+        if (cudaGetDevice(&s->streamDevice) != cudaSuccess ||
+            cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&own, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+            delete s;
+            return fail(VSIM_ERR_CUDA, "create the server's stream");
+        }
+        s->stream = own;
+        s->ownStream = true;
+    }
     for (int a = 0; a < 3; a++) {
         s->world.min[a] = tank ? tank->min[a] : -INFINITY;
         s->world.max[a] = tank ? tank->max[a] : INFINITY;

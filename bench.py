@@ -745,7 +745,8 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
     session mix), then Poisson arrivals
     at 25/50/70/90 % of that saturation, the 70 % point `repeats_at_70`
     times, each run by vsim_server_run against a pre-drawn schedule, so no
-    client code sits between launches. Each of these starts from the same
+    client code sits between launches, after half a second of the same
+    load that is not measured. Each of these starts from the same
     settled state (every session checkpointed after the settling frames and
     written back before the measurement). Frame latency of a request =
     (completion - scheduled arrival) / k."""
@@ -807,14 +808,21 @@ def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, set
                 "method": "closed loop in the library's request loop (vsim_server_run): as many requests "
                           "outstanding as sessions, each completion replaced by one to a uniformly drawn session"}
 
-    def point(frac, sat_rate):
-        restore()
-        lam = frac * sat_rate
-        gaps = rng.exponential(1 / lam, int(lam * seconds_per_point * 1.5) + 16)
-        arrivals = np.cumsum(gaps)
-        arrivals = arrivals[arrivals < seconds_per_point]
+    def schedule(lam, seconds):
+        arrivals = np.cumsum(rng.exponential(1 / lam, int(lam * seconds * 1.5) + 16))
+        arrivals = arrivals[arrivals < seconds]
         sessions = rng.integers(0, admitted, arrivals.size)
         frames, flags = specs(arrivals.size)
+        return arrivals, sessions, frames, flags
+
+    def point(frac, sat_rate):
+        lam = frac * sat_rate
+        # warm-up: half a second at the same rate, not measured, then the
+        # settled state again
+        restore()
+        server.run(*schedule(lam, 0.5), drags)
+        restore()
+        arrivals, sessions, frames, flags = schedule(lam, seconds_per_point)
         st_before = server.stats()
         done, rep = server.run(arrivals, sessions, frames, flags, drags)
         st_after = server.stats()

@@ -726,7 +726,7 @@ def drift(frames: int = 300):
             "final_max_abs_m": float(np.max(np.abs(g - r)))}
 
 
-def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 3.0, settle_frames: int = 30,
+def serving_sweep(quick: bool, budgets=(0,), seconds_per_point: float = 5.0, settle_frames: int = 30,
                   repeats_at_70: int = 3, engines=("sessions", "frames"), block_cells=(32,), cluster_cells=(512,)):
     """Continuous batching under load: a pool of sessions resident on the
     GPU; requests advance a session k ~ U{1..4} frames, half of them dragging

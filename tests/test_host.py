@@ -252,3 +252,23 @@ def test_sort_entry_points_reject_bad_arguments(vsimlib):
     assert sort(None, order, 10, 32, temp, C.byref(need), None) == inv
     assert sort(keys, keys + 4, 10, 32, temp, C.byref(need), None) == inv
     assert b"overlap" in lib.vsim_last_error()
+
+
+def test_package_gives_each_stream_a_hardware_queue():
+    """Importing the package asks the CUDA driver for 32 hardware queues (the
+    serving engine keeps ten streams busy; with the default eight a launch
+    slot shares the ticks' queue) and keeps a value the caller set."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    pkg = str(Path(__file__).resolve().parent.parent / "visionary-sim_gb300")
+    code = "import os, vsim._ffi; print(os.environ['CUDA_DEVICE_MAX_CONNECTIONS'])"
+    env = {k: v for k, v in os.environ.items() if k != "CUDA_DEVICE_MAX_CONNECTIONS"}
+    env["PYTHONPATH"] = pkg + os.pathsep + env.get("PYTHONPATH", "")
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, check=True)
+    assert out.stdout.strip() == "32"
+    env["CUDA_DEVICE_MAX_CONNECTIONS"] = "1"
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, check=True)
+    assert out.stdout.strip() == "1"

@@ -260,6 +260,41 @@ def test_engines_give_the_same_result(lib, engine, block_cells, cluster_cells):
         srv.destroy()
 
 
+def test_server_on_a_caller_stream(lib):
+    """A server given the caller's stream (vsim_server_create's `stream`)
+    runs its ticks there -- the session engine's launch slots on their own
+    streams as always -- and leaves every session where a server on a stream
+    of its own (made at the device's greatest priority) leaves it; the
+    caller's stream outlives the server."""
+    import torch
+    import vsim.scenes as sc
+    from vsim.server import Server
+
+    bodies, tank = small_pool(7, seed=41)
+    rng = np.random.default_rng(9)
+    drags = [sc.drag_request(b, rng) for b in bodies]
+    arrivals = np.array([0.0, 0.0, 0.0001, 0.0002, 0.0003, 0.0004, 0.0005, 0.002])
+    sessions = np.array([0, 1, 2, 3, 4, 5, 6, 0])
+    frames = np.array([3, 1, 2, 4, 1, 2, 3, 2])
+    flags = np.array([1, 0, 1, 1, 0, 0, 1, 0])
+    caller = torch.cuda.Stream()
+    states = []
+    for stream in (None, caller.cuda_stream):
+        server = Server(bodies, tank, stream=stream)
+        server.set_engine(1, 60, 120)  # blocks, clusters and ticks side by side
+        _, report = server.run(arrivals, sessions, frames, flags, drags)
+        assert report["requests"] == len(frames)
+        states.append([server.read_state(q) for q in range(7)])
+        server.destroy()
+    for q in range(7):
+        for a, b in zip(states[0][q], states[1][q]):
+            assert np.array_equal(a, b), f"session {q}"
+    with torch.cuda.stream(caller):
+        x = torch.ones(4, device="cuda") * 2
+    caller.synchronize()
+    assert float(x.sum()) == 8.0
+
+
 def test_session_kernel_stretch_limit_and_engine_checks(lib):
     """Sessions whose material limits stretch (maxStretch > 1: three limit-only
     sweeps of the eight colours every substep) leave the session kernel --
